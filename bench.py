@@ -1,0 +1,314 @@
+"""Render-throughput benchmark of the nerf-tf2 render path on GB300.
+
+One step = one full 800x800 pinhole frame (640,000 rays) rendered
+hierarchically in 4096-ray chunks with 64 coarse + 128 fine samples per ray
+(the reference's render loop, nerf/main/render.py:79-93 with
+base_dataset.py:797-861), random-init coarse and fine networks, synthetic
+camera on the radius-4 sphere.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--path bf16|fp32]
+    python bench.py --impl reference ...   # the reference algorithm on host cores
+
+Prints one JSON line (rank 0). `value` is whole-job rays/s with rays resident
+in HBM; `e2e` is the same through NeRF.render with the rays in pinned host
+memory and the rgb/depth/acc maps copied back every step.
+"""
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rays/s coarse+fine render, BF16+proposal vs plain FP32, at ≤0.1 dB PSNR gap"
+H = W = 800
+FOCAL = 1111.111
+CHUNK = 4096
+SC, SF = 64, 128
+FLOP_PER_SAMPLE = 1186816          # 2 x 593,408 MAC of the 8x256 MLP + heads
+L2_FLUSH_BYTES = 512 << 20         # > 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--path", default="bf16", choices=["bf16", "fp32"])
+    ap.add_argument("--plain-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)),
+            int(os.environ.get("WORLD_SIZE", 1)))
+
+
+# ---------------------------------------------------------------------------
+# CPU side: the oracle restatement of the reference algorithm
+# ---------------------------------------------------------------------------
+def cpu_render_rate(ng, frame, seconds, max_rays=4096, block=128):
+    """Times the oracle's FP32 hierarchical render on consecutive 128-ray
+    blocks of the frame until `seconds` elapse. Returns (rays/s, rays)."""
+    oracle = importlib.import_module("oracle")
+    o, d, n, f = frame
+    p = ng.make_params()
+    pc = oracle.unpack_params(ng.weights.glorot_blob(0))
+    pf = oracle.unpack_params(ng.weights.glorot_blob(1))
+    rng = np.random.default_rng(0)
+    done, t0 = 0, time.perf_counter()
+    while done < max_rays and (time.perf_counter() - t0) < seconds:
+        s = slice(done, done + block)
+        uc = rng.random((block, SC), dtype=np.float32)
+        uf = rng.random((block, SF), dtype=np.float32)
+        oracle.nerf_forward(p, pc, pf, o[s], d[s], n[s], f[s], uc, uf, np.float32)
+        done += block
+    return done / (time.perf_counter() - t0), done
+
+
+def reference_arm(args):
+    rank, _, world = dist_env()
+    if rank != 0:
+        return
+    ng = importlib.import_module("nerf-tf2_gb300")
+    frame = ng.synthetic.frame_rays(0, H, W, FOCAL)
+    cores = os.cpu_count()
+    per_step = 256
+    for _ in range(args.warmup):
+        cpu_render_rate(ng, frame, 1e9, max_rays=per_step)
+    rates = [cpu_render_rate(ng, frame, 1e9, max_rays=per_step)[0] for _ in range(args.steps)]
+    rate = statistics.mean(rates)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": "rays/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * per_step / rate,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
+        "data": "synthetic",
+        "config": {"workload": "800x800 frame, 4096-ray chunks, 64 coarse + 128 fine, random-init "
+                               "8x256 MLPs", "sample_rays_per_step": per_step},
+        "cpu_baseline": {"value": rate, "unit": "rays/s", "cores": cores, "kind": "port",
+                         "sample": f"{per_step} rays of the frame per step; numpy FP32 restatement "
+                                   "(TensorFlow 2.6 is not installable here), OpenBLAS on all cores"},
+        "e2e": {"value": rate, "unit": "rays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU side
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+    Q = ("index,pci.bus_id,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, bus_id=None):
+        self.bus_id = (bus_id or "").lower()
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.rows = []
+        if self.proc is None:
+            return
+        self.proc.terminate()
+        out, _ = self.proc.communicate(timeout=10)
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 10:
+                continue
+            if self.bus_id and self.bus_id[-12:] not in parts[1].lower():
+                continue
+            self.rows.append(parts)
+
+    def summary(self):
+        if not getattr(self, "rows", None):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        mx = [float(r[3]) for r in self.rows if r[3].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[6 + i] == "Active"})
+        loaded = [s for s in sm if mx and s > 0.5 * max(mx)] or sm
+        return {"sm_mhz": statistics.median(loaded) if loaded else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(self.rows)}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return reference_arm(args)
+    import torch
+    import torch.distributed as tdist
+
+    rank, local_rank, world = dist_env()
+    torch.cuda.set_device(local_rank)
+    if world > 1:
+        tdist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    def barrier():
+        if world > 1:
+            tdist.barrier()
+
+    ng = importlib.import_module("nerf-tf2_gb300")
+    dev = torch.device("cuda", local_rank)
+    params = ng.make_params(N_coarse=SC, N_fine=SF)
+    # weak scaling: every rank renders its own frame (camera seed = rank)
+    frame = ng.synthetic.frame_rays(rank, H, W, FOCAL)
+    R = frame[0].shape[0]
+    host = [torch.from_numpy(x).pin_memory() for x in frame]
+    rays = [h.to(dev) for h in host]
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    nerf = ng.NeRF(params, precision=args.path, seed=0)
+    nerf_plain = ng.NeRF(params, precision="fp32", seed=0)
+    launches_per_chunk = 8  # 2 Philox, coarse sample, MLP, composite, fine sample, MLP, composite
+    n_chunks = (R + CHUNK - 1) // CHUNK
+
+    def timed_steps(fn, steps, warmup):
+        for i in range(warmup):
+            fn(i)
+        torch.cuda.synchronize()
+        times = []
+        for i in range(steps):
+            flush.zero_()
+            barrier()
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn(warmup + i)
+            e1.record()
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1))
+        t = torch.tensor([sum(times)], device=dev, dtype=torch.float64)
+        if world > 1:
+            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        return float(t.item()) / steps, times
+
+    # device-resident throughput
+    def step(i):
+        nerf.render(*rays, chunk=CHUNK, seed=1000 * i)
+    bus = getattr(torch.cuda.get_device_properties(dev), "pci_bus_id", None)
+    with ClockSampler(str(bus) if bus is not None else None) as clk:
+        ms, _ = timed_steps(step, args.steps, args.warmup)
+    value = world * R / (ms / 1000.0)
+
+    # end to end: pinned host rays in, maps out, through the public API
+    out_host = {k: torch.empty((R, 3) if k == "rgb" else (R,), pin_memory=True)
+                for k in ("rgb", "depth", "acc")}
+
+    def e2e_step(i):
+        dr = [h.to(dev, non_blocking=True) for h in host]
+        out = nerf.render(*dr, chunk=CHUNK, seed=1000 * i)
+        for k in out_host:
+            out_host[k].copy_(out[k], non_blocking=True)
+    e2e_ms, _ = timed_steps(e2e_step, max(2, args.steps // 2), 1)
+    h2d = sum(h.numel() * h.element_size() for h in host)
+    d2h = sum(v.numel() * v.element_size() for v in out_host.values())
+
+    # plain FP32 path (the 20x denominator) and the image gap against it
+    if args.path != "fp32":
+        plain_ms, _ = timed_steps(lambda i: nerf_plain.render(*rays, chunk=CHUNK, seed=1000 * i),
+                                  args.plain_steps, 1)
+        img_fast = nerf.render(*rays, chunk=CHUNK, seed=7)["rgb"]
+        img_plain = nerf_plain.render(*rays, chunk=CHUNK, seed=7)["rgb"]
+        psnr_vs_plain = ng.psnr(img_plain, img_fast)
+        max_abs_vs_plain = float((img_plain - img_fast).abs().max())
+    else:
+        plain_ms, psnr_vs_plain, max_abs_vs_plain = ms, float("inf"), 0.0
+    plain_value = world * R / (plain_ms / 1000.0)
+
+    # roofline of the dominant kernel (the MLP) at the fine-pass launch shape
+    rows = CHUNK * (SC + SF)
+    xyz = (torch.rand(rows, 3, device=dev) * 4 - 2)
+    dirs = torch.nn.functional.normalize(torch.randn(CHUNK, 3, device=dev), dim=1)
+    mlp = nerf.fine_model
+    for _ in range(3):
+        mlp((xyz, dirs), rows_per_dir=SC + SF)
+    kt = []
+    for _ in range(5):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        mlp((xyz, dirs), rows_per_dir=SC + SF)
+        e1.record()
+        torch.cuda.synchronize()
+        kt.append(e0.elapsed_time(e1))
+    mlp.check_device_errors()
+    k_ms = statistics.median(kt)
+    peaks = {}
+    pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk_path):
+        peaks = json.load(open(pk_path))
+    achieved = rows * FLOP_PER_SAMPLE / (k_ms / 1000.0) / 1e12
+    if args.path == "bf16":
+        peak, src = peaks.get("bf16_tflops"), "measured bf16 burst (MEASURED_PEAKS.json)"
+        if peak is None:
+            peak, src = 1900.0, "fallback 1.9 PFLOP/s bf16"
+        bound = "tensor"
+    else:
+        clk_max = peaks.get("sm_max_mhz", 2070.0)
+        sms = torch.cuda.get_device_properties(dev).multi_processor_count
+        peak = sms * 128 * 2 * clk_max * 1e6 / 1e12
+        src = f"FP32 FMA issue peak: {sms} SMs x 128 FMA/clk x {clk_max:.0f} MHz"
+        bound = "fp32-simt"
+    traffic = None
+    tr_path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(tr_path):
+        traffic = json.load(open(tr_path)).get(f"mlp_{args.path}_fine_chunk_bytes")
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        rate, nr = cpu_render_rate(ng, frame, args.cpu_seconds)
+        cpu = {"value": rate, "unit": "rays/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"first {nr} rays of the frame in 128-ray blocks, 64+128 samples; numpy "
+                         "FP32 restatement of the reference (TensorFlow 2.6 is not installable "
+                         "here); OpenBLAS on all host cores"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": args.path, "data": "synthetic",
+            "config": {"workload": "800x800 pinhole frame (focal 1111.111) from a random camera on "
+                                   "the radius-4 sphere, 4096-ray chunks, 64 coarse + 128 fine "
+                                   "samples, random-init coarse+fine 8x256 MLPs",
+                       "rays_per_step_per_gpu": R, "path": f"{args.path} plain hierarchical",
+                       "l2": "512 MB buffer written between timed steps"},
+            "plain_fp32": {"value": plain_value, "unit": "rays/s",
+                           "speedup": value / plain_value},
+            "image_vs_plain_fp32": {"psnr_db": psnr_vs_plain, "max_abs_rgb": max_abs_vs_plain},
+            "roofline": {"kernel": f"mlp_{args.path} fine-pass launch ({rows} rows)", "bound": bound,
+                         "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None, "peak_source": src,
+                         "traffic": traffic, "launch_ms": k_ms},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * R / (e2e_ms / 1000.0), "unit": "rays/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": args.steps * n_chunks * launches_per_chunk,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

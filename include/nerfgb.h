@@ -1,0 +1,164 @@
+/*
+ * nerfgb.h - C ABI of libnerfgb.so, the GB300 (sm_103a) render path of
+ * nerf-tf2: stratified sampling, positional encoding, the coarse/fine
+ * 8x256 MLP, alpha compositing and the inverse-transform fine sampler.
+ *
+ * Conventions
+ *  - Every pointer argument is a DEVICE pointer unless stated otherwise.
+ *    Tensors are dense, row-major, float32 (int32 for indices).
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *    stream). Every call is enqueued on it and returns without a host sync.
+ *  - The caller allocates every output and workspace. The library itself
+ *    allocates no device memory.
+ *  - Every entry point returns NERFGB_OK (0) or a negative NERFGB_E_* code.
+ *    None aborts, throws or exits.
+ *  - Kernels with bounded device-side waits report a timeout through
+ *    `err_word` (a caller-zeroed device int32). Read it after a sync and
+ *    decode it with nerfgb_status_string().
+ *
+ * The reference (thatbrguy/nerf-tf2, TensorFlow 2.6) has no native code and no
+ * FFI. Each entry point below names the Python function it replaces; the
+ * Python mirror in the package binds them with ctypes under the reference's
+ * names.
+ */
+#ifndef NERFGB_H_
+#define NERFGB_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NERFGB_ABI_VERSION 1
+
+/* Status codes. */
+#define NERFGB_OK 0
+#define NERFGB_E_INVALID_ARG (-1) /* null pointer, negative size, misaligned  */
+#define NERFGB_E_UNSUPPORTED (-2) /* size or flag outside the kernels' range  */
+#define NERFGB_E_CUDA (-3)        /* CUDA launch or runtime error              */
+#define NERFGB_E_TIMEOUT (-4)     /* a bounded device wait ran out            */
+#define NERFGB_E_DEVICE (-5)      /* no usable sm_103 device                  */
+
+/* MLP arithmetic precision. */
+#define NERFGB_PREC_FP32 0 /* FP32 SIMT, FP32 accumulate                      */
+#define NERFGB_PREC_BF16 1 /* BF16 tcgen05 GEMMs, FP32 accumulate (TMEM)      */
+
+/* Transmittance evaluation in the compositor. */
+#define NERFGB_TRANS_CUMPROD 0 /* sequential FP32 product, as written          */
+#define NERFGB_TRANS_LOGSUM 1  /* exp of a compensated FP32 log-sum            */
+
+int nerfgb_abi_version(void);
+const char *nerfgb_status_string(int status);
+
+/* ---- parameters of one coarse or fine network ------------------------ */
+
+/* Number of float32 values in the flat parameter blob of one network:
+ * dense_0..dense_7, sigma, dense_8, dense_9, rgb; per layer the Keras kernel
+ * [in,out] row-major followed by the bias [out]. The layers are those built
+ * by get_coarse_or_fine_model (nerf/core/model.py:334-394). */
+long long nerfgb_mlp_param_count(void);
+
+/* Bytes of the packed device layout that the MLP kernels read for
+ * `precision`. */
+long long nerfgb_mlp_packed_bytes(int precision);
+
+/* Packs a device float32 parameter blob into `packed`
+ * (nerfgb_mlp_packed_bytes(precision) bytes, 256-byte aligned). */
+int nerfgb_mlp_pack(const float *params, int precision, void *packed,
+                    void *stream);
+
+/* ---- ray operators ----------------------------------------------------- */
+
+/* Replaces ray_utils.create_input_batch_coarse_model
+ * (nerf/utils/ray_utils.py:137-274). Inputs rays_o, rays_d [R,3]; near, far
+ * [R,1]; u_vals [R,S] uniforms in [0,1) (read only when perturb != 0; they
+ * stand in for tf.random.uniform at :230). Outputs xyz, dirs [R*S,3]
+ * (dirs may be NULL), t_vals [R,S], bin_edges [R,S+1], bin_widths [R,S].
+ * left_edges/right_edges are views of bin_edges. 1 <= S <= 1024. */
+int nerfgb_coarse_sample(const float *rays_o, const float *rays_d,
+                         const float *near, const float *far,
+                         const float *u_vals, int n_rays, int n_coarse,
+                         int perturb, int lin_inv_depth, float *xyz,
+                         float *dirs, float *t_vals, float *bin_edges,
+                         float *bin_widths, void *stream);
+
+/* Replaces ray_utils.create_input_batch_fine_model
+ * (nerf/utils/ray_utils.py:276-406). bin_weights, bin_widths, t_vals_coarse
+ * [R,Sc]; left_edges rows of length Sc at row stride ld_left (Sc+1 when it
+ * is a view of bin_edges); u_vals [R,Sf] stand in for tf.random.uniform at
+ * :355. Outputs xyz, dirs [R*(Sc+Sf),3] (dirs may be NULL), t_vals
+ * [R,Sc+Sf] sorted ascending; optional piece_idxs [R,Sf] (the searchsorted
+ * result) and sort_perm [R,Sc+Sf] (stable argsort of concat(t_c, t_f)).
+ * 2 <= Sc <= 256, 1 <= Sf <= 512. */
+int nerfgb_fine_sample(const float *rays_o, const float *rays_d,
+                       const float *bin_weights, const float *left_edges,
+                       int ld_left, const float *bin_widths,
+                       const float *t_vals_coarse, const float *u_vals,
+                       int n_rays, int n_coarse, int n_fine, float *xyz,
+                       float *dirs, float *t_vals, int *piece_idxs,
+                       int *sort_perm, void *stream);
+
+/* Replaces ray_utils.post_process_model_output (ray_utils.py:484-551) with
+ * compute_weights (:426-482) and sigma_to_alpha (:408-424) inside.
+ * sample_rgb [R*S,3], sigma [R*S], t_vals [R,S] -> weights [R,S] (may be
+ * NULL), pred_rgb [R,3], pred_depth [R], acc_map [R]. 1 <= S <= 2048. */
+int nerfgb_composite(const float *sample_rgb, const float *sigma,
+                     const float *t_vals, int n_rays, int n_samples,
+                     int white_bg, int trans_mode, float *weights,
+                     float *pred_rgb, float *pred_depth, float *acc_map,
+                     void *stream);
+
+/* Replaces ray_utils.sigma_to_alpha (ray_utils.py:408-424):
+ * alpha = 1 - exp(-sigma * diffs), n elements. */
+int nerfgb_sigma_to_alpha(const float *sigma, const float *diffs,
+                          long long n, float *alpha, void *stream);
+
+/* Replaces PositionalEncoder(L).call (nerf/core/model.py:319-331):
+ * x [n,3] -> out [n, 3 + 6L]. 1 <= L <= 16. */
+int nerfgb_positional_encode(const float *x, long long n, int L, float *out,
+                             void *stream);
+
+/* Replaces the Keras model returned by get_coarse_or_fine_model
+ * (nerf/core/model.py:334-394) called on (xyz, dirs): xyz [n,3]; dirs
+ * [ceil(n/rows_per_dir), 3] (row i uses dirs[i / rows_per_dir]; 1 = one
+ * direction per sample as in the reference). Outputs rgb [n,3], sigma [n].
+ * `packed` comes from nerfgb_mlp_pack with the same precision. err_word:
+ * caller-zeroed device int32 (may be NULL for FP32). */
+int nerfgb_mlp_forward(const void *packed, int precision, const float *xyz,
+                       const float *dirs, long long n_rows, int rows_per_dir,
+                       float *rgb, float *sigma, int *err_word, void *stream);
+
+/* ---- uniforms -------------------------------------------------------- */
+
+/* Fills out[0..n) with uniforms in [0,1) from Philox4x32-10 keyed by seed;
+ * element i uses counter (offset + i). Used when the caller supplies no
+ * jitter uniforms (the reference draws them with tf.random.uniform). */
+int nerfgb_uniform(unsigned long long seed, unsigned long long offset,
+                   long long n, float *out, void *stream);
+
+/* ---- fused render --------------------------------------------------- */
+
+/* Workspace bytes that nerfgb_render_rays needs for n_rays rays. */
+long long nerfgb_render_workspace_bytes(int n_rays, int n_coarse, int n_fine);
+
+/* Replaces NeRF.forward (nerf/core/model.py:57-125) for inference: coarse
+ * sample -> coarse MLP -> composite -> fine sample -> fine MLP -> composite.
+ * rays_o, rays_d [R,3]; near, far [R,1]; u_coarse [R,Sc] and u_fine [R,Sf]
+ * may be NULL, in which case uniforms come from Philox keyed by `seed`.
+ * Outputs [R,3] rgb and [R] depth/acc of the coarse pass (may be NULL) and
+ * of the fine pass. `workspace` holds nerfgb_render_workspace_bytes bytes. */
+int nerfgb_render_rays(const void *packed_coarse, const void *packed_fine,
+                       int precision, const float *rays_o,
+                       const float *rays_d, const float *near,
+                       const float *far, const float *u_coarse,
+                       const float *u_fine, unsigned long long seed,
+                       int n_rays, int n_coarse, int n_fine, int perturb,
+                       int lin_inv_depth, int white_bg, int trans_mode,
+                       float *rgb_coarse, float *depth_coarse,
+                       float *acc_coarse, float *rgb_fine, float *depth_fine,
+                       float *acc_fine, void *workspace, int *err_word,
+                       void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NERFGB_H_ */

@@ -1,0 +1,20 @@
+"""GB300 (sm_103a) render path of nerf-tf2 behind the reference's API.
+
+    import importlib
+    ng = importlib.import_module("nerf-tf2_gb300")
+    params = ng.make_params()
+    nerf = ng.NeRF(params, precision="bf16")
+    post_proc_CM, post_proc_FM = nerf.forward(rays_o, rays_d, near, far)
+
+Submodules mirror the reference's modules: ``ray_utils`` (nerf/utils/
+ray_utils.py) and ``model`` (nerf/core/model.py). The kernels live in
+libnerfgb.so (C ABI: include/nerfgb.h), built by ``build.py``.
+"""
+from . import ray_utils, synthetic, weights  # noqa: F401
+from ._lib import NerfgbError, lib  # noqa: F401
+from .config import make_params  # noqa: F401
+from .model import (NeRF, NerfMLP, PositionalEncoder,  # noqa: F401
+                    get_coarse_or_fine_model, psnr)
+from .ray_utils import (compute_weights, create_input_batch_coarse_model,  # noqa: F401
+                        create_input_batch_fine_model, post_process_model_output,
+                        set_seed, sigma_to_alpha)

@@ -1,0 +1,134 @@
+// Shared definitions of libnerfgb: parameter layouts, exact-rounding float
+// helpers, Philox4x32-10, argument checks.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "nerfgb.h"
+
+namespace nerfgb {
+
+// ---------------------------------------------------------------------------
+// Network shape (nerf/core/model.py:334-394). GEMM layers in execution order:
+// dense_0..dense_7, dense_8, dense_9. K is padded to a multiple of 32 with
+// zero rows: dense_0 63->64, dense_5 319->320 ([h | enc_xyz]), dense_9
+// 283->288 ([bottleneck | enc_dir]).
+// ---------------------------------------------------------------------------
+constexpr int kNumGemm = 10;
+#define NG_HD __host__ __device__ __forceinline__ constexpr
+NG_HD int gemm_k(int g) { return g == 0 ? 63 : g == 5 ? 319 : g == 9 ? 283 : 256; }
+NG_HD int gemm_kp(int g) { return g == 0 ? 64 : g == 5 ? 320 : g == 9 ? 288 : 256; }
+NG_HD int gemm_n(int g) { return g == 9 ? 128 : 256; }
+NG_HD bool gemm_relu(int g) { return g != 8; }  // dense_8 (model.py:377-378) is linear
+constexpr int kW = 256;          // hidden width
+constexpr int kEncXyz = 63;      // 3 + 3*2*10
+constexpr int kEncDir = 27;      // 3 + 3*2*4
+
+// Flat blob (nerfgb_mlp_param_count): Keras order dense_0..7, sigma, dense_8,
+// dense_9, rgb; per layer kernel [in,out] row-major then bias [out].
+// GEMM layer g sits at flat index flat_idx_of_gemm(g).
+NG_HD int flat_idx_of_gemm(int g) { return g < 8 ? g : g + 1; }
+NG_HD int flat_in(int l) { return l == 0 ? 63 : l == 5 ? 319 : l == 10 ? 283 : l == 11 ? 128 : 256; }
+NG_HD int flat_out(int l) { return l == 8 ? 1 : l == 10 ? 128 : l == 11 ? 3 : 256; }
+
+NG_HD long long flat_offset(int layer) {
+  long long off = 0;
+  for (int i = 0; i < layer; ++i) off += (long long)flat_in(i) * flat_out(i) + flat_out(i);
+  return off;
+}
+constexpr long long kParamCount = flat_offset(12);  // 595,844
+
+// Padded GEMM weights: offset (elements) of layer g's [Kp][N] block.
+NG_HD long long gemm_w_offset(int g) {
+  long long off = 0;
+  for (int i = 0; i < g; ++i) off += (long long)gemm_kp(i) * gemm_n(i);
+  return off;
+}
+constexpr long long kGemmWElems = gemm_w_offset(kNumGemm);  // 593,920
+
+// FP32 side tables shared by both packs (float offsets inside the table).
+NG_HD int bias_offset(int g) {
+  int off = 0;
+  for (int i = 0; i < g; ++i) off += gemm_n(i);
+  return off;
+}
+constexpr int kBiasElems = bias_offset(kNumGemm);     // 2,432
+constexpr int kSigmaWOff = kBiasElems;                // [256]
+constexpr int kSigmaBOff = kSigmaWOff + 256;          // [1] (+3 pad)
+constexpr int kRgbWOff = kSigmaBOff + 4;              // [128][3]
+constexpr int kRgbBOff = kRgbWOff + 128 * 3;          // [3] (+1 pad)
+constexpr int kTableElems = kRgbBOff + 4;
+
+// FP32 pack: padded W blocks [Kp][N] fp32, then the table.
+constexpr long long kFp32TableOff = kGemmWElems;  // floats
+constexpr long long kFp32PackBytes = (kGemmWElems + kTableElems) * 4;
+
+// BF16 pack: per GEMM layer, K chunks of 32; chunk (n, k) byte offset
+// (k/8)*(N*16) + n*16 + (k%8)*2 (K-major core matrices, no swizzle). Then
+// the fp32 table at a 1 KB aligned offset.
+constexpr long long kBf16WBytes = kGemmWElems * 2;
+constexpr long long kBf16TableOff = (kBf16WBytes + 1023) / 1024 * 1024;  // bytes
+constexpr long long kBf16PackBytes = kBf16TableOff + (long long)kTableElems * 4;
+
+// ---------------------------------------------------------------------------
+// Correctly rounded fp32 arithmetic, never fused into FMA. The reference's
+// TensorFlow ops are separate elementwise kernels, so each step rounds.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float fadd(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float fmul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fdiv(float a, float b) { return __fdiv_rn(a, b); }
+
+// fp32(2^l) * fp32(pi): PositionalEncoder multipliers (model.py:309-311).
+__device__ __forceinline__ float enc_multiplier(int l) {
+  return fmul((float)(1u << l), 3.14159265358979323846f);
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel Random Numbers: As
+// Easy as 1, 2, 3", SC 2011): multipliers and Weyl key increments as
+// published there.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint4 philox4x32_10(uint4 ctr, uint2 key) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u;
+  const uint32_t W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int i = 0; i < 10; ++i) {
+    uint32_t hi0 = __umulhi(M0, ctr.x), lo0 = M0 * ctr.x;
+    uint32_t hi1 = __umulhi(M1, ctr.z), lo1 = M1 * ctr.z;
+    ctr = make_uint4(hi1 ^ ctr.y ^ key.x, lo1, hi0 ^ ctr.w ^ key.y, lo0);
+    key.x += W0;
+    key.y += W1;
+  }
+  return ctr;
+}
+
+// Top 24 bits scaled to [0, 1).
+__device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+// Uniform for flat element index e of the stream keyed by seed.
+__device__ __forceinline__ float philox_uniform(unsigned long long seed, unsigned long long e) {
+  unsigned long long c = e >> 2;
+  uint4 r = philox4x32_10(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0u, 0u),
+                          make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
+  uint32_t w = (e & 3) == 0 ? r.x : (e & 3) == 1 ? r.y : (e & 3) == 2 ? r.z : r.w;
+  return u01(w);
+}
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline int launch_status() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? NERFGB_OK : NERFGB_E_CUDA;
+}
+
+inline int num_sms() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+  return n;
+}
+
+inline bool aligned(const void *p, unsigned a) { return ((uintptr_t)p % a) == 0; }
+
+}  // namespace nerfgb

@@ -1,0 +1,484 @@
+// BF16 tensor-core forward of the NeRF MLP (nerf/core/model.py:334-394) on
+// sm_103a: tcgen05.mma with FP32 accumulators in TMEM, operands in shared
+// memory, weights streamed by the bulk-copy (TMA) engine.
+//
+// CTA tile: 256 sample rows = two 128-row sub-tiles (A, B) that share every
+// weight chunk, so each weight byte fetched from L2 feeds 256 rows. The
+// whole 10-GEMM chain runs on chip: activations never leave shared memory and
+// only xyz/dirs (in) and rgb/sigma (out) touch HBM.
+//
+// Warp roles (18 warps):
+//   warp 0      weight producer: cp.async.bulk of 32-K weight chunks into a
+//               4-stage ring (full/empty mbarriers)
+//   warp 1      TMEM allocator and MMA issuer (one elected thread)
+//   warps 2-17  epilogue: 8 warps per sub-tile, one TMEM lane quadrant and
+//               one 128-column half per warp. They compute the positional
+//               encodings, then per layer read the accumulator (tcgen05.ld),
+//               add bias, apply ReLU, round to BF16 and write the next
+//               layer's A operand; the sigma and rgb heads run in FP32.
+//
+// Shared memory (bytes): ring [0,64K) | encA [64K,80K) | encB [80K,96K) |
+// actA [96K,160K) | actB [160K,224K) | barriers, sigma partials.
+// Operand layout: K-major, no swizzle, 8x16-byte core matrices. Element
+// (r, k) of a 128-row operand sits at (k/8)*2048 + r*16 + (k%8)*2; weights
+// (n, k) of an N-row chunk at (k/8)*(N*16) + n*16 + (k%8)*2.
+//
+// Every mbarrier wait is bounded (globaltimer). On a timeout the kernel sets
+// *err_word = NERFGB_E_TIMEOUT, raises an abort flag that every role polls,
+// drains its own bulk copies and MMAs (bounded), frees TMEM and returns.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "mlp_internal.cuh"
+
+namespace nerfgb {
+namespace tc {
+
+constexpr int kRows = 256;          // rows per CTA tile
+constexpr int kStages = 4;          // weight ring depth
+constexpr int kChunkBytesMax = 256 * 32 * 2;
+constexpr int kThreads = 18 * 32;
+constexpr int kChunksPerTile = 77;  // (64 + 4*256 + 320 + 3*256 + 288) / 32
+
+constexpr uint32_t kRingOff = 0;
+constexpr uint32_t kEncOff = 64 * 1024;   // + s * 16K
+constexpr uint32_t kActOff = 96 * 1024;   // + s * 64K
+constexpr uint32_t kMiscOff = 224 * 1024;
+// misc: full[4] empty[4] accf[2] actr[2] drain (13 x 8 B), tmem slot, abort flag
+constexpr uint32_t kBarFull = kMiscOff;
+constexpr uint32_t kBarEmpty = kMiscOff + 32;
+constexpr uint32_t kBarAccf = kMiscOff + 64;
+constexpr uint32_t kBarActr = kMiscOff + 80;
+constexpr uint32_t kBarDrain = kMiscOff + 96;
+constexpr uint32_t kTmemSlot = kMiscOff + 104;
+constexpr uint32_t kAbort = kMiscOff + 108;
+constexpr uint32_t kSigPart = kMiscOff + 128;  // float [2][128]
+constexpr uint32_t kSmemBytes = kSigPart + 2 * 128 * 4;
+
+constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+
+// ---------------------------------------------------------------------------
+// PTX wrappers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t globaltimer() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+               "l"(src), "r"(bytes), "r"(bar)
+               : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                       uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void named_sync(int id, int threads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
+}
+
+// 32 lanes x 32 columns of FP32 from TMEM; thread t gets lane (addr.lane + t).
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[32];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+      "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+        "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+        "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]),
+        "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
+        "=r"(r[30]), "=r"(r[31])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// Shared-memory matrix descriptor: K-major, no swizzle (layout type 0),
+// descriptor version 1 at bit 46. lbo = byte stride between core matrices
+// adjacent in K, sbo = byte stride between 8-row groups.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(lbo >> 4) << 16) | ((uint64_t)(sbo >> 4) << 32) |
+         (1ull << 46);
+}
+
+// Instruction descriptor of kind::f16: BF16 A and B (K-major), FP32 D.
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+  __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&p);
+}
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
+  asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+
+// Bounded wait: returns false (after flagging) on timeout or abort.
+__device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *err) {
+  if (mbar_try(bar, parity)) return true;
+  uint64_t t0 = globaltimer();
+  while (true) {
+    if (mbar_try(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (globaltimer() - t0 > kWaitNs) {
+      atomicExch(err, NERFGB_E_TIMEOUT);
+      *abort_flag = 1;
+      return false;
+    }
+  }
+}
+
+// Chunk q of a tile -> layer g and chunk c within the layer.
+__device__ __forceinline__ void chunk_of(int q, int &g, int &c) {
+  g = 0;
+  int base = 0;
+  while (q >= base + gemm_kp(g) / 32) {
+    base += gemm_kp(g) / 32;
+    ++g;
+  }
+  c = q - base;
+}
+
+// ---------------------------------------------------------------------------
+// Positional encodings written as BF16 A-operand rows.
+// ---------------------------------------------------------------------------
+// enc_xyz columns [32*HF, 32*HF + 32) of row r (63 values, column 63 = 0).
+template <int HF>
+__device__ __forceinline__ void write_enc_xyz(uint32_t enc, int r, const float (&x)[3]) {
+  float v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = 0.0f;
+  if (HF == 0) {
+    v[0] = x[0];
+    v[1] = x[1];
+    v[2] = x[2];
+  }
+#pragma unroll
+  for (int p = 0; p < 30; ++p) {
+    const int ks = 3 + 2 * p;  // sin at ks, cos at ks + 1
+    if (ks + 1 < 32 * HF || ks >= 32 * HF + 32) continue;
+    const int c = p / 10, l = p % 10;
+    float s, co;
+    sincosf(fmul(x[c], enc_multiplier(l)), &s, &co);
+    if (ks >= 32 * HF && ks < 32 * HF + 32) v[ks - 32 * HF] = s;
+    if (ks + 1 >= 32 * HF && ks + 1 < 32 * HF + 32) v[ks + 1 - 32 * HF] = co;
+  }
+#pragma unroll
+  for (int g = 0; g < 4; ++g)
+    st_shared_v4(enc + (uint32_t)(HF * 4 + g) * 2048u + r * 16, pack_bf16(v[8 * g], v[8 * g + 1]),
+                 pack_bf16(v[8 * g + 2], v[8 * g + 3]), pack_bf16(v[8 * g + 4], v[8 * g + 5]),
+                 pack_bf16(v[8 * g + 6], v[8 * g + 7]));
+}
+
+// enc_dir (27 values, 5 zero pad) into K-groups 0..3 of the enc region.
+__device__ __forceinline__ void write_enc_dir(uint32_t enc, int r, const float (&d)[3]) {
+  float v[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) v[i] = 0.0f;
+  v[0] = d[0];
+  v[1] = d[1];
+  v[2] = d[2];
+#pragma unroll
+  for (int p = 0; p < 12; ++p) {
+    const int c = p / 4, l = p % 4;
+    float s, co;
+    sincosf(fmul(d[c], enc_multiplier(l)), &s, &co);
+    v[3 + 2 * p] = s;
+    v[4 + 2 * p] = co;
+  }
+#pragma unroll
+  for (int g = 0; g < 4; ++g)
+    st_shared_v4(enc + (uint32_t)g * 2048u + r * 16, pack_bf16(v[8 * g], v[8 * g + 1]),
+                 pack_bf16(v[8 * g + 2], v[8 * g + 3]), pack_bf16(v[8 * g + 4], v[8 * g + 5]),
+                 pack_bf16(v[8 * g + 6], v[8 * g + 7]));
+}
+
+// ---------------------------------------------------------------------------
+// The kernel
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kThreads, 1)
+    mlp_bf16_kernel(const uint8_t *__restrict__ packed, const float *__restrict__ xyz,
+                    const float *__restrict__ dirs, long long n, int rpd, float *__restrict__ rgb_out,
+                    float *__restrict__ sigma_out, int *__restrict__ err) {
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kAbort);
+  const float *table = reinterpret_cast<const float *>(packed + kBf16TableOff);
+  const long long ntiles = (n + kRows - 1) / kRows;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(sbase + kBarFull + 8 * s, 1);
+      mbar_init(sbase + kBarEmpty + 8 * s, 1);
+    }
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(sbase + kBarAccf + 8 * s, 1);
+      mbar_init(sbase + kBarActr + 8 * s, 256);
+    }
+    mbar_init(sbase + kBarDrain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + kTmemSlot),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(smem + kTmemSlot);
+
+  if (warp == 0) {
+    // ---------------- weight producer ----------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0;
+      int issued = 0;
+      bool ok = true;
+      for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        for (int q = 0; q < kChunksPerTile; ++q) {
+          if (!wait_bar(sbase + kBarEmpty + 8 * stage, phase ^ 1, abort_flag, err)) {
+            ok = false;
+            break;
+          }
+          int g, c;
+          chunk_of(q, g, c);
+          const uint32_t bytes = (uint32_t)gemm_n(g) * 64u;
+          const uint8_t *src = packed + gemm_w_offset(g) * 2 + (long long)c * bytes;
+          mbar_expect_tx(sbase + kBarFull + 8 * stage, bytes);
+          bulk_g2s(sbase + kRingOff + stage * kChunkBytesMax, src, bytes, sbase + kBarFull + 8 * stage);
+          ++issued;
+          if (++stage == kStages) {
+            stage = 0;
+            phase ^= 1;
+          }
+        }
+      }
+      if (!ok) {
+        // Drain: wait (bounded) for the copies of the stages still in flight.
+        for (int k = 0; k < kStages && k < issued; ++k) {
+          int st = (stage + kStages - 1 - k) % kStages;
+          uint32_t ph = (st < stage) ? phase : phase ^ 1;
+          uint64_t t0 = globaltimer();
+          while (!mbar_try(sbase + kBarFull + 8 * st, ph) && globaltimer() - t0 < 10000000ull) {
+          }
+        }
+      }
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      int stage = 0;
+      uint32_t phase = 0, actr_phase = 0;
+      bool ok = true;
+      int issued_any = 0;
+      for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        int q = 0;
+        for (int g = 0; g < kNumGemm && ok; ++g) {
+          if (!wait_bar(sbase + kBarActr, actr_phase, abort_flag, err) ||
+              !wait_bar(sbase + kBarActr + 8, actr_phase, abort_flag, err)) {
+            ok = false;
+            break;
+          }
+          actr_phase ^= 1;
+          tc_fence_after();
+          const int N = gemm_n(g);
+          const uint32_t idesc = idesc_bf16(128, N);
+          const int nch = gemm_kp(g) / 32;
+          for (int c = 0; c < nch; ++c, ++q) {
+            if (!wait_bar(sbase + kBarFull + 8 * stage, phase, abort_flag, err)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t wst = sbase + kRingOff + stage * kChunkBytesMax;
+            bool from_enc = (g == 0) || (g == 5 && c >= 8) || (g == 9 && c == 8);
+            int kg0 = (g == 0) ? 4 * c : (g == 5 && c >= 8) ? 4 * (c - 8) : (g == 9 && c == 8) ? 0 : 4 * c;
+#pragma unroll
+            for (int ks = 0; ks < 2; ++ks) {
+              const uint64_t bdesc = smem_desc(wst + (uint32_t)(2 * ks) * (N * 16), N * 16, 128);
+#pragma unroll
+              for (int s = 0; s < 2; ++s) {
+                const uint32_t region = sbase + (from_enc ? kEncOff + s * 16384u : kActOff + s * 65536u);
+                const uint64_t adesc = smem_desc(region + (uint32_t)(kg0 + 2 * ks) * 2048u, 2048, 128);
+                tc_mma(tmem + s * 256, adesc, bdesc, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+              }
+            }
+            issued_any = 1;
+            tc_commit(sbase + kBarEmpty + 8 * stage);
+            if (++stage == kStages) {
+              stage = 0;
+              phase ^= 1;
+            }
+          }
+          if (!ok) break;
+          tc_commit(sbase + kBarAccf);
+          tc_commit(sbase + kBarAccf + 8);
+        }
+      }
+      if (issued_any) {
+        // Drain every MMA issued by this thread before TMEM is released.
+        tc_commit(sbase + kBarDrain);
+        uint64_t t0 = globaltimer();
+        while (!mbar_try(sbase + kBarDrain, 0) && globaltimer() - t0 < 100000000ull) {
+        }
+      }
+    }
+  } else {
+    // ---------------- epilogue warps ----------------
+    const int ew = warp - 2;
+    const int s = ew >> 3, hf = (ew >> 2) & 1, qd = warp & 3;
+    const int r = 32 * qd + lane;  // row within the sub-tile (= TMEM lane)
+    const uint32_t enc = sbase + kEncOff + s * 16384u;
+    const uint32_t act = sbase + kActOff + s * 65536u;
+    const uint32_t trow = tmem + ((uint32_t)(32 * qd) << 16) + s * 256 + hf * 128;
+    const uint32_t bar_accf = sbase + kBarAccf + 8 * s, bar_actr = sbase + kBarActr + 8 * s;
+    float *sig_part = reinterpret_cast<float *>(smem + kSigPart) + s * 128;
+    uint32_t accf_phase = 0;
+    bool ok = true;
+    for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+      const long long grow = tile * kRows + s * 128 + r;
+      const bool valid = grow < n;
+      float x[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) x[c] = valid ? xyz[grow * 3 + c] : 0.0f;
+      if (hf == 0)
+        write_enc_xyz<0>(enc, r, x);
+      else
+        write_enc_xyz<1>(enc, r, x);
+      fence_proxy_async();
+      tc_fence_before();
+      mbar_arrive(bar_actr);
+      float rgb_acc[3] = {0.f, 0.f, 0.f};
+      for (int g = 0; g < kNumGemm; ++g) {
+        if (!wait_bar(bar_accf, accf_phase, abort_flag, err)) {
+          ok = false;
+          break;
+        }
+        accf_phase ^= 1;
+        tc_fence_after();
+        const float *bias = table + bias_offset(g);
+        const bool relu = gemm_relu(g);
+        float sig = 0.0f;
+        if (!(g == 9 && hf == 1)) {
+#pragma unroll 1
+          for (int j = 0; j < 4; ++j) {
+            float v[32];
+            tmem_ld32(trow + j * 32, v);
+            const int col0 = hf * 128 + j * 32;
+#pragma unroll
+            for (int i = 0; i < 32; ++i) {
+              v[i] += __ldg(bias + col0 + i);
+              if (relu) v[i] = fmaxf(v[i], 0.0f);
+            }
+            if (g == 7) {
+              const float *ws = table + kSigmaWOff + col0;
+#pragma unroll
+              for (int i = 0; i < 32; ++i) sig = fmaf(v[i], __ldg(ws + i), sig);
+            }
+            if (g == 9) {
+              const float *wr = table + kRgbWOff + col0 * 3;
+#pragma unroll
+              for (int i = 0; i < 32; ++i) {
+                rgb_acc[0] = fmaf(v[i], __ldg(wr + 3 * i), rgb_acc[0]);
+                rgb_acc[1] = fmaf(v[i], __ldg(wr + 3 * i + 1), rgb_acc[1]);
+                rgb_acc[2] = fmaf(v[i], __ldg(wr + 3 * i + 2), rgb_acc[2]);
+              }
+            } else {
+#pragma unroll
+              for (int kg = 0; kg < 4; ++kg)
+                st_shared_v4(act + (uint32_t)(col0 / 8 + kg) * 2048u + r * 16, pack_bf16(v[8 * kg], v[8 * kg + 1]),
+                             pack_bf16(v[8 * kg + 2], v[8 * kg + 3]), pack_bf16(v[8 * kg + 4], v[8 * kg + 5]),
+                             pack_bf16(v[8 * kg + 6], v[8 * kg + 7]));
+            }
+          }
+        }
+        if (g == 7) {
+          // sigma = ReLU(h7 . w + b) (model.py:374-375), halves summed in FP32.
+          if (hf == 1) sig_part[r] = sig;
+          named_sync(1 + s, 256);
+          if (hf == 0 && valid) sigma_out[grow] = fmaxf(sig + sig_part[r] + __ldg(table + kSigmaBOff), 0.0f);
+        }
+        if (g == 8 && hf == 0) {
+          // enc_dir into the enc region (enc_xyz was last read by dense_5).
+          const long long dr = (valid ? grow : n - 1) / rpd;
+          float d[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) d[c] = dirs[dr * 3 + c];
+          write_enc_dir(enc, r, d);
+        }
+        if (g == 9) {
+          if (hf == 0 && valid) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c)
+              rgb_out[grow * 3 + c] = 1.0f / (1.0f + expf(-(rgb_acc[c] + __ldg(table + kRgbBOff + c))));
+          }
+        } else {
+          fence_proxy_async();
+          tc_fence_before();
+          mbar_arrive(bar_actr);
+        }
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  }
+}
+
+}  // namespace tc
+
+int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
+                    float *sigma, int *err_word, cudaStream_t stream) {
+  if (cudaFuncSetAttribute(tc::mlp_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)tc::kSmemBytes) != cudaSuccess)
+    return NERFGB_E_CUDA;
+  const long long ntiles = (n + tc::kRows - 1) / tc::kRows;
+  const int sms = num_sms();
+  if (sms <= 0) return NERFGB_E_DEVICE;
+  const int grid = (int)(ntiles < sms ? ntiles : sms);
+  tc::mlp_bf16_kernel<<<grid, tc::kThreads, tc::kSmemBytes, stream>>>(
+      reinterpret_cast<const uint8_t *>(packed), xyz, dirs, n, rpd, rgb, sigma, err_word);
+  return launch_status();
+}
+
+}  // namespace nerfgb

@@ -1,0 +1,452 @@
+// Ray operators of the render path: stratified coarse sampler, positional
+// encoder, compositor and inverse-transform fine sampler.
+//
+// Layout in HBM: rays [R,3]/[R,1] float32; per-sample tensors [R,S] or
+// [R*S,3] row-major, the layouts the reference's TensorFlow tensors have.
+#include <math.h>
+
+#include "common.cuh"
+
+namespace nerfgb {
+
+// ---------------------------------------------------------------------------
+// Stratified coarse sampler (ray_utils.py:137-274). One thread per (ray, bin).
+// ---------------------------------------------------------------------------
+
+// Point i of tf.linspace(a, b, num): a at 0, b at num-1, else a + delta*i with
+// delta = (b - a) / (num - 1), each step rounded (TF's linspace_nd).
+__device__ __forceinline__ float linspace_at(float a, float b, int num, int i) {
+  if (i == 0) return a;
+  if (i == num - 1) return b;
+  float delta = fdiv(fsub(b, a), (float)(num - 1));
+  return fadd(a, fmul(delta, (float)i));
+}
+
+// Bin edge i of S bins (ray_utils.py:183-203).
+__device__ __forceinline__ float bin_edge(float nr, float fr, int S, int i, int lin_inv) {
+  if (!lin_inv) return linspace_at(nr, fr, S + 1, i);
+  return fdiv(1.0f, linspace_at(fdiv(1.0f, nr), fdiv(1.0f, fr), S + 1, i));
+}
+
+__global__ void coarse_sample_kernel(const float *__restrict__ rays_o, const float *__restrict__ rays_d,
+                                     const float *__restrict__ near, const float *__restrict__ far,
+                                     const float *__restrict__ u, int R, int S, int perturb,
+                                     int lin_inv, float *__restrict__ xyz, float *__restrict__ dirs,
+                                     float *__restrict__ t_out, float *__restrict__ edges,
+                                     float *__restrict__ widths) {
+  long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (gid >= (long long)R * S) return;
+  int r = (int)(gid / S), i = (int)(gid - (long long)r * S);
+  float nr = near[r], fr = far[r];
+  float e0 = bin_edge(nr, fr, S, i, lin_inv);
+  float e1 = bin_edge(nr, fr, S, i + 1, lin_inv);
+  float w = fsub(e1, e0);                                        // :226
+  float t = perturb ? fadd(e0, fmul(u[gid], w))                  // :234
+                    : fmul(0.5f, fadd(e0, e1));                  // :243
+  t_out[gid] = t;
+  widths[gid] = w;
+  edges[(long long)r * (S + 1) + i] = e0;
+  if (i == S - 1) edges[(long long)r * (S + 1) + S] = e1;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    float d = rays_d[3 * r + c];
+    xyz[3 * gid + c] = fadd(rays_o[3 * r + c], fmul(t, d));      // :251
+    if (dirs) dirs[3 * gid + c] = d;                             // :253
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Positional encoder (model.py:319-331): out[n, 3+6L] =
+// [x, sin(x_c m_l), cos(x_c m_l)] at index 3 + c*2L + 2l + {0,1}.
+// ---------------------------------------------------------------------------
+__global__ void encode_kernel(const float *__restrict__ x, long long n, int L, float *__restrict__ out) {
+  long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long per = 3 + 3 * L;  // 3 copies + 3L (c,l) pairs
+  if (gid >= n * per) return;
+  long long row = gid / per;
+  int j = (int)(gid - row * per);
+  int D = 3 + 6 * L;
+  if (j < 3) {
+    out[row * D + j] = x[row * 3 + j];
+    return;
+  }
+  j -= 3;
+  int c = j / L, l = j - c * L;
+  float arg = fmul(x[row * 3 + c], enc_multiplier(l));
+  float s, co;
+  sincosf(arg, &s, &co);
+  out[row * D + 3 + c * 2 * L + 2 * l] = s;
+  out[row * D + 3 + c * 2 * L + 2 * l + 1] = co;
+}
+
+// ---------------------------------------------------------------------------
+// Compositor (ray_utils.py:408-551). One warp per ray. Lane l owns the
+// contiguous segment [l*k, (l+1)*k) of the S samples, k = ceil(S/32).
+// Transmittance T_i = prod_{j<i} ((1 - alpha_j) + 1e-10) (:480), either as a
+// product or as exp of a compensated log-sum (Neumaier per lane, TwoSum
+// across lanes).
+// ---------------------------------------------------------------------------
+struct CSum {
+  float s, c;
+};
+__device__ __forceinline__ CSum two_sum_add(CSum a, CSum b) {
+  float s = fadd(a.s, b.s);
+  float bp = fsub(s, a.s);
+  float e = fadd(fsub(a.s, fsub(s, bp)), fsub(b.s, bp));
+  return CSum{s, fadd(fadd(a.c, b.c), e)};
+}
+
+constexpr int kCompWarps = 4;
+
+__global__ void __launch_bounds__(32 * kCompWarps)
+    composite_kernel(const float *__restrict__ rgb, const float *__restrict__ sigma,
+                     const float *__restrict__ t, int R, int S, int white_bg, int mode,
+                     float *__restrict__ weights, float *__restrict__ pred_rgb,
+                     float *__restrict__ pred_depth, float *__restrict__ acc_map) {
+  extern __shared__ float smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  float *s_t = smem + warp * 2 * (S + 1);
+  float *s_sig = s_t + (S + 1);
+  const int k = (S + 31) >> 5;
+  for (int r = blockIdx.x * kCompWarps + warp; r < R; r += gridDim.x * kCompWarps) {
+    const long long base = (long long)r * S;
+    for (int j = lane; j < S; j += 32) {
+      s_t[j] = t[base + j];
+      s_sig[j] = sigma[base + j];
+    }
+    __syncwarp();
+    const int j0 = min(lane * k, S), j1 = min(j0 + k, S);
+    // Per-sample alpha and transmittance factor.
+    float loc_prod = 1.0f;
+    CSum loc{0.0f, 0.0f};
+    for (int j = j0; j < j1; ++j) {
+      float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : 1e10f;   // :462-468
+      float alpha = fsub(1.0f, expf(fmul(-s_sig[j], delta)));         // :423
+      float fac = fadd(fsub(1.0f, alpha), 1e-10f);                    // :480
+      if (mode == NERFGB_TRANS_CUMPROD) {
+        loc_prod = fmul(loc_prod, fac);
+      } else {
+        loc = two_sum_add(loc, CSum{logf(fac), 0.0f});
+      }
+    }
+    // Exclusive scan across lanes.
+    float ex_prod = 1.0f;
+    CSum ex{0.0f, 0.0f};
+    if (mode == NERFGB_TRANS_CUMPROD) {
+      float inc = loc_prod;
+      for (int off = 1; off < 32; off <<= 1) {
+        float o = __shfl_up_sync(0xffffffffu, inc, off);
+        if (lane >= off) inc = fmul(o, inc);
+      }
+      ex_prod = __shfl_up_sync(0xffffffffu, inc, 1);
+      if (lane == 0) ex_prod = 1.0f;
+    } else {
+      CSum inc = loc;
+      for (int off = 1; off < 32; off <<= 1) {
+        float os = __shfl_up_sync(0xffffffffu, inc.s, off);
+        float oc = __shfl_up_sync(0xffffffffu, inc.c, off);
+        if (lane >= off) inc = two_sum_add(CSum{os, oc}, inc);
+      }
+      ex.s = __shfl_up_sync(0xffffffffu, inc.s, 1);
+      ex.c = __shfl_up_sync(0xffffffffu, inc.c, 1);
+      if (lane == 0) ex = CSum{0.0f, 0.0f};
+    }
+    // Weights and partial sums.
+    float pr = 0.f, pg = 0.f, pb = 0.f, pd = 0.f, pa = 0.f;
+    float run_prod = ex_prod;
+    CSum run = ex;
+    for (int j = j0; j < j1; ++j) {
+      float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : 1e10f;
+      float alpha = fsub(1.0f, expf(fmul(-s_sig[j], delta)));
+      float fac = fadd(fsub(1.0f, alpha), 1e-10f);
+      float T;
+      if (mode == NERFGB_TRANS_CUMPROD) {
+        T = run_prod;
+        run_prod = fmul(run_prod, fac);
+      } else {
+        T = expf(fadd(run.s, run.c));
+        run = two_sum_add(run, CSum{logf(fac), 0.0f});
+      }
+      float w = fmul(alpha, T);                                       // :480
+      if (weights) weights[base + j] = w;
+      const float *c = rgb + 3 * (base + j);
+      pr = fadd(pr, fmul(w, c[0]));                                   // :534
+      pg = fadd(pg, fmul(w, c[1]));
+      pb = fadd(pb, fmul(w, c[2]));
+      pd = fadd(pd, fmul(s_t[j], w));                                 // :537
+      pa = fadd(pa, w);                                               // :540
+    }
+    for (int off = 16; off > 0; off >>= 1) {
+      pr = fadd(pr, __shfl_xor_sync(0xffffffffu, pr, off));
+      pg = fadd(pg, __shfl_xor_sync(0xffffffffu, pg, off));
+      pb = fadd(pb, __shfl_xor_sync(0xffffffffu, pb, off));
+      pd = fadd(pd, __shfl_xor_sync(0xffffffffu, pd, off));
+      pa = fadd(pa, __shfl_xor_sync(0xffffffffu, pa, off));
+    }
+    if (lane == 0) {
+      if (white_bg) {                                                 // :542-544
+        float bg = fsub(1.0f, pa);
+        pr = fadd(pr, bg);
+        pg = fadd(pg, bg);
+        pb = fadd(pb, bg);
+      }
+      pred_rgb[3 * r + 0] = pr;
+      pred_rgb[3 * r + 1] = pg;
+      pred_rgb[3 * r + 2] = pb;
+      pred_depth[r] = pd;
+      acc_map[r] = pa;
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void sigma_to_alpha_kernel(const float *__restrict__ sigma, const float *__restrict__ diffs,
+                                      long long n, float *__restrict__ alpha) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) alpha[i] = fsub(1.0f, expf(fmul(-sigma[i], diffs[i])));
+}
+
+// ---------------------------------------------------------------------------
+// Inverse-transform fine sampler (ray_utils.py:276-406). One warp per ray.
+// The two reductions that feed the CDF (denominator :338, cumsum :342) run
+// left to right in one lane, in fp32 without FMA, so the CDF, the
+// searchsorted indices and the sorted t are bit-identical to the sequential
+// restatement.
+// ---------------------------------------------------------------------------
+constexpr int kFineWarps = 4;
+
+// Strict weak order of numpy's stable sort: NaN after every number, ties by
+// original index.
+__device__ __forceinline__ bool sort_before(float a, int ia, float b, int ib) {
+  bool na = isnan(a), nb = isnan(b);
+  if (na || nb) return (!na && nb) || (na && nb && ia < ib);
+  return a < b || (a == b && ia < ib);
+}
+
+__global__ void __launch_bounds__(32 * kFineWarps)
+    fine_sample_kernel(const float *__restrict__ rays_o, const float *__restrict__ rays_d,
+                       const float *__restrict__ bin_weights, const float *__restrict__ left_edges,
+                       int ld_left, const float *__restrict__ bin_widths,
+                       const float *__restrict__ t_coarse, const float *__restrict__ u, int R, int Sc,
+                       int Sf, float *__restrict__ xyz, float *__restrict__ dirs,
+                       float *__restrict__ t_out, int *__restrict__ piece_idxs,
+                       int *__restrict__ sort_perm) {
+  extern __shared__ float smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int S = Sc + Sf;
+  const int per_warp = 4 * Sc + (Sc + 1) + 2 * S;
+  float *s_w = smem + warp * per_warp;  // w + 1e-5, then pdf * width
+  float *s_pdf = s_w + Sc;
+  float *s_left = s_pdf + Sc;
+  float *s_wid = s_left + Sc;
+  float *s_agg = s_wid + Sc;      // Sc + 1
+  float *s_t = s_agg + Sc + 1;    // concat(t_c, t_f), S
+  float *s_srt = s_t + S;         // sorted, S
+  for (int r = blockIdx.x * kFineWarps + warp; r < R; r += gridDim.x * kFineWarps) {
+    const long long rb = (long long)r * Sc;
+    for (int j = lane; j < Sc; j += 32) {
+      float w = fadd(bin_weights[rb + j], 1e-5f);                     // :335
+      float wd = bin_widths[rb + j];
+      s_w[j] = w;
+      s_pdf[j] = fmul(w, wd);
+      s_wid[j] = wd;
+      s_left[j] = left_edges[(long long)r * ld_left + j];
+      s_t[j] = t_coarse[rb + j];
+    }
+    __syncwarp();
+    float denom = 0.0f;
+    if (lane == 0)
+      for (int j = 0; j < Sc; ++j) denom = fadd(denom, s_pdf[j]);     // :338
+    denom = __shfl_sync(0xffffffffu, denom, 0);
+    __syncwarp();
+    for (int j = lane; j < Sc; j += 32) {
+      float p = fdiv(s_w[j], denom);                                  // :339
+      s_pdf[j] = p;
+      s_w[j] = fmul(p, s_wid[j]);
+    }
+    __syncwarp();
+    if (lane == 0) {                                                  // :342-345
+      float acc = 0.0f;
+      s_agg[0] = 0.0f;
+      for (int j = 0; j < Sc; ++j) {
+        acc = fadd(acc, s_w[j]);
+        s_agg[j + 1] = acc;
+      }
+    }
+    __syncwarp();
+    const long long ub = (long long)r * Sf;
+    for (int k = lane; k < Sf; k += 32) {
+      float uk = u[ub + k];
+      // upper_bound over the inner edges agg[1..Sc-1] (:363).
+      int first = 0, count = Sc - 1;
+      while (count > 0) {
+        int step = count >> 1, it = first + step;
+        if (!(uk < s_agg[1 + it])) {
+          first = it + 1;
+          count -= step + 1;
+        } else {
+          count = step;
+        }
+      }
+      float a_ = s_agg[first], p_ = s_pdf[first], l_ = s_left[first];  // :366-368
+      float mask = (p_ < 1e-8f) ? 0.0f : 1.0f;                          // :372
+      p_ = fmaxf(p_, 1e-8f);                                            // :373
+      s_t[Sc + k] = fadd(fmul(fdiv(fsub(uk, a_), p_), mask), l_);       // :376
+      if (piece_idxs) piece_idxs[ub + k] = first;
+    }
+    __syncwarp();
+    // Rank sort of concat(t_c, t_f) (:380-385): rank = number of elements
+    // that precede e in the stable order.
+    const long long sb = (long long)r * S;
+    for (int e = lane; e < S; e += 32) {
+      float v = s_t[e];
+      int rank = 0;
+      for (int q = 0; q < S; ++q) rank += sort_before(s_t[q], q, v, e) ? 1 : 0;
+      s_srt[rank] = v;
+      if (sort_perm) sort_perm[sb + rank] = e;
+    }
+    __syncwarp();
+    float o0 = rays_o[3 * r], o1 = rays_o[3 * r + 1], o2 = rays_o[3 * r + 2];
+    float d0 = rays_d[3 * r], d1 = rays_d[3 * r + 1], d2 = rays_d[3 * r + 2];
+    for (int p = lane; p < S; p += 32) {
+      float tv = s_srt[p];
+      t_out[sb + p] = tv;
+      float *x = xyz + 3 * (sb + p);                                  // :389
+      x[0] = fadd(o0, fmul(tv, d0));
+      x[1] = fadd(o1, fmul(tv, d1));
+      x[2] = fadd(o2, fmul(tv, d2));
+      if (dirs) {
+        float *dd = dirs + 3 * (sb + p);
+        dd[0] = d0;
+        dd[1] = d1;
+        dd[2] = d2;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void uniform_kernel(unsigned long long seed, unsigned long long offset, long long n,
+                               float *__restrict__ out) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = philox_uniform(seed, offset + (unsigned long long)i);
+}
+
+static int grid_for(long long n, int block) {
+  long long g = (n + block - 1) / block;
+  return (int)(g > 0x7fffffffLL ? 0x7fffffff : g);
+}
+
+}  // namespace nerfgb
+
+using namespace nerfgb;
+
+extern "C" int nerfgb_abi_version(void) { return NERFGB_ABI_VERSION; }
+
+extern "C" const char *nerfgb_status_string(int s) {
+  switch (s) {
+    case NERFGB_OK: return "NERFGB_OK";
+    case NERFGB_E_INVALID_ARG: return "NERFGB_E_INVALID_ARG";
+    case NERFGB_E_UNSUPPORTED: return "NERFGB_E_UNSUPPORTED";
+    case NERFGB_E_CUDA: return "NERFGB_E_CUDA";
+    case NERFGB_E_TIMEOUT: return "NERFGB_E_TIMEOUT";
+    case NERFGB_E_DEVICE: return "NERFGB_E_DEVICE";
+    default: return "NERFGB_E_UNKNOWN";
+  }
+}
+
+extern "C" int nerfgb_coarse_sample(const float *rays_o, const float *rays_d, const float *near,
+                                    const float *far, const float *u_vals, int n_rays, int n_coarse,
+                                    int perturb, int lin_inv_depth, float *xyz, float *dirs,
+                                    float *t_vals, float *bin_edges, float *bin_widths, void *stream) {
+  if (n_rays < 0 || n_coarse < 1) return NERFGB_E_INVALID_ARG;
+  if (n_coarse > 1024) return NERFGB_E_UNSUPPORTED;
+  if (n_rays == 0) return NERFGB_OK;
+  if (!rays_o || !rays_d || !near || !far || !xyz || !t_vals || !bin_edges || !bin_widths ||
+      (perturb && !u_vals))
+    return NERFGB_E_INVALID_ARG;
+  long long n = (long long)n_rays * n_coarse;
+  coarse_sample_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
+      rays_o, rays_d, near, far, u_vals, n_rays, n_coarse, perturb, lin_inv_depth, xyz, dirs, t_vals,
+      bin_edges, bin_widths);
+  return launch_status();
+}
+
+extern "C" int nerfgb_positional_encode(const float *x, long long n, int L, float *out, void *stream) {
+  if (n < 0 || L < 1) return NERFGB_E_INVALID_ARG;
+  if (L > 16) return NERFGB_E_UNSUPPORTED;
+  if (n == 0) return NERFGB_OK;
+  if (!x || !out) return NERFGB_E_INVALID_ARG;
+  long long work = n * (3 + 3 * L);
+  encode_kernel<<<grid_for(work, 256), 256, 0, as_stream(stream)>>>(x, n, L, out);
+  return launch_status();
+}
+
+extern "C" int nerfgb_composite(const float *sample_rgb, const float *sigma, const float *t_vals,
+                                int n_rays, int n_samples, int white_bg, int trans_mode,
+                                float *weights, float *pred_rgb, float *pred_depth, float *acc_map,
+                                void *stream) {
+  if (n_rays < 0 || n_samples < 1) return NERFGB_E_INVALID_ARG;
+  if (n_samples > 2048) return NERFGB_E_UNSUPPORTED;
+  if (trans_mode != NERFGB_TRANS_CUMPROD && trans_mode != NERFGB_TRANS_LOGSUM)
+    return NERFGB_E_UNSUPPORTED;
+  if (n_rays == 0) return NERFGB_OK;
+  if (!sample_rgb || !sigma || !t_vals || !pred_rgb || !pred_depth || !acc_map)
+    return NERFGB_E_INVALID_ARG;
+  size_t smem = (size_t)kCompWarps * 2 * (n_samples + 1) * sizeof(float);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(composite_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return NERFGB_E_CUDA;
+  int sms = num_sms();
+  int blocks = (n_rays + kCompWarps - 1) / kCompWarps;
+  int cap = (sms > 0 ? sms : 148) * 16;
+  composite_kernel<<<blocks < cap ? blocks : cap, 32 * kCompWarps, smem, as_stream(stream)>>>(
+      sample_rgb, sigma, t_vals, n_rays, n_samples, white_bg, trans_mode, weights, pred_rgb,
+      pred_depth, acc_map);
+  return launch_status();
+}
+
+extern "C" int nerfgb_sigma_to_alpha(const float *sigma, const float *diffs, long long n, float *alpha,
+                                     void *stream) {
+  if (n < 0) return NERFGB_E_INVALID_ARG;
+  if (n == 0) return NERFGB_OK;
+  if (!sigma || !diffs || !alpha) return NERFGB_E_INVALID_ARG;
+  sigma_to_alpha_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(sigma, diffs, n, alpha);
+  return launch_status();
+}
+
+extern "C" int nerfgb_fine_sample(const float *rays_o, const float *rays_d, const float *bin_weights,
+                                  const float *left_edges, int ld_left, const float *bin_widths,
+                                  const float *t_vals_coarse, const float *u_vals, int n_rays,
+                                  int n_coarse, int n_fine, float *xyz, float *dirs, float *t_vals,
+                                  int *piece_idxs, int *sort_perm, void *stream) {
+  if (n_rays < 0 || n_coarse < 2 || n_fine < 1 || ld_left < n_coarse) return NERFGB_E_INVALID_ARG;
+  if (n_coarse > 256 || n_fine > 512) return NERFGB_E_UNSUPPORTED;
+  if (n_rays == 0) return NERFGB_OK;
+  if (!rays_o || !rays_d || !bin_weights || !left_edges || !bin_widths || !t_vals_coarse ||
+      !u_vals || !xyz || !t_vals)
+    return NERFGB_E_INVALID_ARG;
+  int S = n_coarse + n_fine;
+  size_t smem = (size_t)kFineWarps * (4 * n_coarse + (n_coarse + 1) + 2 * S) * sizeof(float);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(fine_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return NERFGB_E_CUDA;
+  int sms = num_sms();
+  int blocks = (n_rays + kFineWarps - 1) / kFineWarps;
+  int cap = (sms > 0 ? sms : 148) * 16;
+  fine_sample_kernel<<<blocks < cap ? blocks : cap, 32 * kFineWarps, smem, as_stream(stream)>>>(
+      rays_o, rays_d, bin_weights, left_edges, ld_left, bin_widths, t_vals_coarse, u_vals, n_rays,
+      n_coarse, n_fine, xyz, dirs, t_vals, piece_idxs, sort_perm);
+  return launch_status();
+}
+
+extern "C" int nerfgb_uniform(unsigned long long seed, unsigned long long offset, long long n, float *out,
+                              void *stream) {
+  if (n < 0) return NERFGB_E_INVALID_ARG;
+  if (n == 0) return NERFGB_OK;
+  if (!out) return NERFGB_E_INVALID_ARG;
+  uniform_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(seed, offset, n, out);
+  return launch_status();
+}

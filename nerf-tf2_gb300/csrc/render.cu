@@ -1,0 +1,100 @@
+// Fused render: the inference body of NeRF.forward (nerf/core/model.py:57-125)
+// as one C-ABI call over caller-provided workspace. The chain is the one the
+// reference runs: coarse sample -> coarse MLP -> composite -> fine sample ->
+// fine MLP -> composite. Directions are read per ray (rows_per_dir = samples
+// per ray), so the broadcast dir_inputs tensor is never materialised.
+#include "common.cuh"
+#include "mlp_internal.cuh"
+
+namespace nerfgb {
+
+struct RenderWs {
+  float *u_c, *u_f, *xyz_c, *t_c, *edges, *widths, *rgb_c, *sig_c, *w_c, *xyz_f, *t_f, *rgb_f, *sig_f;
+  float *map_rgb_c, *map_depth_c, *map_acc_c;
+  long long bytes;
+};
+
+static long long align256(long long b) { return (b + 255) / 256 * 256; }
+
+static RenderWs carve(void *base, int R, int Sc, int Sf) {
+  RenderWs w{};
+  const long long r = R, S = Sc + Sf;
+  const long long sizes[16] = {r * Sc, r * Sf, r * Sc * 3, r * Sc, r * (Sc + 1), r * Sc, r * Sc * 3, r * Sc,
+                               r * Sc, r * S * 3, r * S,    r * S * 3, r * S,       r * 3,  r,          r};
+  float **slots[16] = {&w.u_c,   &w.u_f,  &w.xyz_c, &w.t_c,   &w.edges,     &w.widths,
+                       &w.rgb_c, &w.sig_c, &w.w_c,  &w.xyz_f, &w.t_f,       &w.rgb_f,
+                       &w.sig_f, &w.map_rgb_c, &w.map_depth_c, &w.map_acc_c};
+  long long off = 0;
+  for (int i = 0; i < 16; ++i) {
+    if (base) *slots[i] = reinterpret_cast<float *>(static_cast<char *>(base) + off);
+    off += align256(sizes[i] * (long long)sizeof(float));
+  }
+  w.bytes = off;
+  return w;
+}
+
+int launch_mlp(const void *packed, int precision, const float *xyz, const float *dirs, long long n, int rpd,
+               float *rgb, float *sigma, int *err_word, cudaStream_t stream) {
+  if (precision == NERFGB_PREC_FP32) return launch_mlp_fp32(packed, xyz, dirs, n, rpd, rgb, sigma, stream);
+  return launch_mlp_bf16(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
+}
+
+}  // namespace nerfgb
+
+using namespace nerfgb;
+
+extern "C" long long nerfgb_render_workspace_bytes(int n_rays, int n_coarse, int n_fine) {
+  if (n_rays < 0 || n_coarse < 1 || n_fine < 0) return -1;
+  return carve(nullptr, n_rays, n_coarse, n_fine).bytes;
+}
+
+extern "C" int nerfgb_render_rays(const void *packed_coarse, const void *packed_fine, int precision,
+                                  const float *rays_o, const float *rays_d, const float *near, const float *far,
+                                  const float *u_coarse, const float *u_fine, unsigned long long seed,
+                                  int n_rays, int n_coarse, int n_fine, int perturb, int lin_inv_depth,
+                                  int white_bg, int trans_mode, float *rgb_coarse, float *depth_coarse,
+                                  float *acc_coarse, float *rgb_fine, float *depth_fine, float *acc_fine,
+                                  void *workspace, int *err_word, void *stream) {
+  if (n_rays < 0 || n_coarse < 2 || n_fine < 1) return NERFGB_E_INVALID_ARG;
+  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16) return NERFGB_E_UNSUPPORTED;
+  if (n_rays == 0) return NERFGB_OK;
+  if (!packed_coarse || !packed_fine || !rays_o || !rays_d || !near || !far || !rgb_fine || !depth_fine ||
+      !acc_fine || !workspace || !aligned(workspace, 256))
+    return NERFGB_E_INVALID_ARG;
+  if (precision == NERFGB_PREC_BF16 && !err_word) return NERFGB_E_INVALID_ARG;
+  cudaStream_t st = as_stream(stream);
+  const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
+  RenderWs w = carve(workspace, R, Sc, Sf);
+  int rc;
+  const float *uc = u_coarse, *uf = u_fine;
+  // Uniforms: coarse draws use counters [0, R*Sc), fine draws [R*Sc, R*S).
+  if (perturb && !uc) {
+    if ((rc = nerfgb_uniform(seed, 0, (long long)R * Sc, w.u_c, stream)) != NERFGB_OK) return rc;
+    uc = w.u_c;
+  }
+  if (!uf) {
+    if ((rc = nerfgb_uniform(seed, (unsigned long long)R * Sc, (long long)R * Sf, w.u_f, stream)) != NERFGB_OK)
+      return rc;
+    uf = w.u_f;
+  }
+  if ((rc = nerfgb_coarse_sample(rays_o, rays_d, near, far, uc, R, Sc, perturb, lin_inv_depth, w.xyz_c, nullptr,
+                                 w.t_c, w.edges, w.widths, stream)) != NERFGB_OK)
+    return rc;
+  if ((rc = launch_mlp(packed_coarse, precision, w.xyz_c, rays_d, (long long)R * Sc, Sc, w.rgb_c, w.sig_c,
+                       err_word, st)) != NERFGB_OK)
+    return rc;
+  float *rc_rgb = rgb_coarse ? rgb_coarse : w.map_rgb_c;
+  float *rc_dep = depth_coarse ? depth_coarse : w.map_depth_c;
+  float *rc_acc = acc_coarse ? acc_coarse : w.map_acc_c;
+  if ((rc = nerfgb_composite(w.rgb_c, w.sig_c, w.t_c, R, Sc, white_bg, trans_mode, w.w_c, rc_rgb, rc_dep, rc_acc,
+                             stream)) != NERFGB_OK)
+    return rc;
+  if ((rc = nerfgb_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, uf, R, Sc, Sf, w.xyz_f,
+                               nullptr, w.t_f, nullptr, nullptr, stream)) != NERFGB_OK)
+    return rc;
+  if ((rc = launch_mlp(packed_fine, precision, w.xyz_f, rays_d, (long long)R * S, S, w.rgb_f, w.sig_f, err_word,
+                       st)) != NERFGB_OK)
+    return rc;
+  return nerfgb_composite(w.rgb_f, w.sig_f, w.t_f, R, S, white_bg, trans_mode, nullptr, rgb_fine, depth_fine,
+                          acc_fine, stream);
+}

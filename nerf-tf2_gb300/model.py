@@ -1,0 +1,208 @@
+"""Drop-in for the render-path parts of nerf/core/model.py, on CUDA.
+
+* ``PositionalEncoder(L, name=None)`` - model.py:289-332.
+* ``get_coarse_or_fine_model(model_name, num_units=256)`` - model.py:334-394;
+  returns a callable ``model(inputs=(xyz, dir)) -> (rgb [M,3], sigma [M,1])``
+  whose weights live on the device as the flat blob of ``weights.py``.
+* ``NeRF(params)`` with ``forward(rays_o, rays_d, near, far)`` -
+  model.py:18-125; returns ``(post_proc_CM, post_proc_FM)``.
+
+The MLP runs as one kernel per call: FP32 SIMT (``precision="fp32"``, the
+plain path) or BF16 tcgen05 GEMMs with FP32 accumulation
+(``precision="bf16"``).
+"""
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib, ray_utils
+from ._tensors import as_cuda, device, empty, ptr, stream
+from .weights import PARAM_COUNT, from_dict, glorot_blob, to_dict
+
+PRECISIONS = {"fp32": _lib.PREC_FP32, "bf16": _lib.PREC_BF16}
+
+
+class PositionalEncoder:
+    """model.py:289-332: x [n,3] -> [x, sin(x 2^l pi), cos(x 2^l pi)] with the
+    reference's interleaving (coordinate-major, then frequency, then
+    sin/cos)."""
+
+    def __init__(self, L, name=None):
+        self.L = int(L)
+        self.name = name
+
+    def __call__(self, x):
+        x = as_cuda(x, name="x")
+        n = x.shape[0]
+        x = as_cuda(x, shape=(n, 3), name="x")
+        out = empty(n, 3 + 6 * self.L)
+        _lib.call("nerfgb_positional_encode", ptr(x), n, self.L, ptr(out), stream())
+        return out
+
+    call = __call__
+
+
+class NerfMLP:
+    """The Keras model of get_coarse_or_fine_model as a device-resident
+    callable. ``params`` is the flat float32 blob (``weights.py``)."""
+
+    def __init__(self, model_name, params=None, seed=0, precision="fp32"):
+        self.name = model_name
+        blob = glorot_blob(seed) if params is None else params
+        self.params = as_cuda(blob, shape=(PARAM_COUNT,), name="params").clone()
+        self.precision = precision
+        self._packed = {}
+        self._version = 0
+        self.err_word = torch.zeros(1, dtype=torch.int32, device=device())
+
+    # -- weights -------------------------------------------------------------
+    def mark_updated(self):
+        """Call after changing ``params`` in place; repacks lazily."""
+        self._version += 1
+
+    def packed(self, precision=None):
+        prec = PRECISIONS[precision or self.precision]
+        hit = self._packed.get(prec)
+        if hit is not None and hit[0] == self._version:
+            return hit[1]
+        nbytes = _lib.lib().nerfgb_mlp_packed_bytes(prec)
+        buf = torch.empty(nbytes, dtype=torch.uint8, device=self.params.device)
+        _lib.call("nerfgb_mlp_pack", ptr(self.params), prec, ptr(buf), stream())
+        self._packed[prec] = (self._version, buf)
+        return buf
+
+    def get_weights(self):
+        """{"<model>/<layer>/kernel:0": ndarray, ...} (Keras variable names)."""
+        return to_dict(self.params.detach().cpu().numpy(), self.name)
+
+    def set_weights(self, d):
+        blob = from_dict(d, self.name)
+        self.params.copy_(torch.from_numpy(blob))
+        self.mark_updated()
+
+    # -- forward -------------------------------------------------------------
+    def __call__(self, inputs, *, precision=None, rows_per_dir=1):
+        xyz, dirs = inputs
+        xyz = as_cuda(xyz, name="xyz")
+        n = xyz.shape[0]
+        xyz = as_cuda(xyz, shape=(n, 3), name="xyz")
+        nd = (n + rows_per_dir - 1) // rows_per_dir
+        dirs = as_cuda(dirs, shape=(nd, 3), name="dir")
+        prec = PRECISIONS[precision or self.precision]
+        rgb = empty(n, 3)
+        sigma = empty(n, 1)
+        _lib.call("nerfgb_mlp_forward", ptr(self.packed(precision)), prec, ptr(xyz), ptr(dirs), n,
+                  int(rows_per_dir), ptr(rgb), ptr(sigma), ptr(self.err_word), stream())
+        return rgb, sigma
+
+    call = __call__
+
+    def check_device_errors(self):
+        """Synchronises and raises if a bounded device wait timed out."""
+        torch.cuda.synchronize()
+        code = int(self.err_word.item())
+        if code != 0:
+            self.err_word.zero_()
+            raise _lib.NerfgbError("nerfgb_mlp_forward (device)", code, _lib.status_name(code))
+
+
+def get_coarse_or_fine_model(model_name, num_units=256, *, params=None, seed=0, precision="fp32"):
+    """model.py:334-394. Only num_units=256 (the reference's value) has
+    kernels."""
+    assert model_name in ("coarse", "fine")
+    if num_units != 256:
+        raise ValueError("the CUDA MLP is specialised for num_units=256")
+    return NerfMLP(model_name, params=params, seed=seed, precision=precision)
+
+
+class NeRF:
+    """model.py:18-125: coarse and fine networks plus the hierarchical
+    render. ``forward`` mirrors the reference op by op and returns its dicts;
+    ``render`` runs the same chain as one fused library call per chunk."""
+
+    def __init__(self, params, *, precision="fp32", seed=0, coarse_params=None, fine_params=None,
+                 trans_mode=None):
+        self.params = params
+        self.white_bg = bool(params.system.white_bg)
+        self.precision = precision
+        self.trans_mode = ray_utils.DEFAULT_TRANS_MODE if trans_mode is None else trans_mode
+        self.coarse_model = get_coarse_or_fine_model("coarse", params=coarse_params, seed=seed,
+                                                     precision=precision)
+        self.fine_model = get_coarse_or_fine_model("fine", params=fine_params, seed=seed + 1,
+                                                   precision=precision)
+
+    def forward(self, rays_o, rays_d, near, far, *, u_coarse=None, u_fine=None):
+        """model.py:57-125 with optional explicit jitter uniforms."""
+        data_CM = ray_utils.create_input_batch_coarse_model(
+            params=self.params, rays_o=rays_o, rays_d=rays_d, near=near, far=far, u_vals=u_coarse)
+        rgb_CM, sigma_CM = self.coarse_model(inputs=(data_CM["xyz_inputs"], data_CM["dir_inputs"]))
+        post_proc_CM = ray_utils.post_process_model_output(
+            sample_rgb=rgb_CM, sigma=sigma_CM, t_vals=data_CM["t_vals"], white_bg=self.white_bg,
+            trans_mode=self.trans_mode)
+        data_FM = ray_utils.create_input_batch_fine_model(
+            params=self.params, rays_o=rays_o, rays_d=rays_d, bin_weights=post_proc_CM["weights"],
+            t_vals_coarse=data_CM["t_vals"], bin_data=data_CM["bin_data"], u_vals=u_fine)
+        rgb_FM, sigma_FM = self.fine_model(inputs=(data_FM["xyz_inputs"], data_FM["dir_inputs"]))
+        post_proc_FM = ray_utils.post_process_model_output(
+            sample_rgb=rgb_FM, sigma=sigma_FM, t_vals=data_FM["t_vals"], white_bg=self.white_bg,
+            trans_mode=self.trans_mode)
+        return post_proc_CM, post_proc_FM
+
+    def __call__(self, inputs):
+        """model.py:36-55: inputs[0] = (rays_o, rays_d, near, far)."""
+        return self.forward(*inputs[0])
+
+    call = __call__
+    predict_step = __call__
+
+    # -- fused inference ----------------------------------------------------
+    def render(self, rays_o, rays_d, near, far, *, chunk=4096, u_coarse=None, u_fine=None, seed=0,
+               precision=None, return_coarse=False):
+        """Fine (and optionally coarse) rgb/depth/acc maps for every ray, in
+        chunks of `chunk` rays (the reference renders 4096-ray batches,
+        base_dataset.py:853-857). Uniforms come from Philox keyed by `seed`
+        when not supplied."""
+        prec = PRECISIONS[precision or self.precision]
+        rays_o = as_cuda(rays_o, name="rays_o")
+        R = rays_o.shape[0]
+        rays_d = as_cuda(rays_d, shape=(R, 3), name="rays_d")
+        near = as_cuda(near, shape=(R, 1), name="near")
+        far = as_cuda(far, shape=(R, 1), name="far")
+        Sc, Sf = int(self.params.sampling.N_coarse), int(self.params.sampling.N_fine)
+        if u_coarse is not None:
+            u_coarse = as_cuda(u_coarse, shape=(R, Sc), name="u_coarse")
+        if u_fine is not None:
+            u_fine = as_cuda(u_fine, shape=(R, Sf), name="u_fine")
+        out = {k: empty(R, 3) if k.startswith("rgb") else empty(R)
+               for k in (["rgb", "depth", "acc"] + (["rgb_coarse", "depth_coarse", "acc_coarse"]
+                                                     if return_coarse else []))}
+        lib = _lib.lib()
+        ws = torch.empty(lib.nerfgb_render_workspace_bytes(min(chunk, R), Sc, Sf), dtype=torch.uint8,
+                         device=rays_o.device)
+        pc, pf = self.coarse_model.packed(precision), self.fine_model.packed(precision)
+        for s in range(0, R, chunk):
+            e = min(R, s + chunk)
+            sl = slice(s, e)
+            _lib.call("nerfgb_render_rays", ptr(pc), ptr(pf), prec, ptr(rays_o[sl]), ptr(rays_d[sl]),
+                      ptr(near[sl]), ptr(far[sl]),
+                      ptr(u_coarse[sl]) if u_coarse is not None else None,
+                      ptr(u_fine[sl]) if u_fine is not None else None,
+                      ctypes.c_ulonglong(int(seed) + s), e - s, Sc, Sf,
+                      int(bool(self.params.sampling.perturb)),
+                      int(bool(self.params.sampling.lin_inv_depth)), int(self.white_bg),
+                      int(self.trans_mode),
+                      ptr(out["rgb_coarse"][sl]) if return_coarse else None,
+                      ptr(out["depth_coarse"][sl]) if return_coarse else None,
+                      ptr(out["acc_coarse"][sl]) if return_coarse else None,
+                      ptr(out["rgb"][sl]), ptr(out["depth"][sl]), ptr(out["acc"][sl]), ptr(ws),
+                      ptr(self.coarse_model.err_word), stream())
+        return out
+
+
+def psnr(y_true, y_pred):
+    """nerf/core/ops.py:249-257: per-element PSNR in dB (float64)."""
+    a = torch.as_tensor(y_true).double()
+    b = torch.as_tensor(y_pred).to(a.device).double()
+    mse = torch.mean((a - b) ** 2)
+    return float(-10.0 * torch.log10(mse))

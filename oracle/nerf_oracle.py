@@ -1,0 +1,376 @@
+"""numpy restatement of the nerf-tf2 render path. TEST INFRASTRUCTURE ONLY.
+
+Parity unpinned: TensorFlow 2.6 (the reference's runtime, pinned at
+requirements.txt:44) is absent, and the reference has no tests or golden
+vectors. Every function below restates the reference line by line and cites it.
+Each runs in float32 (the reference's precision) or float64 (the FP64 oracle
+pass), chosen by ``dtype``.
+
+The TensorFlow ops the reference calls are restated from their published
+semantics (tensorflow==2.6.0):
+  * ``tf.linspace(start, stop, num, axis)``: first point = start, last
+    point = stop, interior points ``start + i * ((stop - start) / (num - 1))``,
+    one multiply and one add per point (TF's ``linspace_nd``).
+  * ``tf.searchsorted(a, v, side='right')``: per row, ``std::upper_bound``
+    binary search. It returns the count of elements <= v on a sorted row.
+  * ``tf.reduce_sum`` and ``tf.cumsum``: TF does not specify an order. Here
+    both are sequential left to right in the working dtype. The CUDA kernels
+    use the same order, so the fine sampler's CDF and indices are bit-exact.
+  * ``tf.sort``: ascending. The permutation returned with it is the stable
+    argsort (ties keep concatenation order).
+"""
+import numpy as np
+
+F32 = np.float32
+F64 = np.float64
+
+# ---------------------------------------------------------------------------
+# Parameter layout of one coarse/fine network (nerf/core/model.py:334-394).
+# Flat blob order: dense_0..dense_7, sigma, dense_8, dense_9, rgb; per layer
+# the Keras kernel [in, out] row-major, then the bias [out].
+# ---------------------------------------------------------------------------
+LAYERS = (
+    ("dense_0", 63, 256), ("dense_1", 256, 256), ("dense_2", 256, 256),
+    ("dense_3", 256, 256), ("dense_4", 256, 256), ("dense_5", 319, 256),
+    ("dense_6", 256, 256), ("dense_7", 256, 256), ("sigma", 256, 1),
+    ("dense_8", 256, 256), ("dense_9", 283, 128), ("rgb", 128, 3),
+)
+
+
+def param_count():
+    return sum(i * o + o for _, i, o in LAYERS)
+
+
+def unpack_params(blob, dtype=F32):
+    """Flat blob -> {name: (W[in,out], b[out])}."""
+    blob = np.asarray(blob)
+    out, off = {}, 0
+    for name, i, o in LAYERS:
+        W = blob[off:off + i * o].reshape(i, o).astype(dtype)
+        off += i * o
+        b = blob[off:off + o].astype(dtype)
+        off += o
+        out[name] = (W, b)
+    assert off == blob.size
+    return out
+
+
+def pack_params(p):
+    parts = []
+    for name, i, o in LAYERS:
+        W, b = p[name]
+        parts += [np.asarray(W).reshape(-1), np.asarray(b).reshape(-1)]
+    return np.concatenate(parts)
+
+
+def glorot_params(seed, dtype=F32):
+    """Keras defaults: GlorotUniform kernel (limit sqrt(6/(in+out))), zero bias
+    (Dense defaults used at model.py:368,375,378,384,387)."""
+    rng = np.random.default_rng(seed)
+    p = {}
+    for name, i, o in LAYERS:
+        lim = np.sqrt(6.0 / (i + o))
+        p[name] = (rng.uniform(-lim, lim, size=(i, o)).astype(dtype),
+                   np.zeros(o, dtype))
+    return p
+
+
+# ---------------------------------------------------------------------------
+# Stratified coarse sampler: ray_utils.py:137-274
+# ---------------------------------------------------------------------------
+def tf_linspace(start, stop, num, dtype=F32):
+    """tf.linspace(start, stop, num, axis=1) for [R,1] start/stop -> [R,num]."""
+    start = np.asarray(start, dtype).reshape(-1, 1)
+    stop = np.asarray(stop, dtype).reshape(-1, 1)
+    n_steps = max(num - 1, 1)
+    delta = (stop - start) / dtype(n_steps)
+    i = np.arange(1, num - 1, dtype=dtype)[None, :]
+    mid = start + delta * i
+    return np.concatenate([start, mid, stop], axis=1)[:, :num]
+
+
+def bin_edges(near, far, n_coarse, lin_inv_depth, dtype=F32):
+    """ray_utils.py:183-206: linear in t, or linear in inverse depth."""
+    near = np.asarray(near, dtype).reshape(-1, 1)
+    far = np.asarray(far, dtype).reshape(-1, 1)
+    if not lin_inv_depth:
+        return tf_linspace(near, far, n_coarse + 1, dtype)
+    one = dtype(1)
+    return one / tf_linspace(one / near, one / far, n_coarse + 1, dtype)
+
+
+def create_input_batch_coarse_model(params, rays_o, rays_d, near, far,
+                                    u_vals=None, dtype=F32):
+    """ray_utils.py:137-274. ``u_vals`` [R, N_coarse] in [0,1) replaces the
+    internal tf.random.uniform draw at :230. When perturb is False the
+    reference raises NameError at :263 (bin_widths undefined); here the widths
+    are computed in both branches."""
+    S = params.sampling.N_coarse
+    rays_o = np.asarray(rays_o, dtype)
+    rays_d = np.asarray(rays_d, dtype)
+    edges = bin_edges(near, far, S, params.sampling.lin_inv_depth, dtype)  # :183-206
+    left = edges[:, :-1]                                                   # :212
+    right = edges[:, 1:]                                                   # :214
+    widths = right - left                                                  # :226
+    if params.sampling.perturb:
+        u = np.asarray(u_vals, dtype)
+        t = left + (u * widths)                                            # :234
+    else:
+        t = dtype(0.5) * (left + right)                                    # :243
+    xyz = rays_o[:, None, :] + t[..., None] * rays_d[:, None, :]           # :251
+    dirs = np.broadcast_to(rays_d[:, None, :], xyz.shape)                  # :253
+    return {
+        "xyz_inputs": xyz.reshape(-1, 3),
+        "dir_inputs": np.ascontiguousarray(dirs).reshape(-1, 3),
+        "bin_data": {"bin_edges": edges, "left_edges": left,
+                     "right_edges": right, "bin_widths": widths},
+        "t_vals": t,
+    }
+
+
+# ---------------------------------------------------------------------------
+# Inverse-transform fine sampler: ray_utils.py:276-406
+# ---------------------------------------------------------------------------
+def seq_sum(x):
+    """Left-to-right sum along axis 1 in x's dtype."""
+    acc = np.zeros(x.shape[0], x.dtype)
+    for j in range(x.shape[1]):
+        acc = acc + x[:, j]
+    return acc
+
+
+def seq_cumsum(x):
+    out = np.empty_like(x)
+    acc = np.zeros(x.shape[0], x.dtype)
+    for j in range(x.shape[1]):
+        acc = acc + x[:, j]
+        out[:, j] = acc
+    return out
+
+
+def upper_bound(a, v):
+    """Row-wise std::upper_bound(a[r], v[r, k]) (tf.searchsorted side='right',
+    ray_utils.py:363). a [R, n], v [R, m] -> int32 [R, m]."""
+    R, n = a.shape
+    first = np.zeros(v.shape, np.int64)
+    count = np.full(v.shape, n, np.int64)
+    rows = np.arange(R)[:, None]
+    while True:
+        active = count > 0
+        if not active.any():
+            break
+        step = count // 2
+        it = np.minimum(first + step, n - 1)
+        go_right = active & ~(v < a[rows, it])
+        first = np.where(go_right, first + step + 1, first)
+        count = np.where(active, np.where(go_right, count - step - 1, step), 0)
+    return first.astype(np.int32)
+
+
+def create_input_batch_fine_model(params, rays_o, rays_d, bin_weights, bin_data,
+                                  t_vals_coarse, u_vals, dtype=F32,
+                                  return_indices=False):
+    """ray_utils.py:276-406 with ``u_vals`` [R, N_fine] supplied in place of the
+    tf.random.uniform draw at :355 (``det`` is hard-wired False at :348)."""
+    rays_o = np.asarray(rays_o, dtype)
+    rays_d = np.asarray(rays_d, dtype)
+    left = np.asarray(bin_data["left_edges"], dtype)                       # :330
+    widths = np.asarray(bin_data["bin_widths"], dtype)                     # :331
+    w = np.asarray(bin_weights, dtype) + dtype(1e-5)                       # :335
+    denom = seq_sum(w * widths)[:, None]                                   # :338
+    pdf = w / denom                                                        # :339
+    agg = seq_cumsum(pdf * widths)                                         # :342
+    agg = np.concatenate([np.zeros_like(agg[:, :1]), agg], axis=1)         # :345
+    u = np.asarray(u_vals, dtype)
+    idx = upper_bound(agg[:, 1:-1], u)                                     # :363
+    rows = np.arange(u.shape[0])[:, None]
+    agg_ = agg[:, :-1][rows, idx]                                          # :366
+    pdf_ = pdf[rows, idx]                                                  # :367
+    left_ = left[rows, idx]                                                # :368
+    mask = np.where(pdf_ < dtype(1e-8), dtype(0), dtype(1))                # :372
+    pdf_ = np.maximum(pdf_, dtype(1e-8))                                   # :373
+    t_fine = (((u - agg_) / pdf_) * mask) + left_                          # :376
+    t_cat = np.concatenate([np.asarray(t_vals_coarse, dtype), t_fine], 1)  # :380
+    perm = np.argsort(t_cat, axis=1, kind="stable").astype(np.int32)       # :385
+    t = np.take_along_axis(t_cat, perm, axis=1)
+    xyz = rays_o[:, None, :] + t[..., None] * rays_d[:, None, :]           # :389
+    dirs = np.broadcast_to(rays_d[:, None, :], xyz.shape)                  # :392
+    out = {"xyz_inputs": xyz.reshape(-1, 3),
+           "dir_inputs": np.ascontiguousarray(dirs).reshape(-1, 3),
+           "t_vals": t}
+    if return_indices:
+        out["piece_idxs"] = idx
+        out["sort_perm"] = perm
+        out["t_vals_fine"] = t_fine
+    return out
+
+
+# ---------------------------------------------------------------------------
+# Compositing: ray_utils.py:408-551
+# ---------------------------------------------------------------------------
+def sigma_to_alpha(sigma, diffs):
+    """ray_utils.py:423."""
+    return 1 - np.exp(-sigma * diffs)
+
+
+def compute_weights(sigma, t_vals, N_samples):
+    """ray_utils.py:426-482. The exclusive cumprod is sequential (TF does not
+    specify an order)."""
+    dtype = t_vals.dtype.type
+    EPS, INF = dtype(1e-10), dtype(1e10)                                   # :458-459
+    diffs = t_vals[:, 1:] - t_vals[:, :-1]                                 # :462
+    diffs_ = np.concatenate(
+        [diffs, np.full((t_vals.shape[0], 1), INF, dtype)], axis=-1)       # :465-468
+    sigma_ = np.asarray(sigma, dtype).reshape(-1, N_samples)               # :474
+    alpha = sigma_to_alpha(sigma_, diffs_)                                 # :476
+    fac = dtype(1) - alpha + EPS                                           # :480
+    T = np.empty_like(fac)
+    acc = np.ones(fac.shape[0], dtype)
+    for j in range(fac.shape[1]):
+        T[:, j] = acc
+        acc = acc * fac[:, j]
+    return alpha * T
+
+
+def post_process_model_output(sample_rgb, sigma, t_vals, white_bg=False):
+    """ray_utils.py:484-551."""
+    t_vals = np.asarray(t_vals)
+    dtype = t_vals.dtype.type
+    N = t_vals.shape[1]
+    weights = compute_weights(np.asarray(sigma, dtype), t_vals, N)         # :528
+    rgb_ = np.asarray(sample_rgb, dtype).reshape(-1, N, 3)                 # :531
+    pred_rgb = np.sum(weights[..., None] * rgb_, axis=1)                   # :534
+    pred_depth = np.sum(t_vals * weights, axis=1)                          # :537
+    acc_map = np.sum(weights, axis=1)                                      # :540
+    if white_bg:
+        pred_rgb = pred_rgb + (1 - acc_map[:, None])                       # :544
+    return {"acc_map": acc_map, "weights": weights,
+            "pred_rgb": pred_rgb, "pred_depth": pred_depth}
+
+
+# ---------------------------------------------------------------------------
+# Positional encoder and MLP: model.py:289-394
+# ---------------------------------------------------------------------------
+def encoder_multipliers(L, dtype=F32):
+    """model.py:309-311: (2 ** range(L)) * pi. In float32, pi is rounded to
+    float32 first (np.pi enters a float32 tensor)."""
+    return (np.float64(2.0) ** np.arange(L)).astype(dtype) * dtype(np.pi)
+
+
+def positional_encoding(x, L, dtype=F32):
+    """model.py:319-331: [x, sin/cos interleaved], coordinate-major, then
+    frequency, then (sin, cos)."""
+    x = np.asarray(x, dtype)
+    expanded = x[..., None] * encoder_multipliers(L, dtype)[None, None, :]  # :323
+    sincos = np.stack([np.sin(expanded), np.cos(expanded)], axis=-1)       # :325-328
+    return np.concatenate([x, sincos.reshape(x.shape[0], -1)], axis=-1)    # :329-330
+
+
+def relu(x):
+    return np.maximum(x, 0)
+
+
+def sigmoid(x):
+    one = x.dtype.type(1)
+    return one / (one + np.exp(-x))
+
+
+def mlp_forward(p, xyz, dirs, dtype=F32, cache=False):
+    """get_coarse_or_fine_model (model.py:334-394) applied to (xyz, dirs).
+    Returns (rgb [M,3], sigma [M,1]) and, when ``cache``, the activations."""
+    p = {k: (np.asarray(W, dtype), np.asarray(b, dtype)) for k, (W, b) in p.items()}
+    enc_xyz = positional_encoding(xyz, 10, dtype)                          # :359
+    enc_dir = positional_encoding(dirs, 4, dtype)                          # :362
+    acts = {"enc_xyz": enc_xyz, "enc_dir": enc_dir}
+    h = enc_xyz
+    for i in range(8):                                                     # :366-372
+        W, b = p[f"dense_{i}"]
+        h = relu(h @ W + b)
+        acts[f"h{i}"] = h
+        if i == 4:
+            h = np.concatenate([h, enc_xyz], axis=-1)
+    W, b = p["sigma"]
+    sigma = relu(h @ W + b)                                                # :375
+    W, b = p["dense_8"]
+    bott = h @ W + b                                                       # :378
+    h9in = np.concatenate([bott, enc_dir], axis=-1)                        # :381
+    W, b = p["dense_9"]
+    h9 = relu(h9in @ W + b)                                                # :384
+    W, b = p["rgb"]
+    rgb = sigmoid(h9 @ W + b)                                              # :387
+    acts.update(bott=bott, h9=h9, sigma_pre=None)
+    if cache:
+        return rgb, sigma, acts
+    return rgb, sigma
+
+
+def nerf_forward(params, p_coarse, p_fine, rays_o, rays_d, near, far,
+                 u_coarse, u_fine, dtype=F32):
+    """NeRF.forward (model.py:57-125) with supplied uniforms."""
+    d_cm = create_input_batch_coarse_model(params, rays_o, rays_d, near, far,
+                                           u_coarse, dtype)
+    rgb_c, sig_c = mlp_forward(p_coarse, d_cm["xyz_inputs"], d_cm["dir_inputs"], dtype)
+    pp_cm = post_process_model_output(rgb_c, sig_c, d_cm["t_vals"],
+                                      params.system.white_bg)
+    d_fm = create_input_batch_fine_model(params, rays_o, rays_d, pp_cm["weights"],
+                                         d_cm["bin_data"], d_cm["t_vals"], u_fine,
+                                         dtype)
+    rgb_f, sig_f = mlp_forward(p_fine, d_fm["xyz_inputs"], d_fm["dir_inputs"], dtype)
+    pp_fm = post_process_model_output(rgb_f, sig_f, d_fm["t_vals"],
+                                      params.system.white_bg)
+    return pp_cm, pp_fm
+
+
+def psnr(y_true, y_pred):
+    """nerf/core/ops.py:249-257 (per-element mean)."""
+    mse = np.mean(np.square(np.asarray(y_true, F64) - np.asarray(y_pred, F64)))
+    return -10.0 * (np.log(mse) / np.log(10.0))
+
+
+# ---------------------------------------------------------------------------
+# Synthetic rays (test-side restatement of ray_utils.get_rays, :6-51)
+# ---------------------------------------------------------------------------
+def get_rays(H, W, intrinsic, c2w):
+    """ray_utils.py:6-51 in float64 (pose_utils.normalize uses EPS 1e-8)."""
+    u, v = np.meshgrid(np.arange(W, dtype=F64), np.arange(H, dtype=F64), indexing="xy")
+    x = (u - intrinsic[0, 2]) / intrinsic[0, 0]
+    y = (v - intrinsic[1, 2]) / intrinsic[1, 1]
+    d = np.stack([x, y, np.ones_like(x)], -1).reshape(-1, 3)
+    d = d @ c2w[:3, :3].T
+    d = d / (np.sqrt(np.sum(d ** 2, axis=1, keepdims=True)) + 1e-8)
+    o = np.broadcast_to(c2w[:3, 3], d.shape)
+    return o, d
+
+
+# ---------------------------------------------------------------------------
+# Philox4x32-10 in numpy (Salmon et al., SC 2011), to check the library's
+# device uniforms: element e of the stream keyed by seed is output (e mod 4)
+# of counter (e div 4), top 24 bits scaled to [0, 1).
+# ---------------------------------------------------------------------------
+def philox4x32_10(x0, x1, x2, x3, k0, k1):
+    """Ten Philox4x32 rounds on uint32 arrays; returns the four output words."""
+    M0, M1 = np.uint64(0xD2511F53), np.uint64(0xCD9E8D57)
+    W0, W1 = np.uint32(0x9E3779B9), np.uint32(0xBB67AE85)
+    x0, x1, x2, x3 = (np.asarray(v, np.uint32) for v in (x0, x1, x2, x3))
+    k0, k1 = np.uint32(k0), np.uint32(k1)
+    with np.errstate(over="ignore"):
+        for _ in range(10):
+            p0 = M0 * x0.astype(np.uint64)
+            p1 = M1 * x2.astype(np.uint64)
+            hi0, lo0 = (p0 >> np.uint64(32)).astype(np.uint32), p0.astype(np.uint32)
+            hi1, lo1 = (p1 >> np.uint64(32)).astype(np.uint32), p1.astype(np.uint32)
+            x0, x1, x2, x3 = hi1 ^ x1 ^ k0, lo1, hi0 ^ x3 ^ k1, lo0
+            k0 = np.uint32(k0 + W0)
+            k1 = np.uint32(k1 + W1)
+    return x0, x1, x2, x3
+
+
+def philox_uniform(seed, offset, n):
+    e = np.arange(offset, offset + n, dtype=np.uint64)
+    c = e >> np.uint64(2)
+    lo = (c & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    hi = (c >> np.uint64(32)).astype(np.uint32)
+    z = np.zeros_like(lo)
+    words = np.stack(philox4x32_10(lo, hi, z, z, seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF), axis=1)
+    w = words[np.arange(n), (e & np.uint64(3)).astype(np.int64)]
+    return (w >> np.uint32(8)).astype(np.float32) * np.float32(1.0 / 16777216.0)

@@ -1,0 +1,86 @@
+"""Parity of the MLP kernels with the CPU oracle (nerf/core/model.py:334-394).
+
+FP32 SIMT against the fp32 and fp64 oracle; BF16 tcgen05 against the fp64
+oracle with a BF16-sized tolerance.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+F32, F64 = np.float32, np.float64
+
+
+def dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(x):
+    return x.detach().cpu().numpy()
+
+
+def samples(n, seed, rows_per_dir=1):
+    rng = np.random.default_rng(seed)
+    x = rng.uniform(-4.0, 4.0, (n, 3)).astype(F32)
+    nd = (n + rows_per_dir - 1) // rows_per_dir
+    d = rng.normal(size=(nd, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(F32)
+    return x, d
+
+
+def biased_blob(ng, seed):
+    """Glorot kernels plus non-zero biases, so that every bias path is used."""
+    blob = ng.weights.glorot_blob(seed)
+    rng = np.random.default_rng(seed + 99)
+    for name, (ko, bo, i, o) in ng.weights.offsets().items():
+        blob[bo:bo + o] = rng.uniform(-0.1, 0.1, o)
+    return blob
+
+
+@pytest.mark.parametrize("n", [1000, 64, 1, 4097])
+def test_mlp_fp32_vs_oracle(ng, oracle, cuda, n):
+    blob = biased_blob(ng, 5)
+    x, d = samples(n, n)
+    mlp = ng.get_coarse_or_fine_model("coarse", params=blob, precision="fp32")
+    rgb, sigma = mlp((dev(x), dev(d)))
+    assert rgb.shape == (n, 3) and sigma.shape == (n, 1)
+    p32 = oracle.unpack_params(blob, F32)
+    r32, s32 = oracle.mlp_forward(p32, x, d, F32)
+    r64, s64 = oracle.mlp_forward(oracle.unpack_params(blob, F64), x, d, F64)
+    # tolerance: fp32 dot products of length <= 320 in another order, 10 layers
+    np.testing.assert_allclose(host(rgb), r32, atol=2e-5, rtol=0)
+    np.testing.assert_allclose(host(sigma), s32, atol=1e-4, rtol=1e-4)
+    np.testing.assert_allclose(host(rgb), r64, atol=1e-3, rtol=0)
+    np.testing.assert_allclose(host(sigma), s64, atol=2e-3, rtol=2e-3)
+
+
+def test_mlp_rows_per_dir(ng, cuda):
+    blob = biased_blob(ng, 6)
+    S = 192
+    x, d = samples(8 * S, 1, rows_per_dir=S)
+    mlp = ng.get_coarse_or_fine_model("fine", params=blob)
+    a_rgb, a_sig = mlp((dev(x), dev(d)), rows_per_dir=S)
+    b_rgb, b_sig = mlp((dev(x), dev(np.repeat(d, S, axis=0))))
+    assert torch.equal(a_rgb, b_rgb) and torch.equal(a_sig, b_sig)
+
+
+def test_mlp_empty(ng, cuda):
+    mlp = ng.get_coarse_or_fine_model("coarse")
+    rgb, sigma = mlp((torch.zeros(0, 3, device=cuda), torch.zeros(0, 3, device=cuda)))
+    assert rgb.shape == (0, 3) and sigma.shape == (0, 1)
+
+
+@pytest.mark.parametrize("n", [4096, 300, 1])
+def test_mlp_bf16_vs_fp64(ng, oracle, cuda, n):
+    blob = biased_blob(ng, 8)
+    x, d = samples(n, 11 + n)
+    mlp = ng.get_coarse_or_fine_model("coarse", params=blob, precision="bf16")
+    rgb, sigma = mlp((dev(x), dev(d)))
+    mlp.check_device_errors()
+    r64, s64 = oracle.mlp_forward(oracle.unpack_params(blob, F64), x, d, F64)
+    # BF16 operands (8-bit mantissa), FP32 accumulation over 10 layers
+    err_rgb = np.abs(host(rgb) - r64).max()
+    err_sig = np.abs(host(sigma) - s64).max() / max(1.0, np.abs(s64).max())
+    assert err_rgb < 2e-2, err_rgb
+    assert err_sig < 5e-2, err_sig
+    assert np.abs(host(rgb) - r64).mean() < 3e-3

@@ -1,0 +1,80 @@
+"""End-to-end parity of NeRF.forward (nerf/core/model.py:57-125) and of the fused
+render with the CPU oracle on the same rays, weights and uniforms."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+F32, F64 = np.float32, np.float64
+
+
+def dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(x):
+    return x.detach().cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def case(ng):
+    R = 96
+    o, d, n, f = ng.synthetic.sphere_rays(R, 42)
+    rng = np.random.default_rng(43)
+    uc = rng.random((R, 64), dtype=F32)
+    uf = rng.random((R, 128), dtype=F32)
+    bc, bf = ng.weights.glorot_blob(1), ng.weights.glorot_blob(2)
+    return R, o, d, n, f, uc, uf, bc, bf
+
+
+@pytest.mark.parametrize("white_bg", [False, True])
+def test_forward_fp32_vs_oracle(ng, oracle, cuda, case, white_bg):
+    R, o, d, n, f, uc, uf, bc, bf = case
+    p = ng.make_params(white_bg=white_bg)
+    nerf = ng.NeRF(p, precision="fp32", coarse_params=bc, fine_params=bf,
+                   trans_mode=ng._lib.TRANS_CUMPROD)
+    cm, fm = nerf.forward(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc), u_fine=dev(uf))
+    wcm, wfm = oracle.nerf_forward(p, oracle.unpack_params(bc), oracle.unpack_params(bf),
+                                   o, d, n, f, uc, uf, F32)
+    for got, want in ((cm, wcm), (fm, wfm)):
+        assert set(got) == {"acc_map", "weights", "pred_rgb", "pred_depth"}
+        np.testing.assert_allclose(host(got["pred_rgb"]), want["pred_rgb"], atol=1e-4)
+        np.testing.assert_allclose(host(got["acc_map"]), want["acc_map"], atol=1e-4)
+        np.testing.assert_allclose(host(got["pred_depth"]), want["pred_depth"], atol=5e-4)
+        np.testing.assert_allclose(host(got["weights"]), want["weights"], atol=1e-4)
+
+
+def test_forward_fp32_vs_fp64_oracle(ng, oracle, cuda, case):
+    R, o, d, n, f, uc, uf, bc, bf = case
+    p = ng.make_params()
+    nerf = ng.NeRF(p, precision="fp32", coarse_params=bc, fine_params=bf)
+    _, fm = nerf.forward(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc), u_fine=dev(uf))
+    _, wfm = oracle.nerf_forward(p, oracle.unpack_params(bc, F64), oracle.unpack_params(bf, F64),
+                                 o, d, n, f, uc.astype(F64), uf.astype(F64), F64)
+    err = np.abs(host(fm["pred_rgb"]) - wfm["pred_rgb"]).max()
+    assert err < 2e-3, err
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_fused_render_matches_forward(ng, cuda, case, precision):
+    R, o, d, n, f, uc, uf, bc, bf = case
+    p = ng.make_params()
+    nerf = ng.NeRF(p, precision=precision, coarse_params=bc, fine_params=bf)
+    cm, fm = nerf.forward(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc), u_fine=dev(uf))
+    out = nerf.render(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc), u_fine=dev(uf), chunk=40,
+                      return_coarse=True)
+    nerf.coarse_model.check_device_errors()
+    assert torch.equal(out["rgb"], fm["pred_rgb"])
+    assert torch.equal(out["depth"], fm["pred_depth"])
+    assert torch.equal(out["acc"], fm["acc_map"])
+    assert torch.equal(out["rgb_coarse"], cm["pred_rgb"])
+
+
+def test_render_default_uniforms_deterministic(ng, cuda, case):
+    R, o, d, n, f, uc, uf, bc, bf = case
+    nerf = ng.NeRF(ng.make_params(), coarse_params=bc, fine_params=bf)
+    a = nerf.render(dev(o), dev(d), dev(n), dev(f), seed=7)
+    b = nerf.render(dev(o), dev(d), dev(n), dev(f), seed=7)
+    c = nerf.render(dev(o), dev(d), dev(n), dev(f), seed=8)
+    assert torch.equal(a["rgb"], b["rgb"])
+    assert not torch.equal(a["rgb"], c["rgb"])
