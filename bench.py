@@ -46,7 +46,36 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--kernel", default=None, choices=["mlp"],
+                    help="run only the MLP kernel at the fine-pass launch shape (for ncu)")
+    ap.add_argument("--rows", type=int, default=CHUNK * (SC + SF))
     return ap.parse_args()
+
+
+def kernel_only(args):
+    """The MLP kernel alone, `--steps` launches on `--rows` rows (the fine pass
+    of one 4096-ray chunk by default). Prints the median launch time."""
+    import torch
+    ng = importlib.import_module("nerf-tf2_gb300")
+    dev = torch.device("cuda", 0)
+    torch.manual_seed(0)
+    xyz = torch.rand(args.rows, 3, device=dev) * 4 - 2
+    dirs = torch.nn.functional.normalize(torch.randn(args.rows, 3, device=dev), dim=1)
+    mlp = ng.get_coarse_or_fine_model("fine", seed=1, precision=args.path)
+    for _ in range(args.warmup):
+        mlp((xyz, dirs))
+    ts = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        mlp((xyz, dirs))
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    mlp.check_device_errors()
+    ms = statistics.median(ts)
+    print(json.dumps({"kernel": f"mlp_{args.path}", "rows": args.rows, "launch_ms": ms,
+                      "tflops": args.rows * FLOP_PER_SAMPLE / ms / 1e9}), flush=True)
 
 
 def dist_env():
@@ -155,6 +184,8 @@ def main():
     args = parse()
     if args.impl == "reference":
         return reference_arm(args)
+    if args.kernel == "mlp":
+        return kernel_only(args)
     import torch
     import torch.distributed as tdist
 

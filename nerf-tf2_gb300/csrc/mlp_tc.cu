@@ -2,14 +2,15 @@
 // sm_103a: tcgen05.mma with FP32 accumulators in TMEM, operands in shared
 // memory, weights streamed by the bulk-copy (TMA) engine.
 //
-// CTA tile: 256 sample rows = two 128-row sub-tiles (A, B) that share every
-// weight chunk, so each weight byte fetched from L2 feeds 256 rows. The
+// CTA tile: 256 sample rows = two 128-row sub-tiles (A, B) in ping-pong: the
+// tensor core runs layer g of A, then layer g of B, so the epilogue of A(g)
+// overlaps the MMAs of B(g) and the epilogue of B(g) those of A(g+1). The
 // whole 10-GEMM chain runs on chip: activations never leave shared memory and
 // only xyz/dirs (in) and rgb/sigma (out) touch HBM.
 //
 // Warp roles (18 warps):
 //   warp 0      weight producer: cp.async.bulk of 32-K weight chunks into a
-//               4-stage ring (full/empty mbarriers)
+//               3-stage ring (full/empty mbarriers), once per sub-tile
 //   warp 1      TMEM allocator and MMA issuer (one elected thread)
 //   warps 2-17  epilogue: 8 warps per sub-tile, one TMEM lane quadrant and
 //               one 128-column half per warp. They compute the positional
@@ -17,8 +18,9 @@
 //               add bias, apply ReLU, round to BF16 and write the next
 //               layer's A operand; the sigma and rgb heads run in FP32.
 //
-// Shared memory (bytes): ring [0,64K) | encA [64K,80K) | encB [80K,96K) |
-// actA [96K,160K) | actB [160K,224K) | barriers, sigma partials.
+// Shared memory (bytes): ring [0,48K) | encA [48K,64K) | encB [64K,80K) |
+// actA [80K,144K) | actB [144K,208K) | bias/head table (12,320 B) |
+// barriers, sigma partials.
 // Operand layout: K-major, no swizzle, 8x16-byte core matrices. Element
 // (r, k) of a 128-row operand sits at (k/8)*2048 + r*16 + (k%8)*2; weights
 // (n, k) of an N-row chunk at (k/8)*(N*16) + n*16 + (k%8)*2.
@@ -36,16 +38,16 @@ namespace nerfgb {
 namespace tc {
 
 constexpr int kRows = 256;          // rows per CTA tile
-constexpr int kStages = 4;          // weight ring depth
+constexpr int kStages = 3;          // weight ring depth
 constexpr int kChunkBytesMax = 256 * 32 * 2;
 constexpr int kThreads = 18 * 32;
-constexpr int kChunksPerTile = 77;  // (64 + 4*256 + 320 + 3*256 + 288) / 32
 
 constexpr uint32_t kRingOff = 0;
-constexpr uint32_t kEncOff = 64 * 1024;   // + s * 16K
-constexpr uint32_t kActOff = 96 * 1024;   // + s * 64K
-constexpr uint32_t kMiscOff = 224 * 1024;
-// misc: full[4] empty[4] accf[2] actr[2] drain (13 x 8 B), tmem slot, abort flag
+constexpr uint32_t kEncOff = 48 * 1024;   // + s * 16K
+constexpr uint32_t kActOff = 80 * 1024;   // + s * 64K
+constexpr uint32_t kTableOff = 208 * 1024;
+constexpr uint32_t kMiscOff = kTableOff + ((kTableElems * 4 + 127) / 128) * 128;
+// misc: full[4] empty[4] accf[2] actr[2] drain (8 B each), tmem slot, abort flag
 constexpr uint32_t kBarFull = kMiscOff;
 constexpr uint32_t kBarEmpty = kMiscOff + 32;
 constexpr uint32_t kBarAccf = kMiscOff + 64;
@@ -108,8 +110,9 @@ __device__ __forceinline__ void named_sync(int id, int threads) {
 }
 
 // 32 lanes x 32 columns of FP32 from TMEM; thread t gets lane (addr.lane + t).
-__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
-  uint32_t r[32];
+// The load is asynchronous until tmem_wait32, which also ties the registers
+// so no use can be scheduled before the wait.
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
       "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
@@ -119,9 +122,16 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
         "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]),
         "=r"(r[30]), "=r"(r[31])
       : "r"(taddr));
-  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-  for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(r[i]);
+}
+__device__ __forceinline__ void tmem_wait32(uint32_t (&r)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                 "+r"(r[15]), "+r"(r[16]), "+r"(r[17]), "+r"(r[18]), "+r"(r[19]), "+r"(r[20]), "+r"(r[21]),
+                 "+r"(r[22]), "+r"(r[23]), "+r"(r[24]), "+r"(r[25]), "+r"(r[26]), "+r"(r[27]), "+r"(r[28]),
+                 "+r"(r[29]), "+r"(r[30]), "+r"(r[31])
+               :
+               : "memory");
 }
 
 // Shared-memory matrix descriptor: K-major, no swizzle (layout type 0),
@@ -141,6 +151,12 @@ __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<uint32_t *>(&p);
 }
+// max(x, 0) of both values, rounded to BF16 and packed (lo in the low half).
+__device__ __forceinline__ uint32_t pack_bf16_relu(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
 
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
@@ -159,17 +175,6 @@ __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile
       return false;
     }
   }
-}
-
-// Chunk q of a tile -> layer g and chunk c within the layer.
-__device__ __forceinline__ void chunk_of(int q, int &g, int &c) {
-  g = 0;
-  int base = 0;
-  while (q >= base + gemm_kp(g) / 32) {
-    base += gemm_kp(g) / 32;
-    ++g;
-  }
-  c = q - base;
 }
 
 // ---------------------------------------------------------------------------
@@ -237,9 +242,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kAbort);
-  const float *table = reinterpret_cast<const float *>(packed + kBf16TableOff);
+  float *table = reinterpret_cast<float *>(smem + kTableOff);
   const long long ntiles = (n + kRows - 1) / kRows;
 
+  {  // bias and head table -> shared memory
+    const float4 *src = reinterpret_cast<const float4 *>(packed + kBf16TableOff);
+    for (int i = threadIdx.x; i < kTableElems / 4; i += kThreads) reinterpret_cast<float4 *>(table)[i] = src[i];
+  }
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(sbase + kBarFull + 8 * s, 1);
@@ -264,28 +273,32 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(smem + kTmemSlot);
 
   if (warp == 0) {
-    // ---------------- weight producer ----------------
+    // ---------------- weight producer: per tile, per layer, per sub-tile ----------------
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
       int issued = 0;
       bool ok = true;
       for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        for (int q = 0; q < kChunksPerTile; ++q) {
-          if (!wait_bar(sbase + kBarEmpty + 8 * stage, phase ^ 1, abort_flag, err)) {
-            ok = false;
-            break;
-          }
-          int g, c;
-          chunk_of(q, g, c);
+        for (int g = 0; g < kNumGemm && ok; ++g) {
           const uint32_t bytes = (uint32_t)gemm_n(g) * 64u;
-          const uint8_t *src = packed + gemm_w_offset(g) * 2 + (long long)c * bytes;
-          mbar_expect_tx(sbase + kBarFull + 8 * stage, bytes);
-          bulk_g2s(sbase + kRingOff + stage * kChunkBytesMax, src, bytes, sbase + kBarFull + 8 * stage);
-          ++issued;
-          if (++stage == kStages) {
-            stage = 0;
-            phase ^= 1;
+          const uint8_t *lsrc = packed + gemm_w_offset(g) * 2;
+          const int nch = gemm_kp(g) / 32;
+          for (int s = 0; s < 2 && ok; ++s) {
+            for (int c = 0; c < nch; ++c) {
+              if (!wait_bar(sbase + kBarEmpty + 8 * stage, phase ^ 1, abort_flag, err)) {
+                ok = false;
+                break;
+              }
+              mbar_expect_tx(sbase + kBarFull + 8 * stage, bytes);
+              bulk_g2s(sbase + kRingOff + stage * kChunkBytesMax, lsrc + (long long)c * bytes, bytes,
+                       sbase + kBarFull + 8 * stage);
+              ++issued;
+              if (++stage == kStages) {
+                stage = 0;
+                phase ^= 1;
+              }
+            }
           }
         }
       }
@@ -301,54 +314,51 @@ __global__ void __launch_bounds__(kThreads, 1)
       }
     }
   } else if (warp == 1) {
-    // ---------------- MMA issuer ----------------
+    // ---------------- MMA issuer: A(g), B(g), A(g+1), ... ----------------
     if (lane == 0) {
       int stage = 0;
-      uint32_t phase = 0, actr_phase = 0;
+      uint32_t phase = 0;
+      uint32_t actr_phase[2] = {0, 0};
       bool ok = true;
       int issued_any = 0;
       for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        int q = 0;
         for (int g = 0; g < kNumGemm && ok; ++g) {
-          if (!wait_bar(sbase + kBarActr, actr_phase, abort_flag, err) ||
-              !wait_bar(sbase + kBarActr + 8, actr_phase, abort_flag, err)) {
-            ok = false;
-            break;
-          }
-          actr_phase ^= 1;
-          tc_fence_after();
           const int N = gemm_n(g);
           const uint32_t idesc = idesc_bf16(128, N);
           const int nch = gemm_kp(g) / 32;
-          for (int c = 0; c < nch; ++c, ++q) {
-            if (!wait_bar(sbase + kBarFull + 8 * stage, phase, abort_flag, err)) {
+          for (int s = 0; s < 2 && ok; ++s) {
+            if (!wait_bar(sbase + kBarActr + 8 * s, actr_phase[s], abort_flag, err)) {
               ok = false;
               break;
             }
+            actr_phase[s] ^= 1;
             tc_fence_after();
-            const uint32_t wst = sbase + kRingOff + stage * kChunkBytesMax;
-            bool from_enc = (g == 0) || (g == 5 && c >= 8) || (g == 9 && c == 8);
-            int kg0 = (g == 0) ? 4 * c : (g == 5 && c >= 8) ? 4 * (c - 8) : (g == 9 && c == 8) ? 0 : 4 * c;
+            const uint32_t enc = sbase + kEncOff + s * 16384u, act = sbase + kActOff + s * 65536u;
+            for (int c = 0; c < nch; ++c) {
+              if (!wait_bar(sbase + kBarFull + 8 * stage, phase, abort_flag, err)) {
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+              const uint32_t wst = sbase + kRingOff + stage * kChunkBytesMax;
+              const bool from_enc = (g == 0) || (g == 5 && c >= 8) || (g == 9 && c == 8);
+              const int kg0 = (g == 0) ? 4 * c : (g == 5 && c >= 8) ? 4 * (c - 8) : (g == 9 && c == 8) ? 0 : 4 * c;
+              const uint32_t region = from_enc ? enc : act;
 #pragma unroll
-            for (int ks = 0; ks < 2; ++ks) {
-              const uint64_t bdesc = smem_desc(wst + (uint32_t)(2 * ks) * (N * 16), N * 16, 128);
-#pragma unroll
-              for (int s = 0; s < 2; ++s) {
-                const uint32_t region = sbase + (from_enc ? kEncOff + s * 16384u : kActOff + s * 65536u);
+              for (int ks = 0; ks < 2; ++ks) {
+                const uint64_t bdesc = smem_desc(wst + (uint32_t)(2 * ks) * (N * 16), N * 16, 128);
                 const uint64_t adesc = smem_desc(region + (uint32_t)(kg0 + 2 * ks) * 2048u, 2048, 128);
                 tc_mma(tmem + s * 256, adesc, bdesc, idesc, (c > 0 || ks > 0) ? 1u : 0u);
               }
+              issued_any = 1;
+              tc_commit(sbase + kBarEmpty + 8 * stage);
+              if (++stage == kStages) {
+                stage = 0;
+                phase ^= 1;
+              }
             }
-            issued_any = 1;
-            tc_commit(sbase + kBarEmpty + 8 * stage);
-            if (++stage == kStages) {
-              stage = 0;
-              phase ^= 1;
-            }
+            if (ok) tc_commit(sbase + kBarAccf + 8 * s);
           }
-          if (!ok) break;
-          tc_commit(sbase + kBarAccf);
-          tc_commit(sbase + kBarAccf + 8);
         }
       }
       if (issued_any) {
@@ -393,38 +403,47 @@ __global__ void __launch_bounds__(kThreads, 1)
         accf_phase ^= 1;
         tc_fence_after();
         const float *bias = table + bias_offset(g);
-        const bool relu = gemm_relu(g);
         float sig = 0.0f;
         if (!(g == 9 && hf == 1)) {
 #pragma unroll 1
           for (int j = 0; j < 4; ++j) {
-            float v[32];
-            tmem_ld32(trow + j * 32, v);
+            uint32_t raw[32];
+            tmem_ld32(trow + j * 32, raw);
             const int col0 = hf * 128 + j * 32;
+            float b[32];
 #pragma unroll
-            for (int i = 0; i < 32; ++i) {
-              v[i] += __ldg(bias + col0 + i);
-              if (relu) v[i] = fmaxf(v[i], 0.0f);
-            }
+            for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4 *>(b + i) = *reinterpret_cast<const float4 *>(bias + col0 + i);
+            tmem_wait32(raw);
+            float v[32];
+#pragma unroll
+            for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(raw[i]) + b[i];
             if (g == 7) {
               const float *ws = table + kSigmaWOff + col0;
 #pragma unroll
-              for (int i = 0; i < 32; ++i) sig = fmaf(v[i], __ldg(ws + i), sig);
+              for (int i = 0; i < 32; ++i) sig = fmaf(fmaxf(v[i], 0.0f), ws[i], sig);
             }
             if (g == 9) {
               const float *wr = table + kRgbWOff + col0 * 3;
 #pragma unroll
               for (int i = 0; i < 32; ++i) {
-                rgb_acc[0] = fmaf(v[i], __ldg(wr + 3 * i), rgb_acc[0]);
-                rgb_acc[1] = fmaf(v[i], __ldg(wr + 3 * i + 1), rgb_acc[1]);
-                rgb_acc[2] = fmaf(v[i], __ldg(wr + 3 * i + 2), rgb_acc[2]);
+                const float h = fmaxf(v[i], 0.0f);
+                rgb_acc[0] = fmaf(h, wr[3 * i], rgb_acc[0]);
+                rgb_acc[1] = fmaf(h, wr[3 * i + 1], rgb_acc[1]);
+                rgb_acc[2] = fmaf(h, wr[3 * i + 2], rgb_acc[2]);
               }
-            } else {
+            } else if (g == 8) {  // dense_8 is linear (model.py:377-378)
 #pragma unroll
               for (int kg = 0; kg < 4; ++kg)
                 st_shared_v4(act + (uint32_t)(col0 / 8 + kg) * 2048u + r * 16, pack_bf16(v[8 * kg], v[8 * kg + 1]),
                              pack_bf16(v[8 * kg + 2], v[8 * kg + 3]), pack_bf16(v[8 * kg + 4], v[8 * kg + 5]),
                              pack_bf16(v[8 * kg + 6], v[8 * kg + 7]));
+            } else {
+#pragma unroll
+              for (int kg = 0; kg < 4; ++kg)
+                st_shared_v4(act + (uint32_t)(col0 / 8 + kg) * 2048u + r * 16,
+                             pack_bf16_relu(v[8 * kg], v[8 * kg + 1]), pack_bf16_relu(v[8 * kg + 2], v[8 * kg + 3]),
+                             pack_bf16_relu(v[8 * kg + 4], v[8 * kg + 5]),
+                             pack_bf16_relu(v[8 * kg + 6], v[8 * kg + 7]));
             }
           }
         }
@@ -432,7 +451,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           // sigma = ReLU(h7 . w + b) (model.py:374-375), halves summed in FP32.
           if (hf == 1) sig_part[r] = sig;
           named_sync(1 + s, 256);
-          if (hf == 0 && valid) sigma_out[grow] = fmaxf(sig + sig_part[r] + __ldg(table + kSigmaBOff), 0.0f);
+          if (hf == 0 && valid) sigma_out[grow] = fmaxf(sig + sig_part[r] + table[kSigmaBOff], 0.0f);
         }
         if (g == 8 && hf == 0) {
           // enc_dir into the enc region (enc_xyz was last read by dense_5).
@@ -446,7 +465,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (hf == 0 && valid) {
 #pragma unroll
             for (int c = 0; c < 3; ++c)
-              rgb_out[grow * 3 + c] = 1.0f / (1.0f + expf(-(rgb_acc[c] + __ldg(table + kRgbBOff + c))));
+              rgb_out[grow * 3 + c] = 1.0f / (1.0f + expf(-(rgb_acc[c] + table[kRgbBOff + c])));
           }
         } else {
           fence_proxy_async();
