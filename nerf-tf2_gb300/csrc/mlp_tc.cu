@@ -2,15 +2,17 @@
 // sm_103a: tcgen05.mma with FP32 accumulators in TMEM, operands in shared
 // memory, weights streamed by the bulk-copy (TMA) engine.
 //
-// CTA tile: 256 sample rows = two 128-row sub-tiles (A, B) in ping-pong: the
-// tensor core runs layer g of A, then layer g of B, so the epilogue of A(g)
-// overlaps the MMAs of B(g) and the epilogue of B(g) those of A(g+1). The
-// whole 10-GEMM chain runs on chip: activations never leave shared memory and
-// only xyz/dirs (in) and rgb/sigma (out) touch HBM.
+// CTA tile: 256 sample rows = two 128-row sub-tiles (A, B). Two schedules
+// are compiled from one source: lockstep (A and B consume every weight chunk
+// together, so each weight byte fetched from L2 feeds 256 rows) and ping-pong
+// (the tensor core runs layer g of A, then of B, so each sub-tile's epilogue
+// overlaps the other's MMAs, at twice the weight traffic). The whole 10-GEMM
+// chain runs on chip: activations never leave shared memory and only
+// xyz/dirs (in) and rgb/sigma (out) touch HBM.
 //
 // Warp roles (18 warps):
 //   warp 0      weight producer: cp.async.bulk of 32-K weight chunks into a
-//               3-stage ring (full/empty mbarriers), once per sub-tile
+//               3-stage ring (full/empty mbarriers), one lane per stage
 //   warp 1      TMEM allocator and MMA issuer (one elected thread)
 //   warps 2-17  epilogue: 8 warps per sub-tile, one TMEM lane quadrant and
 //               one 128-column half per warp. They compute the positional
@@ -38,8 +40,7 @@ namespace nerfgb {
 namespace tc {
 
 constexpr int kRows = 256;          // rows per CTA tile
-constexpr int kStages = 3;          // weight ring depth
-constexpr int kChunkBytesMax = 256 * 32 * 2;
+constexpr uint32_t kRingBytes = 48 * 1024;  // weight ring: kRingBytes / (N*KCH*2) stages
 constexpr int kThreads = 18 * 32;
 
 constexpr uint32_t kRingOff = 0;
@@ -48,14 +49,14 @@ constexpr uint32_t kActOff = 80 * 1024;   // + s * 64K
 constexpr uint32_t kTableOff = 208 * 1024;
 constexpr uint32_t kMiscOff = kTableOff + ((kTableElems * 4 + 127) / 128) * 128;
 // misc: full[4] empty[4] accf[2] actr[2] drain (8 B each), tmem slot, abort flag
-constexpr uint32_t kBarFull = kMiscOff;
-constexpr uint32_t kBarEmpty = kMiscOff + 32;
-constexpr uint32_t kBarAccf = kMiscOff + 64;
-constexpr uint32_t kBarActr = kMiscOff + 80;
-constexpr uint32_t kBarDrain = kMiscOff + 96;
-constexpr uint32_t kTmemSlot = kMiscOff + 104;
-constexpr uint32_t kAbort = kMiscOff + 108;
-constexpr uint32_t kSigPart = kMiscOff + 128;  // float [2][128]
+constexpr uint32_t kBarFull = kMiscOff;          // [8]
+constexpr uint32_t kBarEmpty = kMiscOff + 64;    // [8]
+constexpr uint32_t kBarAccf = kMiscOff + 128;    // [2]
+constexpr uint32_t kBarActr = kMiscOff + 144;    // [2]
+constexpr uint32_t kBarDrain = kMiscOff + 160;
+constexpr uint32_t kTmemSlot = kMiscOff + 168;
+constexpr uint32_t kAbort = kMiscOff + 172;
+constexpr uint32_t kSigPart = kMiscOff + 192;  // float [2][128]
 constexpr uint32_t kSmemBytes = kSigPart + 2 * 128 * 4;
 
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
@@ -234,6 +235,11 @@ __device__ __forceinline__ void write_enc_dir(uint32_t enc, int r, const float (
 // ---------------------------------------------------------------------------
 // The kernel
 // ---------------------------------------------------------------------------
+// KCH: K rows per weight chunk; NST: ring stages. PINGPONG: the tensor core
+// runs A(g) then B(g), each streaming the layer's weights (epilogues overlap
+// MMAs); otherwise A and B share every chunk in lockstep (half the weight
+// traffic, epilogues exposed).
+template <int KCH, int NST, bool PINGPONG>
 __global__ void __launch_bounds__(kThreads, 1)
     mlp_bf16_kernel(const uint8_t *__restrict__ packed, const float *__restrict__ xyz,
                     const float *__restrict__ dirs, long long n, int rpd, float *__restrict__ rgb_out,
@@ -250,7 +256,7 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (int i = threadIdx.x; i < kTableElems / 4; i += kThreads) reinterpret_cast<float4 *>(table)[i] = src[i];
   }
   if (threadIdx.x == 0) {
-    for (int s = 0; s < kStages; ++s) {
+    for (int s = 0; s < NST; ++s) {
       mbar_init(sbase + kBarFull + 8 * s, 1);
       mbar_init(sbase + kBarEmpty + 8 * s, 1);
     }
@@ -273,48 +279,45 @@ __global__ void __launch_bounds__(kThreads, 1)
   const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(smem + kTmemSlot);
 
   if (warp == 0) {
-    // ---------------- weight producer: per tile, per layer, per sub-tile ----------------
-    if (lane == 0) {
-      int stage = 0;
+    // ---------------- weight producer ----------------
+    // Lane l owns ring stage l and issues every NST-th chunk: bulk copies
+    // issued by one thread complete one after another, copies issued by
+    // different threads overlap.
+    if (lane < NST) {
+      const int st = lane;
       uint32_t phase = 0;
-      int issued = 0;
-      bool ok = true;
+      long long q = 0;  // chunk counter over the CTA's whole sequence
+      bool ok = true, issued = false;
       for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         for (int g = 0; g < kNumGemm && ok; ++g) {
-          const uint32_t bytes = (uint32_t)gemm_n(g) * 64u;
+          const uint32_t bytes = (uint32_t)gemm_n(g) * KCH * 2u;
           const uint8_t *lsrc = packed + gemm_w_offset(g) * 2;
-          const int nch = gemm_kp(g) / 32;
-          for (int s = 0; s < 2 && ok; ++s) {
-            for (int c = 0; c < nch; ++c) {
-              if (!wait_bar(sbase + kBarEmpty + 8 * stage, phase ^ 1, abort_flag, err)) {
+          const int nch = gemm_kp(g) / KCH;
+          for (int s = 0; s < (PINGPONG ? 2 : 1) && ok; ++s) {
+            for (int c = 0; c < nch; ++c, ++q) {
+              if ((int)(q % NST) != st) continue;
+              if (!wait_bar(sbase + kBarEmpty + 8 * st, phase ^ 1, abort_flag, err)) {
                 ok = false;
                 break;
               }
-              mbar_expect_tx(sbase + kBarFull + 8 * stage, bytes);
-              bulk_g2s(sbase + kRingOff + stage * kChunkBytesMax, lsrc + (long long)c * bytes, bytes,
-                       sbase + kBarFull + 8 * stage);
-              ++issued;
-              if (++stage == kStages) {
-                stage = 0;
-                phase ^= 1;
-              }
+              mbar_expect_tx(sbase + kBarFull + 8 * st, bytes);
+              bulk_g2s(sbase + kRingOff + st * (256 * KCH * 2), lsrc + (long long)c * bytes, bytes,
+                       sbase + kBarFull + 8 * st);
+              issued = true;
+              phase ^= 1;
             }
           }
         }
       }
-      if (!ok) {
-        // Drain: wait (bounded) for the copies of the stages still in flight.
-        for (int k = 0; k < kStages && k < issued; ++k) {
-          int st = (stage + kStages - 1 - k) % kStages;
-          uint32_t ph = (st < stage) ? phase : phase ^ 1;
-          uint64_t t0 = globaltimer();
-          while (!mbar_try(sbase + kBarFull + 8 * st, ph) && globaltimer() - t0 < 10000000ull) {
-          }
+      if (!ok && issued) {
+        // Drain: wait (bounded) for this stage's copy still in flight.
+        uint64_t t0 = globaltimer();
+        while (!mbar_try(sbase + kBarFull + 8 * st, phase ^ 1) && globaltimer() - t0 < 10000000ull) {
         }
       }
     }
   } else if (warp == 1) {
-    // ---------------- MMA issuer: A(g), B(g), A(g+1), ... ----------------
+    // ---------------- MMA issuer ----------------
     if (lane == 0) {
       int stage = 0;
       uint32_t phase = 0;
@@ -325,39 +328,49 @@ __global__ void __launch_bounds__(kThreads, 1)
         for (int g = 0; g < kNumGemm && ok; ++g) {
           const int N = gemm_n(g);
           const uint32_t idesc = idesc_bf16(128, N);
-          const int nch = gemm_kp(g) / 32;
-          for (int s = 0; s < 2 && ok; ++s) {
-            if (!wait_bar(sbase + kBarActr + 8 * s, actr_phase[s], abort_flag, err)) {
-              ok = false;
-              break;
+          const int nch = gemm_kp(g) / KCH;
+          // PINGPONG: pass s serves sub-tile s. Lockstep: one pass serves both.
+          for (int pass = 0; pass < (PINGPONG ? 2 : 1) && ok; ++pass) {
+            const int s_lo = PINGPONG ? pass : 0, s_hi = PINGPONG ? pass : 1;
+            for (int s = s_lo; s <= s_hi; ++s) {
+              if (!wait_bar(sbase + kBarActr + 8 * s, actr_phase[s], abort_flag, err)) {
+                ok = false;
+                break;
+              }
+              actr_phase[s] ^= 1;
             }
-            actr_phase[s] ^= 1;
+            if (!ok) break;
             tc_fence_after();
-            const uint32_t enc = sbase + kEncOff + s * 16384u, act = sbase + kActOff + s * 65536u;
             for (int c = 0; c < nch; ++c) {
               if (!wait_bar(sbase + kBarFull + 8 * stage, phase, abort_flag, err)) {
                 ok = false;
                 break;
               }
               tc_fence_after();
-              const uint32_t wst = sbase + kRingOff + stage * kChunkBytesMax;
-              const bool from_enc = (g == 0) || (g == 5 && c >= 8) || (g == 9 && c == 8);
-              const int kg0 = (g == 0) ? 4 * c : (g == 5 && c >= 8) ? 4 * (c - 8) : (g == 9 && c == 8) ? 0 : 4 * c;
-              const uint32_t region = from_enc ? enc : act;
+              const uint32_t wst = sbase + kRingOff + stage * (256 * KCH * 2);
+              // K rows [k0, k0 + KCH) of this layer's input: enc_xyz for dense_0,
+              // [h | enc_xyz] for dense_5, [bottleneck | enc_dir] for dense_9.
+              const int k0 = c * KCH;
+              const bool from_enc = (g == 0) || ((g == 5 || g == 9) && k0 >= 256);
+              const int kg0 = (g == 0 || !from_enc) ? k0 / 8 : (k0 - 256) / 8;
 #pragma unroll
-              for (int ks = 0; ks < 2; ++ks) {
+              for (int ks = 0; ks < KCH / 16; ++ks) {
                 const uint64_t bdesc = smem_desc(wst + (uint32_t)(2 * ks) * (N * 16), N * 16, 128);
-                const uint64_t adesc = smem_desc(region + (uint32_t)(kg0 + 2 * ks) * 2048u, 2048, 128);
-                tc_mma(tmem + s * 256, adesc, bdesc, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+                for (int s = s_lo; s <= s_hi; ++s) {
+                  const uint32_t region = from_enc ? sbase + kEncOff + s * 16384u : sbase + kActOff + s * 65536u;
+                  const uint64_t adesc = smem_desc(region + (uint32_t)(kg0 + 2 * ks) * 2048u, 2048, 128);
+                  tc_mma(tmem + s * 256, adesc, bdesc, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+                }
               }
               issued_any = 1;
               tc_commit(sbase + kBarEmpty + 8 * stage);
-              if (++stage == kStages) {
+              if (++stage == NST) {
                 stage = 0;
                 phase ^= 1;
               }
             }
-            if (ok) tc_commit(sbase + kBarAccf + 8 * s);
+            if (!ok) break;
+            for (int s = s_lo; s <= s_hi; ++s) tc_commit(sbase + kBarAccf + 8 * s);
           }
         }
       }
@@ -486,18 +499,28 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 }  // namespace tc
 
-int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
-                    float *sigma, int *err_word, cudaStream_t stream) {
-  if (cudaFuncSetAttribute(tc::mlp_bf16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)tc::kSmemBytes) != cudaSuccess)
+template <int KCH, int NST, bool PP>
+static int launch_variant(const void *packed, const float *xyz, const float *dirs, long long n, int rpd,
+                          float *rgb, float *sigma, int *err_word, cudaStream_t stream) {
+  static_assert(NST * 256 * KCH * 2 <= (int)tc::kRingBytes && NST <= 8, "ring does not fit");
+  auto kern = tc::mlp_bf16_kernel<KCH, NST, PP>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kSmemBytes) != cudaSuccess)
     return NERFGB_E_CUDA;
   const long long ntiles = (n + tc::kRows - 1) / tc::kRows;
   const int sms = num_sms();
   if (sms <= 0) return NERFGB_E_DEVICE;
   const int grid = (int)(ntiles < sms ? ntiles : sms);
-  tc::mlp_bf16_kernel<<<grid, tc::kThreads, tc::kSmemBytes, stream>>>(
-      reinterpret_cast<const uint8_t *>(packed), xyz, dirs, n, rpd, rgb, sigma, err_word);
+  kern<<<grid, tc::kThreads, tc::kSmemBytes, stream>>>(reinterpret_cast<const uint8_t *>(packed), xyz, dirs, n,
+                                                          rpd, rgb, sigma, err_word);
   return launch_status();
+}
+
+int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
+                    float *sigma, int *err_word, cudaStream_t stream) {
+  // Lockstep, 32-K chunks, 3 stages: a 48 KB ring cannot cover the bulk-copy
+  // round trip for the ping-pong schedule's weight rate (64 B/clk/SM), while
+  // lockstep needs half of it.
+  return launch_variant<32, 3, false>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
 }
 
 }  // namespace nerfgb
