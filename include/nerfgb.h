@@ -37,6 +37,7 @@ extern "C" {
 #define NERFGB_E_CUDA (-3)        /* CUDA launch or runtime error              */
 #define NERFGB_E_TIMEOUT (-4)     /* a bounded device wait ran out            */
 #define NERFGB_E_DEVICE (-5)      /* no usable sm_103 device                  */
+#define NERFGB_E_SCRATCH_LIMIT (-6) /* request needs more than the built-in scratch */
 
 /* MLP arithmetic precision. */
 #define NERFGB_PREC_FP32 0 /* FP32 SIMT, FP32 accumulate                      */
@@ -157,6 +158,36 @@ int nerfgb_render_rays(const void *packed_coarse, const void *packed_fine,
                        float *acc_coarse, float *rgb_fine, float *depth_fine,
                        float *acc_fine, void *workspace, int *err_word,
                        void *stream);
+
+/* ---- fused render without allocation --------------------------------- */
+
+/* Size of the built-in scratch array of nerfgb_render_rays_noalloc: 16 MiB,
+ * enough for 1,700 rays per call at 64 coarse + 128 fine samples
+ * (nerfgb_render_workspace_bytes gives the need of a request). */
+#define NERFGB_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* No counterpart in the reference. nerfgb_render_rays for callers that
+ * cannot allocate device memory (for example code running inside a framework
+ * that has reserved the GPU's memory for its own allocator, as TensorFlow
+ * does): same arguments without `workspace`. The intermediates live in a
+ * library-owned device array of NERFGB_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading this code holds until the process exits; the call allocates
+ * nothing. Requests needing more return NERFGB_E_SCRATCH_LIMIT (render in
+ * smaller chunks). The first call on a device looks up the array's address;
+ * make it before any stream capture. All calls share the array: calls that
+ * overlap on the GPU race and must be serialised. */
+int nerfgb_render_rays_noalloc(const void *packed_coarse,
+                               const void *packed_fine, int precision,
+                               const float *rays_o, const float *rays_d,
+                               const float *near, const float *far,
+                               const float *u_coarse, const float *u_fine,
+                               unsigned long long seed, int n_rays,
+                               int n_coarse, int n_fine, int perturb,
+                               int lin_inv_depth, int white_bg,
+                               int trans_mode, float *rgb_coarse,
+                               float *depth_coarse, float *acc_coarse,
+                               float *rgb_fine, float *depth_fine,
+                               float *acc_fine, int *err_word, void *stream);
 
 #ifdef __cplusplus
 }

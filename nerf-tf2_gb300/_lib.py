@@ -21,6 +21,7 @@ E_UNSUPPORTED = -2
 E_CUDA = -3
 E_TIMEOUT = -4
 E_DEVICE = -5
+E_SCRATCH_LIMIT = -6
 PREC_FP32 = 0
 PREC_BF16 = 1
 TRANS_CUMPROD = 0
@@ -43,6 +44,8 @@ SIGNATURES = {
     "nerfgb_render_workspace_bytes": (LL, [I, I, I]),
     "nerfgb_render_rays": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
                                P, P, P, P, P, P, P, P, P]),
+    "nerfgb_render_rays_noalloc": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
+                                       P, P, P, P, P, P, P, P]),
 }
 
 

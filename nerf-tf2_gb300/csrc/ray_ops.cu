@@ -351,6 +351,7 @@ extern "C" const char *nerfgb_status_string(int s) {
     case NERFGB_E_CUDA: return "NERFGB_E_CUDA";
     case NERFGB_E_TIMEOUT: return "NERFGB_E_TIMEOUT";
     case NERFGB_E_DEVICE: return "NERFGB_E_DEVICE";
+    case NERFGB_E_SCRATCH_LIMIT: return "NERFGB_E_SCRATCH_LIMIT";
     default: return "NERFGB_E_UNKNOWN";
   }
 }
