@@ -159,6 +159,76 @@ int nerfgb_render_rays(const void *packed_coarse, const void *packed_fine,
                        float *acc_fine, void *workspace, int *err_word,
                        void *stream);
 
+/* ---- learned proposal sampler (not in the reference) ------------------- */
+
+/* Parameters of the proposal network: a 2x64 ReLU MLP on the L=6 positional
+ * encoding of xyz (39 inputs) with a softplus density output. Flat float32
+ * blob of 6,785 values: W1 [39,64], b1 [64], W2 [64,64], b2 [64], W3 [64],
+ * b3 [1]. */
+long long nerfgb_proposal_param_count(void);
+
+/* sigma [n] = proposal density at xyz [n,3]. */
+int nerfgb_proposal_forward(const float *params, const float *xyz, long long n,
+                            float *sigma, void *stream);
+
+/* grad_params [6785] += d/dparams of sum_i grad_sigma[i] * sigma_i
+ * (accumulates; zero it first). */
+int nerfgb_proposal_backward(const float *params, const float *xyz,
+                             const float *grad_sigma, long long n,
+                             float *grad_params, void *stream);
+
+/* nerfgb_render_rays with the proposal network in place of the coarse MLP:
+ * its density at the Sc stratified samples, composited as the coarse pass
+ * is, gives the PDF of the fine sampler; the fine MLP then runs on the
+ * Sc + Sf sorted samples. Outputs the fine rgb/depth/acc maps. Same
+ * workspace size as nerfgb_render_rays. */
+int nerfgb_render_rays_proposal(const float *proposal_params,
+                                const void *packed_fine, int precision,
+                                const float *rays_o, const float *rays_d,
+                                const float *near, const float *far,
+                                const float *u_coarse, const float *u_fine,
+                                unsigned long long seed, int n_rays,
+                                int n_coarse, int n_fine, int perturb,
+                                int lin_inv_depth, int white_bg,
+                                int trans_mode, float *rgb_fine,
+                                float *depth_fine, float *acc_fine,
+                                void *workspace, int *err_word, void *stream);
+
+/* ---- training --------------------------------------------------------- */
+
+/* Gradient of compositing (ray_utils.py:408-551, differentiated as
+ * tf.GradientTape does at nerf/core/model.py:148-170): given dL/dpred_rgb
+ * [R,3] and/or dL/dweights [R,S] (either may be NULL, not both), writes
+ * dL/dsigma [R*S] and, when grad_sample_rgb is not NULL, dL/dsample_rgb
+ * [R*S,3]. sample_rgb is needed only with grad_rgb_map. */
+int nerfgb_composite_backward(const float *sigma, const float *t_vals,
+                              const float *sample_rgb,
+                              const float *grad_rgb_map,
+                              const float *grad_weights, int n_rays,
+                              int n_samples, int white_bg, float *grad_sigma,
+                              float *grad_sample_rgb, void *stream);
+
+/* keras.losses.MeanSquaredError (nerf/core/model.py:32, :157-168) over n
+ * elements, times `scale`: *loss += scale * mean((pred - target)^2) (loss may
+ * be NULL), grad[i] = scale * 2 (pred - target) / n (grad may be NULL). */
+int nerfgb_mse_loss(const float *pred, const float *target, long long n,
+                    float scale, float *loss, float *grad, void *stream);
+
+/* Envelope loss of the proposal on weight histograms [R, n_bins]:
+ * *loss += sum (1 + lam [w_prop < w_target]) (w_prop - w_target)^2 / R;
+ * grad = dloss/dw_prop. */
+int nerfgb_envelope_loss(const float *w_prop, const float *w_target,
+                         int n_rays, int n_bins, float lam, float *loss,
+                         float *grad, void *stream);
+
+/* One Adam step as TensorFlow's ApplyAdam computes it for Keras Adam
+ * (nerf/core/model.py:413-418): lr_t = lr sqrt(1 - b2^step) / (1 - b1^step);
+ * m += (g - m)(1 - b1); v += (g^2 - v)(1 - b2); p -= lr_t m / (sqrt(v) + eps).
+ * step >= 1. */
+int nerfgb_adam_step(float *params, float *m, float *v, const float *grads,
+                     long long n, float lr, float beta1, float beta2,
+                     float eps, long long step, void *stream);
+
 /* ---- fused render without allocation --------------------------------- */
 
 /* Size of the built-in scratch array of nerfgb_render_rays_noalloc: 16 MiB,

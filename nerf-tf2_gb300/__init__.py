@@ -10,11 +10,12 @@ Submodules mirror the reference's modules: ``ray_utils`` (nerf/utils/
 ray_utils.py) and ``model`` (nerf/core/model.py). The kernels live in
 libnerfgb.so (C ABI: include/nerfgb.h), built by ``build.py``.
 """
-from . import ray_utils, synthetic, weights  # noqa: F401
+from . import proposal, ray_utils, synthetic, weights  # noqa: F401
 from ._lib import NerfgbError, lib  # noqa: F401
 from .config import make_params  # noqa: F401
 from .model import (NeRF, NerfMLP, PositionalEncoder,  # noqa: F401
                     get_coarse_or_fine_model, psnr)
+from .proposal import ProposalNetwork, ProposalTrainer  # noqa: F401
 from .ray_utils import (compute_weights, create_input_batch_coarse_model,  # noqa: F401
                         create_input_batch_fine_model, post_process_model_output,
                         set_seed, sigma_to_alpha)

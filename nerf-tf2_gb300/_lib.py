@@ -13,6 +13,7 @@ P = ctypes.c_void_p
 I = ctypes.c_int
 LL = ctypes.c_longlong
 ULL = ctypes.c_ulonglong
+F = ctypes.c_float
 
 # Status codes and enums (include/nerfgb.h).
 OK = 0
@@ -44,6 +45,15 @@ SIGNATURES = {
     "nerfgb_render_workspace_bytes": (LL, [I, I, I]),
     "nerfgb_render_rays": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
                                P, P, P, P, P, P, P, P, P]),
+    "nerfgb_proposal_param_count": (LL, []),
+    "nerfgb_proposal_forward": (I, [P, P, LL, P, P]),
+    "nerfgb_proposal_backward": (I, [P, P, P, LL, P, P]),
+    "nerfgb_render_rays_proposal": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
+                                        P, P, P, P, P, P]),
+    "nerfgb_composite_backward": (I, [P, P, P, P, P, I, I, I, P, P, P]),
+    "nerfgb_mse_loss": (I, [P, P, LL, F, P, P, P]),
+    "nerfgb_envelope_loss": (I, [P, P, I, I, F, P, P, P]),
+    "nerfgb_adam_step": (I, [P, P, P, P, LL, F, F, F, F, LL, P]),
     "nerfgb_render_rays_noalloc": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
                                        P, P, P, P, P, P, P, P]),
 }

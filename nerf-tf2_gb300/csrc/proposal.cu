@@ -1,0 +1,244 @@
+// Learned proposal sampler (not in the reference): a 2x64 ReLU MLP on the
+// L=6 positional encoding of xyz (39 inputs, the concatenation convention of
+// nerf/core/model.py:323-330) with a softplus density output. At inference
+// its density at the 64 stratified samples, composited exactly as the coarse
+// pass is (ray_utils.py:426-482), replaces the coarse MLP's weights as the
+// PDF of the inverse-transform fine sampler (ray_utils.py:276-406).
+//
+// Parameters (flat float32, 6,785 values): W1 [39,64], b1 [64], W2 [64,64],
+// b2 [64], W3 [64], b3 [1].
+//
+// Forward: one thread per sample, weights broadcast from shared memory.
+// Backward: recompute per 128-sample tile; per-sample vectors go to shared
+// memory (odd row strides, conflict-free), then each thread reduces its own
+// slice of dW over the tile in registers and adds it to the CTA's gradient
+// in shared memory; one atomicAdd per parameter per CTA at the end.
+#include <math.h>
+
+#include "common.cuh"
+#include "mlp_internal.cuh"
+
+namespace nerfgb {
+namespace prop {
+
+constexpr int kIn = 39, kH = 64;
+constexpr int kW1 = 0, kB1 = kW1 + kIn * kH, kW2 = kB1 + kH, kB2 = kW2 + kH * kH, kW3 = kB2 + kH, kB3 = kW3 + kH;
+constexpr int kParams = kB3 + 1;  // 6785
+constexpr int kThreads = 128;
+constexpr int kEncLd = 41, kRowLd = 65;
+
+__device__ __forceinline__ void encode6(const float x[3], float enc[kIn]) {
+  enc[0] = x[0];
+  enc[1] = x[1];
+  enc[2] = x[2];
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int l = 0; l < 6; ++l) {
+      float s, co;
+      sincosf(fmul(x[c], enc_multiplier(l)), &s, &co);
+      enc[3 + c * 12 + 2 * l] = s;
+      enc[3 + c * 12 + 2 * l + 1] = co;
+    }
+}
+
+__device__ __forceinline__ float softplus(float z) { return fmaxf(z, 0.0f) + log1pf(expf(-fabsf(z))); }
+
+__device__ __forceinline__ void load_params(const float *__restrict__ p, float *sw) {
+  for (int i = threadIdx.x; i < kParams; i += blockDim.x) sw[i] = p[i];
+}
+
+// h1 = ReLU(enc W1 + b1), z2 = h1 W2 + b2.
+__device__ __forceinline__ void hidden(const float *sw, const float enc[kIn], float h1[kH], float z2[kH]) {
+#pragma unroll
+  for (int j = 0; j < kH; ++j) h1[j] = sw[kB1 + j];
+#pragma unroll
+  for (int k = 0; k < kIn; ++k) {
+    const float e = enc[k];
+#pragma unroll
+    for (int j = 0; j < kH; j += 4) {
+      const float4 w = *reinterpret_cast<const float4 *>(sw + kW1 + k * kH + j);
+      h1[j] = fmaf(e, w.x, h1[j]);
+      h1[j + 1] = fmaf(e, w.y, h1[j + 1]);
+      h1[j + 2] = fmaf(e, w.z, h1[j + 2]);
+      h1[j + 3] = fmaf(e, w.w, h1[j + 3]);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < kH; ++j) h1[j] = fmaxf(h1[j], 0.0f);
+#pragma unroll
+  for (int j = 0; j < kH; ++j) z2[j] = sw[kB2 + j];
+#pragma unroll 4
+  for (int k = 0; k < kH; ++k) {
+    const float h = h1[k];
+#pragma unroll
+    for (int j = 0; j < kH; j += 4) {
+      const float4 w = *reinterpret_cast<const float4 *>(sw + kW2 + k * kH + j);
+      z2[j] = fmaf(h, w.x, z2[j]);
+      z2[j + 1] = fmaf(h, w.y, z2[j + 1]);
+      z2[j + 2] = fmaf(h, w.z, z2[j + 2]);
+      z2[j + 3] = fmaf(h, w.w, z2[j + 3]);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    prop_fwd_kernel(const float *__restrict__ params, const float *__restrict__ xyz, long long n,
+                    float *__restrict__ sigma) {
+  __shared__ __align__(16) float sw[kParams + 3];
+  load_params(params, sw);
+  __syncthreads();
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    float x[3] = {xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]};
+    float enc[kIn], h1[kH], z2[kH];
+    encode6(x, enc);
+    hidden(sw, enc, h1, z2);
+    float z3 = sw[kB3];
+#pragma unroll
+    for (int j = 0; j < kH; ++j) z3 = fmaf(fmaxf(z2[j], 0.0f), sw[kW3 + j], z3);
+    sigma[i] = softplus(z3);
+  }
+}
+
+constexpr size_t kBwdSmem =
+    (size_t)(2 * (kParams + 3) + kThreads * kEncLd + 4 * kThreads * kRowLd + kThreads) * sizeof(float);
+
+// grads += d/dparams sum_i dsigma_i * sigma_i.
+__global__ void __launch_bounds__(kThreads)
+    prop_bwd_kernel(const float *__restrict__ params, const float *__restrict__ xyz, const float *__restrict__ dsig,
+                    long long n, float *__restrict__ grads) {
+  extern __shared__ __align__(16) float sm[];
+  float *sw = sm;
+  float *sacc = sw + kParams + 3;  // this CTA's gradient, one slice per thread
+  float *sENC = sacc + kParams + 3;
+  float *sH1 = sENC + kThreads * kEncLd;
+  float *sH2 = sH1 + kThreads * kRowLd;
+  float *sDZ2 = sH2 + kThreads * kRowLd;
+  float *sDZ1 = sDZ2 + kThreads * kRowLd;
+  float *sDZ3 = sDZ1 + kThreads * kRowLd;
+  const int tid = threadIdx.x, j = tid & 63, half = tid >> 6;
+  load_params(params, sw);
+  for (int q = tid; q < kParams; q += kThreads) sacc[q] = 0.0f;
+  __syncthreads();
+  const long long ntiles = (n + kThreads - 1) / kThreads;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long i = tile * kThreads + tid;
+    const bool valid = i < n;
+    float x[3] = {0.f, 0.f, 0.f};
+    if (valid) {
+      x[0] = xyz[3 * i];
+      x[1] = xyz[3 * i + 1];
+      x[2] = xyz[3 * i + 2];
+    }
+    float enc[kIn], h1[kH], z2[kH];
+    encode6(x, enc);
+    hidden(sw, enc, h1, z2);
+#pragma unroll
+    for (int k = 0; k < kIn; ++k) sENC[tid * kEncLd + k] = enc[k];
+#pragma unroll
+    for (int k = 0; k < kH; ++k) sH1[tid * kRowLd + k] = h1[k];
+    float z3 = sw[kB3];
+#pragma unroll
+    for (int q = 0; q < kH; ++q) z3 = fmaf(fmaxf(z2[q], 0.0f), sw[kW3 + q], z3);
+    const float dz3 = valid ? dsig[i] / (1.0f + expf(-z3)) : 0.0f;  // softplus' = sigmoid
+    sDZ3[tid] = dz3;
+#pragma unroll
+    for (int q = 0; q < kH; ++q) {
+      sH2[tid * kRowLd + q] = fmaxf(z2[q], 0.0f);
+      z2[q] = z2[q] > 0.0f ? sw[kW3 + q] * dz3 : 0.0f;  // z2 now holds dz2
+      sDZ2[tid * kRowLd + q] = z2[q];
+    }
+    // dz1 = (W2 dz2) * [h1 > 0]
+#pragma unroll 4
+    for (int k = 0; k < kH; ++k) {
+      float acc = 0.0f;
+#pragma unroll
+      for (int q = 0; q < kH; q += 4) {
+        const float4 w = *reinterpret_cast<const float4 *>(sw + kW2 + k * kH + q);
+        acc = fmaf(w.x, z2[q], acc);
+        acc = fmaf(w.y, z2[q + 1], acc);
+        acc = fmaf(w.z, z2[q + 2], acc);
+        acc = fmaf(w.w, z2[q + 3], acc);
+      }
+      sDZ1[tid * kRowLd + k] = sH1[tid * kRowLd + k] > 0.0f ? acc : 0.0f;
+    }
+    __syncthreads();
+    // Reduce this tile into the thread's slice: column j, rows of its half.
+    float aW2[32], aW1[20], aB1 = 0.f, aB2 = 0.f, aW3 = 0.f, aB3 = 0.f;
+#pragma unroll
+    for (int q = 0; q < 32; ++q) aW2[q] = 0.f;
+#pragma unroll
+    for (int q = 0; q < 20; ++q) aW1[q] = 0.f;
+    for (int t = 0; t < kThreads; ++t) {
+      const float d2 = sDZ2[t * kRowLd + j], d1 = sDZ1[t * kRowLd + j];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) aW2[q] = fmaf(sH1[t * kRowLd + half * 32 + q], d2, aW2[q]);
+#pragma unroll
+      for (int q = 0; q < 20; ++q)
+        if (half * 20 + q < kIn) aW1[q] = fmaf(sENC[t * kEncLd + half * 20 + q], d1, aW1[q]);
+      if (half == 0) {
+        aB1 += d1;
+        aB2 += d2;
+        aW3 = fmaf(sH2[t * kRowLd + j], sDZ3[t], aW3);
+        if (j == 0) aB3 += sDZ3[t];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 32; ++q) sacc[kW2 + (half * 32 + q) * kH + j] += aW2[q];
+#pragma unroll
+    for (int q = 0; q < 20; ++q)
+      if (half * 20 + q < kIn) sacc[kW1 + (half * 20 + q) * kH + j] += aW1[q];
+    if (half == 0) {
+      sacc[kB1 + j] += aB1;
+      sacc[kB2 + j] += aB2;
+      sacc[kW3 + j] += aW3;
+      if (j == 0) sacc[kB3] += aB3;
+    }
+    __syncthreads();
+  }
+  for (int q = tid; q < kParams; q += kThreads) atomicAdd(grads + q, sacc[q]);
+}
+
+static int grid_for(long long n, int per_cta_items) {
+  long long g = (n + per_cta_items - 1) / per_cta_items;
+  int sms = num_sms();
+  long long cap = (long long)(sms > 0 ? sms : 148) * 8;
+  return (int)(g < cap ? (g > 0 ? g : 1) : cap);
+}
+
+}  // namespace prop
+
+int launch_proposal_forward(const float *params, const float *xyz, long long n, float *sigma, cudaStream_t stream) {
+  prop::prop_fwd_kernel<<<prop::grid_for(n, prop::kThreads), prop::kThreads, 0, stream>>>(params, xyz, n, sigma);
+  return launch_status();
+}
+
+}  // namespace nerfgb
+
+using namespace nerfgb;
+
+extern "C" long long nerfgb_proposal_param_count(void) { return prop::kParams; }
+
+extern "C" int nerfgb_proposal_forward(const float *params, const float *xyz, long long n, float *sigma,
+                                       void *stream) {
+  if (n < 0) return NERFGB_E_INVALID_ARG;
+  if (n == 0) return NERFGB_OK;
+  if (!params || !xyz || !sigma) return NERFGB_E_INVALID_ARG;
+  return launch_proposal_forward(params, xyz, n, sigma, as_stream(stream));
+}
+
+extern "C" int nerfgb_proposal_backward(const float *params, const float *xyz, const float *grad_sigma, long long n,
+                                        float *grad_params, void *stream) {
+  if (n < 0) return NERFGB_E_INVALID_ARG;
+  if (n == 0) return NERFGB_OK;
+  if (!params || !xyz || !grad_sigma || !grad_params) return NERFGB_E_INVALID_ARG;
+  if (cudaFuncSetAttribute(prop::prop_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)prop::kBwdSmem) != cudaSuccess)
+    return NERFGB_E_CUDA;
+  const long long ntiles = (n + prop::kThreads - 1) / prop::kThreads;
+  int sms = num_sms();
+  int grid = (int)(ntiles < sms ? ntiles : sms);
+  prop::prop_bwd_kernel<<<grid, prop::kThreads, prop::kBwdSmem, as_stream(stream)>>>(params, xyz, grad_sigma, n,
+                                                                                      grad_params);
+  return launch_status();
+}

@@ -98,3 +98,51 @@ extern "C" int nerfgb_render_rays(const void *packed_coarse, const void *packed_
   return nerfgb_composite(w.rgb_f, w.sig_f, w.t_f, R, S, white_bg, trans_mode, nullptr, rgb_fine, depth_fine,
                           acc_fine, stream);
 }
+
+extern "C" int nerfgb_render_rays_proposal(const float *proposal_params, const void *packed_fine, int precision,
+                                           const float *rays_o, const float *rays_d, const float *near,
+                                           const float *far, const float *u_coarse, const float *u_fine,
+                                           unsigned long long seed, int n_rays, int n_coarse, int n_fine,
+                                           int perturb, int lin_inv_depth, int white_bg, int trans_mode,
+                                           float *rgb_fine, float *depth_fine, float *acc_fine, void *workspace,
+                                           int *err_word, void *stream) {
+  if (n_rays < 0 || n_coarse < 2 || n_fine < 1) return NERFGB_E_INVALID_ARG;
+  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16) return NERFGB_E_UNSUPPORTED;
+  if (n_rays == 0) return NERFGB_OK;
+  if (!proposal_params || !packed_fine || !rays_o || !rays_d || !near || !far || !rgb_fine || !depth_fine ||
+      !acc_fine || !workspace || !aligned(workspace, 256))
+    return NERFGB_E_INVALID_ARG;
+  if (precision == NERFGB_PREC_BF16 && !err_word) return NERFGB_E_INVALID_ARG;
+  cudaStream_t st = as_stream(stream);
+  const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
+  RenderWs w = carve(workspace, R, Sc, Sf);
+  int rc;
+  const float *uc = u_coarse, *uf = u_fine;
+  if (perturb && !uc) {
+    if ((rc = nerfgb_uniform(seed, 0, (long long)R * Sc, w.u_c, stream)) != NERFGB_OK) return rc;
+    uc = w.u_c;
+  }
+  if (!uf) {
+    if ((rc = nerfgb_uniform(seed, (unsigned long long)R * Sc, (long long)R * Sf, w.u_f, stream)) != NERFGB_OK)
+      return rc;
+    uf = w.u_f;
+  }
+  if ((rc = nerfgb_coarse_sample(rays_o, rays_d, near, far, uc, R, Sc, perturb, lin_inv_depth, w.xyz_c, nullptr,
+                                 w.t_c, w.edges, w.widths, stream)) != NERFGB_OK)
+    return rc;
+  // The proposal density at the stratified samples replaces the coarse MLP.
+  if ((rc = launch_proposal_forward(proposal_params, w.xyz_c, (long long)R * Sc, w.sig_c, st)) != NERFGB_OK)
+    return rc;
+  if (cudaMemsetAsync(w.rgb_c, 0, sizeof(float) * 3 * (size_t)R * Sc, st) != cudaSuccess) return NERFGB_E_CUDA;
+  if ((rc = nerfgb_composite(w.rgb_c, w.sig_c, w.t_c, R, Sc, 0, trans_mode, w.w_c, w.map_rgb_c, w.map_depth_c,
+                             w.map_acc_c, stream)) != NERFGB_OK)
+    return rc;
+  if ((rc = nerfgb_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, uf, R, Sc, Sf, w.xyz_f,
+                               nullptr, w.t_f, nullptr, nullptr, stream)) != NERFGB_OK)
+    return rc;
+  if ((rc = launch_mlp(packed_fine, precision, w.xyz_f, rays_d, (long long)R * S, S, w.rgb_f, w.sig_f, err_word,
+                       st)) != NERFGB_OK)
+    return rc;
+  return nerfgb_composite(w.rgb_f, w.sig_f, w.t_f, R, S, white_bg, trans_mode, nullptr, rgb_fine, depth_fine,
+                          acc_fine, stream);
+}

@@ -13,7 +13,6 @@ plain path) or BF16 tcgen05 GEMMs with FP32 accumulation
 """
 import ctypes
 
-import numpy as np
 import torch
 
 from . import _lib, ray_utils
@@ -158,11 +157,13 @@ class NeRF:
 
     # -- fused inference ----------------------------------------------------
     def render(self, rays_o, rays_d, near, far, *, chunk=4096, u_coarse=None, u_fine=None, seed=0,
-               precision=None, return_coarse=False):
+               precision=None, return_coarse=False, proposal=None):
         """Fine (and optionally coarse) rgb/depth/acc maps for every ray, in
         chunks of `chunk` rays (the reference renders 4096-ray batches,
         base_dataset.py:853-857). Uniforms come from Philox keyed by `seed`
-        when not supplied."""
+        when not supplied. With `proposal` (a ProposalNetwork) the proposal's
+        weights replace the coarse MLP's as the fine sampler's PDF and no
+        coarse maps are produced."""
         prec = PRECISIONS[precision or self.precision]
         rays_o = as_cuda(rays_o, name="rays_o")
         R = rays_o.shape[0]
@@ -184,6 +185,19 @@ class NeRF:
         for s in range(0, R, chunk):
             e = min(R, s + chunk)
             sl = slice(s, e)
+            if proposal is not None:
+                if return_coarse:
+                    raise ValueError("the proposal path has no coarse maps")
+                _lib.call("nerfgb_render_rays_proposal", ptr(proposal.params), ptr(pf), prec,
+                          ptr(rays_o[sl]), ptr(rays_d[sl]), ptr(near[sl]), ptr(far[sl]),
+                          ptr(u_coarse[sl]) if u_coarse is not None else None,
+                          ptr(u_fine[sl]) if u_fine is not None else None,
+                          ctypes.c_ulonglong(int(seed) + s), e - s, Sc, Sf,
+                          int(bool(self.params.sampling.perturb)),
+                          int(bool(self.params.sampling.lin_inv_depth)), int(self.white_bg),
+                          int(self.trans_mode), ptr(out["rgb"][sl]), ptr(out["depth"][sl]),
+                          ptr(out["acc"][sl]), ptr(ws), ptr(self.fine_model.err_word), stream())
+                continue
             _lib.call("nerfgb_render_rays", ptr(pc), ptr(pf), prec, ptr(rays_o[sl]), ptr(rays_d[sl]),
                       ptr(near[sl]), ptr(far[sl]),
                       ptr(u_coarse[sl]) if u_coarse is not None else None,

@@ -374,3 +374,159 @@ def philox_uniform(seed, offset, n):
     words = np.stack(philox4x32_10(lo, hi, z, z, seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF), axis=1)
     w = words[np.arange(n), (e & np.uint64(3)).astype(np.int64)]
     return (w >> np.uint32(8)).astype(np.float32) * np.float32(1.0 / 16777216.0)
+
+
+# ---------------------------------------------------------------------------
+# Gradients (the reference takes them with tf.GradientTape, model.py:148-171)
+# ---------------------------------------------------------------------------
+def composite_backward(sigma, t_vals, sample_rgb, grad_rgb_map=None, grad_weights=None,
+                       white_bg=False):
+    """Analytic gradient of compute_weights/post_process_model_output
+    (ray_utils.py:426-551) w.r.t. sigma [R*S] and sample_rgb [R*S,3], given
+    dL/dpred_rgb [R,3] and/or dL/dweights [R,S]."""
+    t = np.asarray(t_vals)
+    dtype = t.dtype.type
+    R, S = t.shape
+    sig = np.asarray(sigma, dtype).reshape(R, S)
+    rgb = np.asarray(sample_rgb, dtype).reshape(R, S, 3)
+    delta = np.concatenate([t[:, 1:] - t[:, :-1], np.full((R, 1), dtype(1e10), dtype)], 1)
+    e = np.exp(-sig * delta)
+    alpha = 1 - e
+    fac = dtype(1) - alpha + dtype(1e-10)
+    T = np.concatenate([np.ones((R, 1), dtype), np.cumprod(fac, axis=1)[:, :-1]], 1)
+    w = alpha * T
+    g = np.zeros((R, S), dtype) if grad_weights is None else np.asarray(grad_weights, dtype).copy()
+    d_rgb = np.zeros_like(rgb)
+    if grad_rgb_map is not None:
+        G = np.asarray(grad_rgb_map, dtype)
+        g = g + np.einsum("rsc,rc->rs", rgb, G)
+        if white_bg:
+            g = g - G.sum(1, keepdims=True)
+        d_rgb = w[..., None] * G[:, None, :]
+    gw = g * w
+    suffix = np.concatenate([np.cumsum(gw[:, ::-1], axis=1)[:, ::-1][:, 1:], np.zeros((R, 1), dtype)], 1)
+    d_alpha = g * T - suffix / fac
+    d_sigma = d_alpha * delta * e
+    return d_sigma.reshape(-1), d_rgb.reshape(-1, 3)
+
+
+def apply_adam(var, m, v, grad, step, lr, beta1=0.9, beta2=0.999, eps=1e-7):
+    """TensorFlow's ApplyAdam as Keras' Adam calls it (model.py:418 uses
+    Keras defaults): lr_t = lr sqrt(1-b2^t)/(1-b1^t); m += (g-m)(1-b1);
+    v += (g^2-v)(1-b2); var -= lr_t m/(sqrt(v)+eps). Returns new (var, m, v)."""
+    b1p, b2p = beta1 ** step, beta2 ** step
+    lr_t = lr * np.sqrt(1 - b2p) / (1 - b1p)
+    m = m + (grad - m) * (1 - beta1)
+    v = v + (grad * grad - v) * (1 - beta2)
+    var = var - lr_t * m / (np.sqrt(v) + eps)
+    return var, m, v
+
+
+def lr_schedule(step):
+    """ExponentialDecay(5e-4, 500000, 0.1), not staircase (model.py:413-417)."""
+    return 5e-4 * 0.1 ** (step / 500000.0)
+
+
+# ---------------------------------------------------------------------------
+# Proposal network (not in the reference): 2x64 ReLU MLP on the L=6 encoding
+# of xyz (39 inputs, model.py:330 concatenation convention), softplus density.
+# Flat blob: W1 [39,64], b1 [64], W2 [64,64], b2 [64], W3 [64], b3 [1].
+# ---------------------------------------------------------------------------
+PROP_SHAPES = (("W1", (39, 64)), ("b1", (64,)), ("W2", (64, 64)), ("b2", (64,)),
+               ("W3", (64,)), ("b3", (1,)))
+
+
+def prop_unpack(blob, dtype=F32):
+    out, off = {}, 0
+    for name, shp in PROP_SHAPES:
+        n = int(np.prod(shp))
+        out[name] = np.asarray(blob[off:off + n], dtype).reshape(shp)
+        off += n
+    return out
+
+
+def prop_pack(p):
+    return np.concatenate([np.asarray(p[name]).reshape(-1) for name, _ in PROP_SHAPES])
+
+
+def softplus(x):
+    return np.maximum(x, 0) + np.log1p(np.exp(-np.abs(x)))
+
+
+def prop_forward(blob, xyz, dtype=F32, cache=False):
+    p = prop_unpack(blob, dtype)
+    enc = positional_encoding(xyz, 6, dtype)
+    z1 = enc @ p["W1"] + p["b1"]
+    h1 = relu(z1)
+    z2 = h1 @ p["W2"] + p["b2"]
+    h2 = relu(z2)
+    z3 = h2 @ p["W3"] + p["b3"][0]
+    sigma = softplus(z3)
+    if cache:
+        return sigma, dict(enc=enc, z1=z1, h1=h1, z2=z2, h2=h2, z3=z3)
+    return sigma
+
+
+def prop_backward(blob, xyz, d_sigma, dtype=F64):
+    """Gradient of sum(d_sigma * prop_forward(xyz)) w.r.t. the flat blob."""
+    p = prop_unpack(blob, dtype)
+    _, c = prop_forward(blob, xyz, dtype, cache=True)
+    dz3 = np.asarray(d_sigma, dtype) / (1 + np.exp(-c["z3"]))
+    g = {"W3": c["h2"].T @ dz3, "b3": np.array([dz3.sum()])}
+    dz2 = np.outer(dz3, p["W3"]) * (c["z2"] > 0)
+    g["W2"] = c["h1"].T @ dz2
+    g["b2"] = dz2.sum(0)
+    dz1 = (dz2 @ p["W2"].T) * (c["z1"] > 0)
+    g["W1"] = c["enc"].T @ dz1
+    g["b1"] = dz1.sum(0)
+    return prop_pack(g)
+
+
+def prop_loss(w_prop, w_target, lam=3.0):
+    """Envelope loss on the 64-bin weight histograms: squared error, with
+    under-estimates of the target weighted (1 + lam). Mean over rays.
+    Returns (loss, dL/dw_prop)."""
+    diff = np.asarray(w_prop) - np.asarray(w_target)
+    rho = 1 + lam * (diff < 0)
+    R = diff.shape[0]
+    return float(np.sum(rho * diff * diff) / R), 2 * rho * diff / R
+
+
+def mlp_backward(p, xyz, dirs, d_rgb, d_sigma, dtype=F64):
+    """Gradient of sum(d_rgb * rgb + d_sigma * sigma) of mlp_forward
+    (model.py:334-394) w.r.t. every layer: {name: (dW, db)}."""
+    p = {k: (np.asarray(W, dtype), np.asarray(b, dtype)) for k, (W, b) in p.items()}
+    rgb, sigma, a = mlp_forward(p, xyz, dirs, dtype, cache=True)
+    d_sigma = np.asarray(d_sigma, dtype).reshape(-1, 1)
+    g = {}
+    dz = np.asarray(d_rgb, dtype) * rgb * (1 - rgb)                      # sigmoid
+    g["rgb"] = (a["h9"].T @ dz, dz.sum(0))
+    dh9 = dz @ p["rgb"][0].T
+    dz9 = dh9 * (a["h9"] > 0)
+    h9in = np.concatenate([a["bott"], a["enc_dir"]], -1)
+    g["dense_9"] = (h9in.T @ dz9, dz9.sum(0))
+    dbott = (dz9 @ p["dense_9"][0].T)[:, :256]
+    g["dense_8"] = (a["h7"].T @ dbott, dbott.sum(0))
+    dh7 = dbott @ p["dense_8"][0].T
+    dzs = d_sigma * (sigma > 0)                                          # sigma ReLU
+    g["sigma"] = (a["h7"].T @ dzs, dzs.sum(0))
+    dh7 = dh7 + dzs @ p["sigma"][0].T
+    dh = dh7
+    for i in range(7, -1, -1):
+        dz_i = dh * (a[f"h{i}"] > 0)
+        if i == 0:
+            inp = a["enc_xyz"]
+        elif i == 5:
+            inp = np.concatenate([a["h4"], a["enc_xyz"]], -1)
+        else:
+            inp = a[f"h{i - 1}"]
+        g[f"dense_{i}"] = (inp.T @ dz_i, dz_i.sum(0))
+        dinp = dz_i @ p[f"dense_{i}"][0].T
+        dh = dinp[:, :256] if i == 5 else dinp
+    return g
+
+
+def mse(y_true, y_pred):
+    """keras.losses.MeanSquaredError: mean over every element (model.py:32)."""
+    d = np.asarray(y_pred) - np.asarray(y_true)
+    return float(np.mean(d * d)), 2 * d / d.size

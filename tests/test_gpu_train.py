@@ -1,0 +1,126 @@
+"""Training-side kernels against the oracle: compositing backward, losses,
+Adam, and the proposal network (forward, backward, training)."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+F32, F64 = np.float32, np.float64
+
+
+def dev(x):
+    return torch.from_numpy(np.ascontiguousarray(x)).cuda()
+
+
+def host(x):
+    return x.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("S,white_bg", [(64, False), (192, True), (7, False)])
+def test_composite_backward_vs_oracle(ng, oracle, cuda, S, white_bg):
+    rng = np.random.default_rng(S)
+    R = 123
+    t = np.sort(rng.uniform(2, 6, (R, S)), 1).astype(F32)
+    sig = (rng.exponential(1.5, R * S) * (rng.random(R * S) < 0.8)).astype(F32)
+    rgb = rng.random((R * S, 3), dtype=F32)
+    G = rng.normal(size=(R, 3)).astype(F32)
+    gw = rng.normal(size=(R, S)).astype(F32)
+    want_s, want_c = oracle.composite_backward(sig.astype(F64), t.astype(F64), rgb.astype(F64),
+                                               G.astype(F64), gw.astype(F64), white_bg)
+    gs = torch.empty(R * S, device="cuda")
+    gc = torch.empty(R * S, 3, device="cuda")
+    d_sig, d_t, d_rgb, d_G, d_gw = dev(sig), dev(t), dev(rgb), dev(G), dev(gw)  # keep alive
+    ng._lib.call("nerfgb_composite_backward", d_sig.data_ptr(), d_t.data_ptr(), d_rgb.data_ptr(),
+                 d_G.data_ptr(), d_gw.data_ptr(), R, S, int(white_bg), gs.data_ptr(), gc.data_ptr(), None)
+    scale = np.abs(want_s).max()
+    # fp32 products/exp vs fp64: relative to the gradient's scale
+    np.testing.assert_allclose(host(gs), want_s, atol=2e-5 * scale, rtol=1e-3)
+    np.testing.assert_allclose(host(gc), want_c, atol=1e-6, rtol=1e-4)
+
+
+def test_losses_vs_oracle(ng, oracle, cuda):
+    rng = np.random.default_rng(0)
+    p, y = rng.random((500, 3), dtype=F32), rng.random((500, 3), dtype=F32)
+    loss = torch.zeros(1, device="cuda")
+    grad = torch.empty(500, 3, device="cuda")
+    d_p, d_y = dev(p), dev(y)
+    ng._lib.call("nerfgb_mse_loss", d_p.data_ptr(), d_y.data_ptr(), 1500, ng._lib.F(1.0),
+                 loss.data_ptr(), grad.data_ptr(), None)
+    wl, wg = oracle.mse(y, p)
+    assert abs(float(loss.item()) - wl) < 1e-6
+    np.testing.assert_allclose(host(grad), wg, rtol=1e-5, atol=1e-9)
+    wp, wt = rng.random((64, 64), dtype=F32), rng.random((64, 64), dtype=F32)
+    loss.zero_()
+    g2 = torch.empty(64, 64, device="cuda")
+    d_wp, d_wt = dev(wp), dev(wt)
+    ng._lib.call("nerfgb_envelope_loss", d_wp.data_ptr(), d_wt.data_ptr(), 64, 64, ng._lib.F(3.0),
+                 loss.data_ptr(), g2.data_ptr(), None)
+    wl, wg = oracle.prop_loss(wp, wt, 3.0)
+    assert abs(float(loss.item()) - wl) < 1e-4 * wl
+    np.testing.assert_allclose(host(g2), wg, rtol=1e-5, atol=1e-9)
+
+
+def test_adam_vs_oracle(ng, oracle, cuda):
+    rng = np.random.default_rng(1)
+    n = 1000
+    var = rng.normal(size=n).astype(F32)
+    m, v = np.zeros(n, F32), np.zeros(n, F32)
+    tv, tm, tvv = dev(var), dev(m), dev(v)
+    for step in range(1, 6):
+        g = rng.normal(size=n).astype(F32)
+        ng.proposal.adam_step(tv, tm, tvv, dev(g), step, 5e-4)
+        var, m, v = oracle.apply_adam(var.astype(F64), m.astype(F64), v.astype(F64), g.astype(F64), step, 5e-4)
+    np.testing.assert_allclose(host(tv), var, atol=1e-6)
+    np.testing.assert_allclose(host(tm), m, atol=1e-6)
+
+
+def test_proposal_forward_backward_vs_oracle(ng, oracle, cuda):
+    rng = np.random.default_rng(3)
+    blob = ng.proposal.glorot_blob(4)
+    blob[2496:2560] = rng.uniform(-0.1, 0.1, 64)
+    n = 1000
+    x = rng.uniform(-4, 4, (n, 3)).astype(F32)
+    prop = ng.ProposalNetwork(blob)
+    sig = host(prop(dev(x)))[:, 0]
+    want = oracle.prop_forward(blob, x, F64)
+    np.testing.assert_allclose(sig, want, rtol=1e-4, atol=1e-5)
+    ds = rng.normal(size=n).astype(F32)
+    g = host(prop.backward(dev(x), dev(ds)))
+    wg = oracle.prop_backward(blob.astype(F64), x.astype(F64), ds.astype(F64))
+    np.testing.assert_allclose(g, wg, atol=1e-3 * np.abs(wg).max(), rtol=1e-3)
+
+
+@pytest.fixture(scope="module")
+def proposal_case(ng):
+    """A random-init NeRF, 32k training rays from 8 random frames and the
+    coarse-pass weight histograms of the plain path as targets."""
+    p = ng.make_params()
+    nerf = ng.NeRF(p, precision="bf16", seed=21)
+    frames = [ng.synthetic.frame_rays(100 + i, H=200, W=200, focal=277.78) for i in range(8)]
+    rays = [torch.from_numpy(np.concatenate([f[k] for f in frames])).cuda() for k in range(4)]
+    R = rays[0].shape[0]
+    g = torch.Generator(device="cuda")
+    g.manual_seed(0)
+    uc = torch.rand(R, 64, device="cuda", generator=g)
+    w_t = ng.proposal.coarse_histograms(nerf, *rays, uc)
+    return nerf, rays, uc, w_t
+
+
+def test_proposal_training_reduces_loss_and_gains(ng, cuda, proposal_case):
+    """Trained by the library's own kernels, the proposal's fine samples land
+    where the coarse pass puts them: its render is far closer to the plain
+    hierarchical render than an untrained proposal's."""
+    nerf, rays, uc, w_t = proposal_case
+    prop = ng.ProposalNetwork(seed=7)
+    untrained = ng.ProposalNetwork(prop.params.clone())
+    trainer = ng.ProposalTrainer(prop, nerf.params, lr=3e-3)
+    losses = trainer.fit(*rays, uc, w_t, steps=600, batch=4096)
+    assert losses[-1] < 0.35 * losses[0], losses
+    # held-out frame, same uniforms for every path
+    o, d, n, f = [torch.from_numpy(x).cuda() for x in ng.synthetic.frame_rays(999, H=200, W=200, focal=277.78)]
+    plain = nerf.render(o, d, n, f, seed=5)["rgb"]
+    fast = nerf.render(o, d, n, f, seed=5, proposal=prop)["rgb"]
+    base = nerf.render(o, d, n, f, seed=5, proposal=untrained)["rgb"]
+    nerf.fine_model.check_device_errors()
+    p_trained, p_untrained = ng.psnr(plain, fast), ng.psnr(plain, base)
+    assert p_trained > p_untrained + 0.5, (p_trained, p_untrained)
