@@ -229,6 +229,30 @@ int nerfgb_adam_step(float *params, float *m, float *v, const float *grads,
                      long long n, float lr, float beta1, float beta2,
                      float eps, long long step, void *stream);
 
+/* Floats of stored activations per MLP row (enc_xyz, h0..h7, bottleneck,
+ * enc_dir, h9) written by nerfgb_mlp_forward_train. */
+long long nerfgb_mlp_acts_floats_per_row(void);
+
+/* The FP32 MLP forward of nerfgb_mlp_forward that also stores every layer's
+ * activations in acts [n_rows, nerfgb_mlp_acts_floats_per_row()] for the
+ * backward (the tape that tf.GradientTape keeps, nerf/core/model.py:148).
+ * `packed` is an FP32 pack. */
+int nerfgb_mlp_forward_train(const void *packed, const float *xyz,
+                             const float *dirs, long long n_rows,
+                             int rows_per_dir, float *rgb, float *sigma,
+                             float *acts, void *stream);
+
+/* Workspace bytes of nerfgb_mlp_backward for n_rows rows. */
+long long nerfgb_mlp_backward_workspace_bytes(long long n_rows);
+
+/* Gradient of sum(d_rgb * rgb + d_sigma * sigma) of the MLP w.r.t. its flat
+ * parameter blob (Keras layout, nerfgb_mlp_param_count floats), ACCUMULATED
+ * into grad_params. acts from nerfgb_mlp_forward_train on the same rows with
+ * the same FP32 pack. d_sigma may be NULL. FP32 throughout. */
+int nerfgb_mlp_backward(const void *packed, const float *acts, long long n_rows,
+                        const float *d_rgb, const float *d_sigma,
+                        float *grad_params, void *workspace, void *stream);
+
 /* ---- fused render without allocation --------------------------------- */
 
 /* Size of the built-in scratch array of nerfgb_render_rays_noalloc: 16 MiB,

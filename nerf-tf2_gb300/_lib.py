@@ -54,6 +54,10 @@ SIGNATURES = {
     "nerfgb_mse_loss": (I, [P, P, LL, F, P, P, P]),
     "nerfgb_envelope_loss": (I, [P, P, I, I, F, P, P, P]),
     "nerfgb_adam_step": (I, [P, P, P, P, LL, F, F, F, F, LL, P]),
+    "nerfgb_mlp_acts_floats_per_row": (LL, []),
+    "nerfgb_mlp_forward_train": (I, [P, P, P, LL, I, P, P, P, P]),
+    "nerfgb_mlp_backward_workspace_bytes": (LL, [LL]),
+    "nerfgb_mlp_backward": (I, [P, P, LL, P, P, P, P, P]),
     "nerfgb_render_rays_noalloc": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
                                        P, P, P, P, P, P, P, P]),
 }

@@ -70,6 +70,13 @@ constexpr long long kBf16WBytes = kGemmWElems * 2;
 constexpr long long kBf16TableOff = (kBf16WBytes + 1023) / 1024 * 1024;  // bytes
 constexpr long long kBf16PackBytes = kBf16TableOff + (long long)kTableElems * 4;
 
+// Stored activations of one row for training (floats): enc_xyz [64] | h0..h7
+// [8 x 256] | bottleneck [256] | enc_dir [32] | h9 [128].
+constexpr int kActsEncXyz = 0;
+constexpr int kActsEncDir = 64 + 9 * 256;     // 2368
+constexpr int kActsLd = kActsEncDir + 32 + 128;  // 2528
+NG_HD int acts_offset(int g) { return g < 9 ? 64 + 256 * g : kActsEncDir + 32; }
+
 // ---------------------------------------------------------------------------
 // Correctly rounded fp32 arithmetic, never fused into FMA. The reference's
 // TensorFlow ops are separate elementwise kernels, so each step rounds.

@@ -134,10 +134,24 @@ __device__ __forceinline__ void fp32_chunk(const float *__restrict__ Xr, const f
   }
 }
 
+// Copies columns [c0, c0 + nc) of the tile's X rows to acts[row][off ..].
+__device__ __forceinline__ void store_cols(float *__restrict__ acts, long long row0, long long n, const float *X,
+                                           int c0, int nc, int off, int tid) {
+  const int per_row = nc / 4;
+  for (int e = tid; e < kTM * per_row; e += 256) {
+    const int r = e / per_row, q = e - r * per_row;
+    if (row0 + r < n)
+      *reinterpret_cast<float4 *>(acts + (row0 + r) * kActsLd + off + 4 * q) =
+          *reinterpret_cast<const float4 *>(X + r * kXLD + c0 + 4 * q);
+  }
+}
+
+// STORE: also write every layer's post-activation rows to `acts` (training).
+template <bool STORE>
 __global__ void __launch_bounds__(256, 1)
     mlp_fp32_kernel(const float *__restrict__ pk, const float *__restrict__ xyz,
                     const float *__restrict__ dirs, long long n, int rpd, float *__restrict__ rgb,
-                    float *__restrict__ sigma) {
+                    float *__restrict__ sigma, float *__restrict__ acts) {
   extern __shared__ __align__(16) float sm[];
   float *X = sm;
   float *Wb = sm + kTM * kXLD;
@@ -233,6 +247,11 @@ __global__ void __launch_bounds__(256, 1)
         for (int e = tid; e < kTM * 5; e += 256) X[(e / 5) * kXLD + 283 + e % 5] = 0.0f;
       }
       __syncthreads();
+      if (STORE) {
+        store_cols(acts, row0, n, X, 0, N, acts_offset(g), tid);
+        if (g == 0) store_cols(acts, row0, n, X, 256, 64, kActsEncXyz, tid);
+        if (g == 8) store_cols(acts, row0, n, X, 256, 32, kActsEncDir, tid);
+      }
       if (g == 7) {
         // sigma = ReLU(h7 . w + b) (model.py:374-375).
         int r = tid >> 2, part = tid & 3;
@@ -282,15 +301,29 @@ extern "C" int nerfgb_mlp_pack(const float *params, int precision, void *packed,
 namespace nerfgb {
 int launch_mlp_fp32(const void *packed, const float *xyz, const float *dirs, long long n, int rpd,
                     float *rgb, float *sigma, cudaStream_t stream) {
-  if (cudaFuncSetAttribute(mlp_fp32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFp32Smem) !=
+  if (cudaFuncSetAttribute(mlp_fp32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFp32Smem) !=
       cudaSuccess)
     return NERFGB_E_CUDA;
   long long ntiles = (n + kTM - 1) / kTM;
   int sms = num_sms();
   if (sms <= 0) return NERFGB_E_DEVICE;
   int grid = (int)(ntiles < sms ? ntiles : sms);
-  mlp_fp32_kernel<<<grid, 256, kFp32Smem, stream>>>(reinterpret_cast<const float *>(packed), xyz, dirs, n,
-                                                     rpd, rgb, sigma);
+  mlp_fp32_kernel<false><<<grid, 256, kFp32Smem, stream>>>(reinterpret_cast<const float *>(packed), xyz, dirs,
+                                                            n, rpd, rgb, sigma, nullptr);
+  return launch_status();
+}
+
+int launch_mlp_fp32_store(const void *packed, const float *xyz, const float *dirs, long long n, int rpd,
+                          float *rgb, float *sigma, float *acts, cudaStream_t stream) {
+  if (cudaFuncSetAttribute(mlp_fp32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFp32Smem) !=
+      cudaSuccess)
+    return NERFGB_E_CUDA;
+  long long ntiles = (n + kTM - 1) / kTM;
+  int sms = num_sms();
+  if (sms <= 0) return NERFGB_E_DEVICE;
+  int grid = (int)(ntiles < sms ? ntiles : sms);
+  mlp_fp32_kernel<true><<<grid, 256, kFp32Smem, stream>>>(reinterpret_cast<const float *>(packed), xyz, dirs, n,
+                                                           rpd, rgb, sigma, acts);
   return launch_status();
 }
 }  // namespace nerfgb

@@ -1,0 +1,365 @@
+// Backward pass of the NeRF MLP (nerf/core/model.py:334-394), the gradient
+// tf.GradientTape takes at model.py:148-170, in FP32 with FP32 master
+// weights.
+//
+// The forward (mlp.cu, STORE variant) writes every layer's post-activation
+// rows to `acts` (kActsLd floats per row). The backward then runs layer by
+// layer from the heads down:
+//   head kernel   rgb = sigmoid(h9 Wr + br), sigma = ReLU(h7 ws + bs):
+//                 dZ9 = (dpre_rgb Wr^T) * [h9 > 0], dpre_sigma, head grads
+//   dW kernel     dW[k][n] += sum_m In[m][k] dZ[m][n]  (split over m, atomics)
+//   dX kernel     dZ_prev[m][k] = (sum_n dZ[m][n] W[k][n] + dpre_sigma[m] ws[k])
+//                                 * [h_prev[m][k] > 0]
+// Gradients land in the flat Keras layout of the parameter blob.
+#include "common.cuh"
+#include "mlp_internal.cuh"
+
+namespace nerfgb {
+namespace train {
+
+constexpr int kTM = 64;
+constexpr int kDzLd = 256;  // row stride of the dZ buffers
+
+// ---------------------------------------------------------------------------
+// Heads
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256)
+    head_bwd_kernel(const float *__restrict__ table, const float *__restrict__ acts, long long n,
+                    const float *__restrict__ d_rgb, const float *__restrict__ d_sigma, float *__restrict__ dz9,
+                    float *__restrict__ dsp_out, float *__restrict__ grads) {
+  extern __shared__ __align__(16) float hsm[];
+  float(*sH9)[128 + 4] = reinterpret_cast<float(*)[128 + 4]>(hsm);
+  float(*sH7)[256 + 4] = reinterpret_cast<float(*)[256 + 4]>(hsm + kTM * (128 + 4));
+  float(*sDRP)[3] = reinterpret_cast<float(*)[3]>(hsm + kTM * (128 + 4) + kTM * (256 + 4));
+  float *sDSP = hsm + kTM * (128 + 4) + kTM * (256 + 4) + kTM * 3;
+  float *sAcc = sDSP + kTM;  // dWr [128][3], dbr [3], dws [256], dbs [1]
+  const int tid = threadIdx.x;
+  for (int e = tid; e < 644; e += 256) sAcc[e] = 0.0f;
+  const float *Wr = table + kRgbWOff, *br = table + kRgbBOff, *ws = table + kSigmaWOff;
+  const long long ntiles = (n + kTM - 1) / kTM;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long row0 = tile * kTM;
+    __syncthreads();
+    for (int e = tid; e < kTM * 32; e += 256) {
+      const int r = e >> 5, q = e & 31;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (row0 + r < n) v = *reinterpret_cast<const float4 *>(acts + (row0 + r) * kActsLd + acts_offset(9) + 4 * q);
+      *reinterpret_cast<float4 *>(&sH9[r][4 * q]) = v;
+    }
+    for (int e = tid; e < kTM * 64; e += 256) {
+      const int r = e >> 6, q = e & 63;
+      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (row0 + r < n) v = *reinterpret_cast<const float4 *>(acts + (row0 + r) * kActsLd + acts_offset(7) + 4 * q);
+      *reinterpret_cast<float4 *>(&sH7[r][4 * q]) = v;
+    }
+    __syncthreads();
+    if (tid < kTM) {
+      const int r = tid;
+      const bool valid = row0 + r < n;
+      float pre[3] = {br[0], br[1], br[2]};
+      for (int j = 0; j < 128; ++j) {
+        const float h = sH9[r][j];
+        pre[0] = fmaf(h, Wr[3 * j], pre[0]);
+        pre[1] = fmaf(h, Wr[3 * j + 1], pre[1]);
+        pre[2] = fmaf(h, Wr[3 * j + 2], pre[2]);
+      }
+      for (int c = 0; c < 3; ++c) {
+        const float y = 1.0f / (1.0f + expf(-pre[c]));
+        sDRP[r][c] = valid ? d_rgb[(row0 + r) * 3 + c] * y * (1.0f - y) : 0.0f;
+      }
+      float sp = table[kSigmaBOff];
+      for (int j = 0; j < 256; ++j) sp = fmaf(sH7[r][j], ws[j], sp);
+      const float dsp = (valid && d_sigma && sp > 0.0f) ? d_sigma[row0 + r] : 0.0f;
+      sDSP[r] = dsp;
+      if (valid) dsp_out[row0 + r] = dsp;
+    }
+    __syncthreads();
+    for (int e = tid; e < kTM * 128; e += 256) {
+      const int r = e >> 7, j = e & 127;
+      if (row0 + r < n) {
+        const float g = sDRP[r][0] * Wr[3 * j] + sDRP[r][1] * Wr[3 * j + 1] + sDRP[r][2] * Wr[3 * j + 2];
+        dz9[(row0 + r) * kDzLd + j] = sH9[r][j] > 0.0f ? g : 0.0f;
+      }
+    }
+    for (int e = tid; e < 644; e += 256) {
+      float a = 0.0f;
+      if (e < 384) {
+        const int j = e / 3, c = e - 3 * j;
+        for (int r = 0; r < kTM; ++r) a = fmaf(sH9[r][j], sDRP[r][c], a);
+      } else if (e < 387) {
+        for (int r = 0; r < kTM; ++r) a += sDRP[r][e - 384];
+      } else if (e < 643) {
+        const int j = e - 387;
+        for (int r = 0; r < kTM; ++r) a = fmaf(sH7[r][j], sDSP[r], a);
+      } else {
+        for (int r = 0; r < kTM; ++r) a += sDSP[r];
+      }
+      sAcc[e] += a;
+    }
+  }
+  __syncthreads();
+  float *gWr = grads + flat_offset(11), *gbr = gWr + 128 * 3;
+  float *gws = grads + flat_offset(8), *gbs = gws + 256;
+  for (int e = tid; e < 644; e += 256) {
+    float *dst = e < 384 ? gWr + e : e < 387 ? gbr + (e - 384) : e < 643 ? gws + (e - 387) : gbs;
+    atomicAdd(dst, sAcc[e]);
+  }
+}
+
+constexpr size_t kHeadSmem = (size_t)(kTM * (128 + 4) + kTM * (256 + 4) + kTM * 3 + kTM + 644) * sizeof(float);
+
+// ---------------------------------------------------------------------------
+// dX: dz_out[m][k] = (sum_n dz_in[m][n] W[k][n] + dsp[m] ws[k]) * mask, k < 256
+// ---------------------------------------------------------------------------
+constexpr int kNC = 32;
+constexpr size_t kDxSmem = (size_t)(kTM * (kNC + 4) + kNC * (256 + 4)) * sizeof(float);
+
+__global__ void __launch_bounds__(256)
+    dx_kernel(const float *__restrict__ W, int N, const float *__restrict__ dz_in, long long n,
+              const float *__restrict__ dsp, const float *__restrict__ ws, const float *__restrict__ acts, int mask_off,
+              float *__restrict__ dz_out) {
+  extern __shared__ __align__(16) float sm[];
+  float *sA = sm;                      // [kTM][kNC + 4]
+  float *sB = sm + kTM * (kNC + 4);    // [kNC][256 + 4]: sB[nn][k] = W[k][n0 + nn]
+  const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  const long long ntiles = (n + kTM - 1) / kTM;
+  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const long long row0 = tile * kTM;
+    float acc[8][8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i)
+#pragma unroll
+      for (int j = 0; j < 8; ++j) acc[i][j] = 0.0f;
+    for (int n0 = 0; n0 < N; n0 += kNC) {
+      __syncthreads();
+      for (int e = tid; e < kTM * (kNC / 4); e += 256) {
+        const int r = e / (kNC / 4), q = e % (kNC / 4);
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (row0 + r < n) v = *reinterpret_cast<const float4 *>(dz_in + (row0 + r) * kDzLd + n0 + 4 * q);
+        *reinterpret_cast<float4 *>(sA + r * (kNC + 4) + 4 * q) = v;
+      }
+      {
+        const int k = tid;  // one W row per thread
+#pragma unroll
+        for (int q = 0; q < kNC / 4; ++q) {
+          const float4 v = *reinterpret_cast<const float4 *>(W + (long long)k * N + n0 + 4 * q);
+          sB[(4 * q) * (256 + 4) + k] = v.x;
+          sB[(4 * q + 1) * (256 + 4) + k] = v.y;
+          sB[(4 * q + 2) * (256 + 4) + k] = v.z;
+          sB[(4 * q + 3) * (256 + 4) + k] = v.w;
+        }
+      }
+      __syncthreads();
+#pragma unroll 4
+      for (int nn = 0; nn < kNC; ++nn) {
+        float a[8];
+#pragma unroll
+        for (int i = 0; i < 8; ++i) a[i] = sA[(ty * 8 + i) * (kNC + 4) + nn];
+        const float4 b0 = *reinterpret_cast<const float4 *>(sB + nn * (256 + 4) + tx * 4);
+        const float4 b1 = *reinterpret_cast<const float4 *>(sB + nn * (256 + 4) + 128 + tx * 4);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          acc[i][0] = fmaf(a[i], b0.x, acc[i][0]);
+          acc[i][1] = fmaf(a[i], b0.y, acc[i][1]);
+          acc[i][2] = fmaf(a[i], b0.z, acc[i][2]);
+          acc[i][3] = fmaf(a[i], b0.w, acc[i][3]);
+          acc[i][4] = fmaf(a[i], b1.x, acc[i][4]);
+          acc[i][5] = fmaf(a[i], b1.y, acc[i][5]);
+          acc[i][6] = fmaf(a[i], b1.z, acc[i][6]);
+          acc[i][7] = fmaf(a[i], b1.w, acc[i][7]);
+        }
+      }
+    }
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const long long m = row0 + ty * 8 + i;
+      if (m >= n) continue;
+      const float ds = dsp ? dsp[m] : 0.0f;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int k = h * 128 + tx * 4;
+        float4 v = make_float4(acc[i][4 * h], acc[i][4 * h + 1], acc[i][4 * h + 2], acc[i][4 * h + 3]);
+        if (dsp) {
+          v.x = fmaf(ds, ws[k], v.x);
+          v.y = fmaf(ds, ws[k + 1], v.y);
+          v.z = fmaf(ds, ws[k + 2], v.z);
+          v.w = fmaf(ds, ws[k + 3], v.w);
+        }
+        if (mask_off >= 0) {
+          const float4 hm = *reinterpret_cast<const float4 *>(acts + m * kActsLd + mask_off + k);
+          v.x = hm.x > 0.0f ? v.x : 0.0f;
+          v.y = hm.y > 0.0f ? v.y : 0.0f;
+          v.z = hm.z > 0.0f ? v.z : 0.0f;
+          v.w = hm.w > 0.0f ? v.w : 0.0f;
+        }
+        *reinterpret_cast<float4 *>(dz_out + m * kDzLd + k) = v;
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// dW: dW[(k_dst0 + k) * out + n] += sum_m In[m][k] dZ[m][n]; db[n] += sum dZ.
+// grid (N/64, ceil(K/64), m-slices); 4x4 outputs per thread.
+// ---------------------------------------------------------------------------
+constexpr int kMC = 32;
+constexpr long long kMSlice = 8192;
+
+__global__ void __launch_bounds__(256)
+    dw_kernel(const float *__restrict__ acts, int in_off, int K, const float *__restrict__ dz, int N, long long n,
+              float *__restrict__ dW, int out, int k_dst0, float *__restrict__ db) {
+  __shared__ __align__(16) float sA[kMC][64 + 4];
+  __shared__ __align__(16) float sB[kMC][64 + 4];
+  const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+  const int n0 = blockIdx.x * 64, k0 = blockIdx.y * 64;
+  const long long m_begin = (long long)blockIdx.z * kMSlice;
+  const long long m_end = m_begin + kMSlice < n ? m_begin + kMSlice : n;
+  float acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = 0.0f;
+  float bacc[4] = {0.f, 0.f, 0.f, 0.f};
+  const bool do_bias = db && blockIdx.y == 0 && ty == 0;
+  for (long long m0 = m_begin; m0 < m_end; m0 += kMC) {
+    __syncthreads();
+    for (int e = tid; e < kMC * 64; e += 256) {
+      const int mm = e >> 6, c = e & 63;
+      const long long m = m0 + mm;
+      sA[mm][c] = (m < m_end && k0 + c < K) ? acts[m * kActsLd + in_off + k0 + c] : 0.0f;
+      sB[mm][c] = (m < m_end && n0 + c < N) ? dz[m * kDzLd + n0 + c] : 0.0f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int mm = 0; mm < kMC; ++mm) {
+      const float4 a = *reinterpret_cast<const float4 *>(&sA[mm][ty * 4]);
+      const float4 b = *reinterpret_cast<const float4 *>(&sB[mm][tx * 4]);
+      const float av[4] = {a.x, a.y, a.z, a.w}, bv[4] = {b.x, b.y, b.z, b.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(av[i], bv[j], acc[i][j]);
+      if (do_bias) {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) bacc[j] += bv[j];
+      }
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int k = k0 + ty * 4 + i;
+    if (k >= K) continue;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int nn = n0 + tx * 4 + j;
+      if (nn < N) atomicAdd(dW + (long long)(k_dst0 + k) * out + nn, acc[i][j]);
+    }
+  }
+  if (do_bias) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (n0 + tx * 4 + j < N) atomicAdd(db + n0 + tx * 4 + j, bacc[j]);
+  }
+}
+
+static int persistent_grid(long long n) {
+  const long long tiles = (n + kTM - 1) / kTM;
+  const int sms = num_sms();
+  const long long cap = (long long)(sms > 0 ? sms : 148) * 2;
+  return (int)(tiles < cap ? tiles : cap);
+}
+
+static int launch_dw(const float *acts, int in_off, int K, const float *dz, int N, long long n, float *grads,
+                     int flat_layer, int k_dst0, bool bias, cudaStream_t st) {
+  const int out = flat_out(flat_layer);
+  float *dW = grads + flat_offset(flat_layer);
+  float *db = bias ? dW + (long long)flat_in(flat_layer) * out : nullptr;
+  dim3 grid((N + 63) / 64, (K + 63) / 64, (unsigned)((n + kMSlice - 1) / kMSlice));
+  dw_kernel<<<grid, 256, 0, st>>>(acts, in_off, K, dz, N, n, dW, out, k_dst0, db);
+  return launch_status();
+}
+
+static int launch_dx(const float *table_base_W, int g, const float *dz_in, long long n, const float *dsp,
+                     const float *ws, const float *acts, int mask_off, float *dz_out, cudaStream_t st) {
+  if (cudaFuncSetAttribute(dx_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDxSmem) != cudaSuccess)
+    return NERFGB_E_CUDA;
+  dx_kernel<<<persistent_grid(n), 256, kDxSmem, st>>>(table_base_W + gemm_w_offset(g), gemm_n(g), dz_in, n, dsp,
+                                                      ws, acts, mask_off, dz_out);
+  return launch_status();
+}
+
+}  // namespace train
+}  // namespace nerfgb
+
+using namespace nerfgb;
+
+extern "C" long long nerfgb_mlp_acts_floats_per_row(void) { return kActsLd; }
+
+extern "C" long long nerfgb_mlp_backward_workspace_bytes(long long n_rows) {
+  if (n_rows < 0) return -1;
+  return (2 * n_rows * train::kDzLd + n_rows) * (long long)sizeof(float);
+}
+
+extern "C" int nerfgb_mlp_forward_train(const void *packed, const float *xyz, const float *dirs, long long n_rows,
+                                        int rows_per_dir, float *rgb, float *sigma, float *acts, void *stream) {
+  if (n_rows < 0 || rows_per_dir < 1) return NERFGB_E_INVALID_ARG;
+  if (n_rows == 0) return NERFGB_OK;
+  if (!packed || !xyz || !dirs || !rgb || !sigma || !acts || !aligned(packed, 256) || !aligned(acts, 16))
+    return NERFGB_E_INVALID_ARG;
+  return launch_mlp_fp32_store(packed, xyz, dirs, n_rows, rows_per_dir, rgb, sigma, acts, as_stream(stream));
+}
+
+extern "C" int nerfgb_mlp_backward(const void *packed, const float *acts, long long n_rows, const float *d_rgb,
+                                   const float *d_sigma, float *grad_params, void *workspace, void *stream) {
+  using namespace train;
+  if (n_rows < 0) return NERFGB_E_INVALID_ARG;
+  if (n_rows == 0) return NERFGB_OK;
+  if (!packed || !acts || !d_rgb || !grad_params || !workspace || !aligned(packed, 256) || !aligned(acts, 16) ||
+      !aligned(workspace, 16))
+    return NERFGB_E_INVALID_ARG;
+  cudaStream_t st = as_stream(stream);
+  const long long n = n_rows;
+  const float *W = reinterpret_cast<const float *>(packed);  // FP32 pack: padded [Kp][N] blocks
+  const float *table = W + kFp32TableOff;
+  float *bufA = reinterpret_cast<float *>(workspace);
+  float *bufB = bufA + n * kDzLd;
+  float *dsp = bufB + n * kDzLd;
+  int rc;
+  if (cudaFuncSetAttribute(head_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHeadSmem) !=
+      cudaSuccess)
+    return NERFGB_E_CUDA;
+  head_bwd_kernel<<<persistent_grid(n), 256, kHeadSmem, st>>>(table, acts, n, d_rgb, d_sigma, bufA, dsp,
+                                                              grad_params);
+  if ((rc = launch_status()) != NERFGB_OK) return rc;
+  // dense_9 (flat 10): input [bottleneck | enc_dir], output 128.
+  if ((rc = launch_dw(acts, acts_offset(8), 256, bufA, 128, n, grad_params, 10, 0, true, st)) != NERFGB_OK) return rc;
+  if ((rc = launch_dw(acts, kActsEncDir, 27, bufA, 128, n, grad_params, 10, 256, false, st)) != NERFGB_OK) return rc;
+  // dBottleneck = dZ9 W9[0:256]^T (dense_8 is linear: no mask).
+  if ((rc = launch_dx(W, 9, bufA, n, nullptr, nullptr, acts, -1, bufB, st)) != NERFGB_OK) return rc;
+  // dense_8 (flat 9): input h7.
+  if ((rc = launch_dw(acts, acts_offset(7), 256, bufB, 256, n, grad_params, 9, 0, true, st)) != NERFGB_OK) return rc;
+  // dZ7 = (dBott W8^T + dpre_sigma ws) * [h7 > 0]
+  if ((rc = launch_dx(W, 8, bufB, n, dsp, table + kSigmaWOff, acts, acts_offset(7), bufA, st)) != NERFGB_OK)
+    return rc;
+  float *cur = bufA, *nxt = bufB;
+  for (int l = 7; l >= 0; --l) {
+    if (l == 0) {
+      if ((rc = launch_dw(acts, kActsEncXyz, 63, cur, 256, n, grad_params, 0, 0, true, st)) != NERFGB_OK) return rc;
+      break;
+    }
+    if (l == 5) {
+      if ((rc = launch_dw(acts, acts_offset(4), 256, cur, 256, n, grad_params, 5, 0, true, st)) != NERFGB_OK)
+        return rc;
+      if ((rc = launch_dw(acts, kActsEncXyz, 63, cur, 256, n, grad_params, 5, 256, false, st)) != NERFGB_OK)
+        return rc;
+    } else {
+      if ((rc = launch_dw(acts, acts_offset(l - 1), 256, cur, 256, n, grad_params, l, 0, true, st)) != NERFGB_OK)
+        return rc;
+    }
+    if ((rc = launch_dx(W, l, cur, n, nullptr, nullptr, acts, acts_offset(l - 1), nxt, st)) != NERFGB_OK) return rc;
+    float *t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  return NERFGB_OK;
+}

@@ -97,6 +97,30 @@ class NerfMLP:
 
     call = __call__
 
+    def forward_train(self, xyz, dirs, rows_per_dir=1):
+        """FP32 forward that also returns the stored activations for
+        ``backward`` (the tape of tf.GradientTape, model.py:148)."""
+        xyz = as_cuda(xyz, name="xyz")
+        n = xyz.shape[0]
+        dirs = as_cuda(dirs, shape=((n + rows_per_dir - 1) // rows_per_dir, 3), name="dir")
+        rgb, sigma = empty(n, 3), empty(n, 1)
+        acts = empty(n, int(_lib.lib().nerfgb_mlp_acts_floats_per_row()))
+        _lib.call("nerfgb_mlp_forward_train", ptr(self.packed("fp32")), ptr(xyz), ptr(dirs), n,
+                  int(rows_per_dir), ptr(rgb), ptr(sigma), ptr(acts), stream())
+        return rgb, sigma, acts
+
+    def backward(self, acts, d_rgb, d_sigma, grad_params):
+        """Accumulates the parameter gradient of sum(d_rgb*rgb + d_sigma*sigma)
+        into grad_params (flat Keras layout)."""
+        n = acts.shape[0]
+        d_rgb = as_cuda(d_rgb, shape=(n, 3), name="d_rgb")
+        d_sigma = as_cuda(d_sigma, shape=(n,), name="d_sigma")
+        ws = torch.empty(int(_lib.lib().nerfgb_mlp_backward_workspace_bytes(n)), dtype=torch.uint8,
+                         device=acts.device)
+        _lib.call("nerfgb_mlp_backward", ptr(self.packed("fp32")), ptr(acts), n, ptr(d_rgb), ptr(d_sigma),
+                  ptr(grad_params), ptr(ws), stream())
+        return grad_params
+
     def check_device_errors(self):
         """Synchronises and raises if a bounded device wait timed out."""
         torch.cuda.synchronize()
@@ -151,6 +175,73 @@ class NeRF:
     def __call__(self, inputs):
         """model.py:36-55: inputs[0] = (rays_o, rays_d, near, far)."""
         return self.forward(*inputs[0])
+
+    # -- training (model.py:127-180, :396-432) -------------------------------
+    def _train_state(self):
+        if not hasattr(self, "_opt"):
+            z = lambda: torch.zeros(PARAM_COUNT, device=self.coarse_model.params.device)  # noqa: E731
+            self._opt = {"step": 0, "m": [z(), z()], "v": [z(), z()], "g": [z(), z()]}
+        return self._opt
+
+    def train_step(self, data, *, u_coarse=None, u_fine=None, lr=None):
+        """One step of NeRF.train_step (model.py:127-180): forward (FP32, with
+        the activation tape), loss = MSE(coarse) + MSE(fine) (:157-168),
+        gradients by the hand-written backward (compositing, then the MLP),
+        and a Keras Adam step with ExponentialDecay(5e-4, 500000, 0.1)
+        (:413-418). ``data`` = ((rays_o, rays_d, near, far), (rgb,)).
+        Returns {"loss", "coarse_loss", "fine_loss", "psnr"} as floats."""
+        (rays_o, rays_d, near, far), (rgb,) = data
+        p = self.params
+        rays_o = as_cuda(rays_o, name="rays_o")
+        R = rays_o.shape[0]
+        rays_d = as_cuda(rays_d, shape=(R, 3), name="rays_d")
+        target = as_cuda(rgb, shape=(R, 3), name="rgb")
+        st = self._train_state()
+        st["step"] += 1
+        d_cm = ray_utils.create_input_batch_coarse_model(p, rays_o, rays_d, near, far, u_vals=u_coarse)
+        t_c = d_cm["t_vals"]
+        Sc = t_c.shape[1]
+        rgb_c, sig_c, acts_c = self.coarse_model.forward_train(d_cm["xyz_inputs"], rays_d, rows_per_dir=Sc)
+        pp_c = ray_utils.post_process_model_output(rgb_c, sig_c, t_c, self.white_bg, trans_mode=self.trans_mode)
+        d_fm = ray_utils.create_input_batch_fine_model(p, rays_o, rays_d, pp_c["weights"], d_cm["bin_data"],
+                                                       t_c, u_vals=u_fine)
+        t_f = d_fm["t_vals"]
+        S = t_f.shape[1]
+        rgb_f, sig_f, acts_f = self.fine_model.forward_train(d_fm["xyz_inputs"], rays_d, rows_per_dir=S)
+        pp_f = ray_utils.post_process_model_output(rgb_f, sig_f, t_f, self.white_bg, trans_mode=self.trans_mode)
+        loss = torch.zeros(3, device=rays_o.device)
+        grads_map = []
+        for k, pp in enumerate((pp_c, pp_f)):
+            g = empty(R, 3)
+            _lib.call("nerfgb_mse_loss", ptr(pp["pred_rgb"]), ptr(target), R * 3, 1.0, ptr(loss[k:k + 1]),
+                      ptr(g), stream())
+            grads_map.append(g)
+        for k, (model, sig, t, rgb_s, acts) in enumerate(((self.coarse_model, sig_c, t_c, rgb_c, acts_c),
+                                                          (self.fine_model, sig_f, t_f, rgb_f, acts_f))):
+            n, Sk = t.shape
+            d_sig, d_rgb = empty(n * Sk), empty(n * Sk, 3)
+            _lib.call("nerfgb_composite_backward", ptr(sig), ptr(t), ptr(rgb_s), ptr(grads_map[k]), None, n, Sk,
+                      int(self.white_bg), ptr(d_sig), ptr(d_rgb), stream())
+            st["g"][k].zero_()
+            model.backward(acts, d_rgb, d_sig, st["g"][k])
+        # keep the step's tape until the next step (inspection and tests)
+        st["tape"] = {"coarse": (t_c, sig_c, rgb_c, acts_c, pp_c["pred_rgb"]),
+                      "fine": (t_f, sig_f, rgb_f, acts_f, pp_f["pred_rgb"])}
+        step_lr = 5e-4 * 0.1 ** (st["step"] / 500000.0) if lr is None else lr
+        for k, model in enumerate((self.coarse_model, self.fine_model)):
+            _lib.call("nerfgb_adam_step", ptr(model.params), ptr(st["m"][k]), ptr(st["v"][k]), ptr(st["g"][k]),
+                      PARAM_COUNT, step_lr, 0.9, 0.999, 1e-7, st["step"], stream())
+            model.mark_updated()
+        _lib.call("nerfgb_mse_loss", ptr(pp_f["pred_rgb"]), ptr(target), R * 3, 1.0, ptr(loss[2:3]), None,
+                  stream())
+        lc, lf, mse_f = (float(x) for x in loss.tolist())
+        return {"loss": lc + lf, "coarse_loss": lc, "fine_loss": lf,
+                "psnr": -10.0 * float(torch.log10(torch.tensor(max(mse_f, 1e-30))))}
+
+    def gradients(self):
+        """Flat parameter gradients of the last train_step: (coarse, fine)."""
+        st = self._train_state()
+        return st["g"][0], st["g"][1]
 
     call = __call__
     predict_step = __call__

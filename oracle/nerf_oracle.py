@@ -496,7 +496,26 @@ def mlp_backward(p, xyz, dirs, d_rgb, d_sigma, dtype=F64):
     """Gradient of sum(d_rgb * rgb + d_sigma * sigma) of mlp_forward
     (model.py:334-394) w.r.t. every layer: {name: (dW, db)}."""
     p = {k: (np.asarray(W, dtype), np.asarray(b, dtype)) for k, (W, b) in p.items()}
-    rgb, sigma, a = mlp_forward(p, xyz, dirs, dtype, cache=True)
+    _, _, a = mlp_forward(p, xyz, dirs, dtype, cache=True)
+    return mlp_backward_cached(p, a, d_rgb, d_sigma, dtype)
+
+
+def acts_from_tape(tape, dtype=F64):
+    """The activation cache of mlp_forward from a stored tape [n, 2528]:
+    enc_xyz [64] | h0..h7 [8 x 256] | bottleneck [256] | enc_dir [32] | h9."""
+    t = np.asarray(tape, dtype)
+    a = {"enc_xyz": t[:, 0:63], "enc_dir": t[:, 2368:2395], "bott": t[:, 2112:2368], "h9": t[:, 2400:2528]}
+    for i in range(8):
+        a[f"h{i}"] = t[:, 64 + 256 * i:64 + 256 * (i + 1)]
+    return a
+
+
+def mlp_backward_cached(p, a, d_rgb, d_sigma, dtype=F64):
+    """mlp_backward on a given activation cache (the heads are recomputed
+    from h7 and h9)."""
+    p = {k: (np.asarray(W, dtype), np.asarray(b, dtype)) for k, (W, b) in p.items()}
+    rgb = sigmoid(a["h9"] @ p["rgb"][0] + p["rgb"][1])
+    sigma = relu(a["h7"] @ p["sigma"][0] + p["sigma"][1])
     d_sigma = np.asarray(d_sigma, dtype).reshape(-1, 1)
     g = {}
     dz = np.asarray(d_rgb, dtype) * rgb * (1 - rgb)                      # sigmoid
