@@ -6,12 +6,14 @@ hierarchically in 4096-ray chunks with 64 coarse + 128 fine samples per ray
 base_dataset.py:797-861), random-init coarse and fine networks, synthetic
 camera on the radius-4 sphere.
 
-    python bench.py [--gpus N] [--steps K] [--warmup W] [--path bf16|fp32]
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--path bf16|fp32] [--proposal 0|1]
     python bench.py --impl reference ...   # the reference algorithm on host cores
 
-Prints one JSON line (rank 0). `value` is whole-job rays/s with rays resident
-in HBM; `e2e` is the same through NeRF.render with the rays in pinned host
-memory and the rgb/depth/acc maps copied back every step.
+Prints one JSON line (rank 0). `value` is whole-job rays/s of the BF16 +
+learned-proposal path with rays resident in HBM; `e2e` is the same through
+NeRF.render with the rays in pinned host memory and the rgb/depth/acc maps
+copied back every step. `plain_fp32` is the plain FP32 coarse+fine path on
+the same frame, `quality` the PSNR of both against a 64+512-sample render.
 """
 import argparse
 import importlib
@@ -34,6 +36,8 @@ CHUNK = 4096
 SC, SF = 64, 128
 FLOP_PER_SAMPLE = 1186816          # 2 x 593,408 MAC of the 8x256 MLP + heads
 L2_FLUSH_BYTES = 512 << 20         # > 129 MB L2
+SCENE_SEED = 21
+SCENE_MAX_FREQ_LOG2 = 6  # scene band-limited to the proposal's encoding (L=6)
 
 
 def parse():
@@ -49,6 +53,9 @@ def parse():
     ap.add_argument("--kernel", default=None, choices=["mlp"],
                     help="run only the MLP kernel at the fine-pass launch shape (for ncu)")
     ap.add_argument("--rows", type=int, default=CHUNK * (SC + SF))
+    ap.add_argument("--proposal", type=int, default=1, help="1: BF16 + learned proposal (headline)")
+    ap.add_argument("--proposal-steps", type=int, default=2000)
+    ap.add_argument("--train-steps", type=int, default=3)
     return ap.parse_args()
 
 
@@ -201,16 +208,36 @@ def main():
     ng = importlib.import_module("nerf-tf2_gb300")
     dev = torch.device("cuda", local_rank)
     params = ng.make_params(N_coarse=SC, N_fine=SF)
+    # Scene: one sparse-density random-init network as coarse and fine.
+    blob = ng.synthetic.sparse_scene_blob(SCENE_SEED, max_freq_log2=SCENE_MAX_FREQ_LOG2)
+    fast = ng.NeRF(params, precision=args.path, coarse_params=blob, fine_params=blob)
+    plain = ng.NeRF(params, precision="fp32", coarse_params=blob, fine_params=blob)
     # weak scaling: every rank renders its own frame (camera seed = rank)
     frame = ng.synthetic.frame_rays(rank, H, W, FOCAL)
     R = frame[0].shape[0]
     host = [torch.from_numpy(x).pin_memory() for x in frame]
     rays = [h.to(dev) for h in host]
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
-    nerf = ng.NeRF(params, precision=args.path, seed=0)
-    nerf_plain = ng.NeRF(params, precision="fp32", seed=0)
-    launches_per_chunk = 8  # 2 Philox, coarse sample, MLP, composite, fine sample, MLP, composite
     n_chunks = (R + CHUNK - 1) // CHUNK
+
+    # Learned proposal: trained (untimed) by the library's own kernels on the
+    # coarse-pass weight histograms of 200k rays of this scene.
+    proposal = None
+    prop_info = None
+    if args.proposal:
+        t0 = time.perf_counter()
+        tr = [torch.from_numpy(x).to(dev) for x in ng.synthetic.training_rays(100 + rank, 8, 25000)]
+        g = torch.Generator(device=dev)
+        g.manual_seed(0)
+        uc = torch.rand(tr[0].shape[0], SC, device=dev, generator=g)
+        w_t = ng.proposal.coarse_histograms(fast, *tr, uc)
+        proposal = ng.ProposalNetwork(seed=7)
+        losses = ng.ProposalTrainer(proposal, params, lr=3e-3).fit(*tr, uc, w_t, steps=args.proposal_steps)
+        torch.cuda.synchronize()
+        prop_info = {"train_rays": int(tr[0].shape[0]), "steps": args.proposal_steps,
+                     "loss_first": losses[0], "loss_last": losses[-1],
+                     "train_s": round(time.perf_counter() - t0, 2)}
+    launches_per_chunk = 7 if proposal is not None else 8
 
     def timed_steps(fn, steps, warmup):
         for i in range(warmup):
@@ -230,46 +257,59 @@ def main():
         t = torch.tensor([sum(times)], device=dev, dtype=torch.float64)
         if world > 1:
             tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        return float(t.item()) / steps, times
+        return float(t.item()) / steps
 
-    # device-resident throughput
+    # headline: device-resident frame through the fast path
     def step(i):
-        nerf.render(*rays, chunk=CHUNK, seed=1000 * i)
+        fast.render(*rays, chunk=CHUNK, seed=1000 * i, proposal=proposal)
     bus = getattr(torch.cuda.get_device_properties(dev), "pci_bus_id", None)
     with ClockSampler(str(bus) if bus is not None else None) as clk:
-        ms, _ = timed_steps(step, args.steps, args.warmup)
+        ms = timed_steps(step, args.steps, args.warmup)
     value = world * R / (ms / 1000.0)
 
     # end to end: pinned host rays in, maps out, through the public API
-    out_host = {k: torch.empty((R, 3) if k == "rgb" else (R,), pin_memory=True)
-                for k in ("rgb", "depth", "acc")}
+    out_host = {k: torch.empty((R, 3) if k == "rgb" else (R,), pin_memory=True) for k in ("rgb", "depth", "acc")}
 
     def e2e_step(i):
         dr = [h.to(dev, non_blocking=True) for h in host]
-        out = nerf.render(*dr, chunk=CHUNK, seed=1000 * i)
+        out = fast.render(*dr, chunk=CHUNK, seed=1000 * i, proposal=proposal)
         for k in out_host:
             out_host[k].copy_(out[k], non_blocking=True)
-    e2e_ms, _ = timed_steps(e2e_step, max(2, args.steps // 2), 1)
+    e2e_ms = timed_steps(e2e_step, max(2, args.steps // 2), 1)
     h2d = sum(h.numel() * h.element_size() for h in host)
     d2h = sum(v.numel() * v.element_size() for v in out_host.values())
 
-    # plain FP32 path (the 20x denominator) and the image gap against it
-    if args.path != "fp32":
-        plain_ms, _ = timed_steps(lambda i: nerf_plain.render(*rays, chunk=CHUNK, seed=1000 * i),
-                                  args.plain_steps, 1)
-        img_fast = nerf.render(*rays, chunk=CHUNK, seed=7)["rgb"]
-        img_plain = nerf_plain.render(*rays, chunk=CHUNK, seed=7)["rgb"]
-        psnr_vs_plain = ng.psnr(img_plain, img_fast)
-        max_abs_vs_plain = float((img_plain - img_fast).abs().max())
-    else:
-        plain_ms, psnr_vs_plain, max_abs_vs_plain = ms, float("inf"), 0.0
-    plain_value = world * R / (plain_ms / 1000.0)
+    # the plain paths: FP32 coarse+fine (the denominator) and BF16 coarse+fine
+    plain_ms = timed_steps(lambda i: plain.render(*rays, chunk=CHUNK, seed=1000 * i), args.plain_steps, 1)
+    bf16_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, seed=1000 * i), args.plain_steps, 1) \
+        if proposal is not None else ms
+
+    # quality on every 4th image row (160k rays), same uniforms for all paths;
+    # ground truth = the plain FP32 path with 512 fine samples
+    rows = torch.arange(0, H, 4, device=dev)
+    sub = (rows[:, None] * W + torch.arange(W, device=dev)[None, :]).reshape(-1)
+    sr = [x[sub] for x in rays]
+    img_plain = plain.render(*sr, chunk=CHUNK, seed=7)
+    img_fast = fast.render(*sr, chunk=CHUNK, seed=7, proposal=proposal)
+    img_bf16 = fast.render(*sr, chunk=CHUNK, seed=7)
+    gt = ng.NeRF(ng.make_params(N_coarse=SC, N_fine=512), precision="fp32", coarse_params=blob,
+                 fine_params=blob).render(*sr, chunk=CHUNK, seed=9)["rgb"]
+    psnr_plain, psnr_fast = ng.psnr(gt, img_plain["rgb"]), ng.psnr(gt, img_fast["rgb"])
+    quality = {"rays": int(sub.numel()), "ground_truth": "plain FP32 hierarchical, 64 coarse + 512 fine",
+               "psnr_plain_fp32_db": psnr_plain, "psnr_fast_db": psnr_fast,
+               "psnr_gap_db": psnr_plain - psnr_fast,
+               "gate_max_gap_db": 0.1, "gate_met": bool(psnr_plain - psnr_fast <= 0.1),
+               "psnr_gap_bf16_plain_db": psnr_plain - ng.psnr(gt, img_bf16["rgb"]),
+               "psnr_bf16_plain_db": ng.psnr(gt, img_bf16["rgb"]),
+               "psnr_fast_vs_plain_db": ng.psnr(img_plain["rgb"], img_fast["rgb"]),
+               "depth_mae_fast_vs_plain": float((img_plain["depth"] - img_fast["depth"]).abs().mean()),
+               "mean_acc": float(img_plain["acc"].mean())}
 
     # roofline of the dominant kernel (the MLP) at the fine-pass launch shape
-    rows = CHUNK * (SC + SF)
-    xyz = (torch.rand(rows, 3, device=dev) * 4 - 2)
+    nrows = CHUNK * (SC + SF)
+    xyz = (torch.rand(nrows, 3, device=dev) * 4 - 2)
     dirs = torch.nn.functional.normalize(torch.randn(CHUNK, 3, device=dev), dim=1)
-    mlp = nerf.fine_model
+    mlp = fast.fine_model
     for _ in range(3):
         mlp((xyz, dirs), rows_per_dir=SC + SF)
     kt = []
@@ -288,11 +328,11 @@ def main():
     pk_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(pk_path):
         peaks = json.load(open(pk_path))
-    achieved = rows * FLOP_PER_SAMPLE / (k_ms / 1000.0) / 1e12
+    achieved = nrows * FLOP_PER_SAMPLE / (k_ms / 1000.0) / 1e12
     if args.path == "bf16":
-        peak, src = peaks.get("bf16_tflops"), "measured bf16 burst (MEASURED_PEAKS.json)"
+        peak, src = peaks.get("bf16_tflops"), "of measured: bf16 burst (MEASURED_PEAKS.json)"
         if peak is None:
-            peak, src = 1900.0, "fallback 1.9 PFLOP/s bf16"
+            peak, src = 1900.0, "of fallback: 1.9 PFLOP/s bf16"
         bound = "tensor"
     else:
         clk_max = peaks.get("sm_max_mhz", 2070.0)
@@ -305,6 +345,16 @@ def main():
     if os.path.exists(tr_path):
         traffic = json.load(open(tr_path)).get(f"mlp_{args.path}_fine_chunk_bytes")
 
+    # training step (model.py:127-180): 4096 rays of the scene's renders
+    train = None
+    if args.train_steps > 0:
+        batch = [torch.from_numpy(x[:4096]).to(dev) for x in ng.synthetic.training_rays(500 + rank, 4, 1024)]
+        target = plain.render(*batch, seed=3)["rgb"]
+        student = ng.NeRF(params, precision="fp32", seed=60)
+        tms = timed_steps(lambda i: student.train_step((tuple(batch), (target,))), args.train_steps, 1)
+        train = {"rays_per_s": 4096 / (tms / 1000.0), "ms_per_step": tms, "batch_rays": 4096,
+                 "precision": "fp32 (GEMMs and master weights)"}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         rate, nr = cpu_render_rate(ng, frame, args.cpu_seconds)
@@ -314,19 +364,24 @@ def main():
                          "here); OpenBLAS on all host cores"}
 
     if rank == 0:
+        path = f"{args.path}+proposal" if proposal is not None else f"{args.path} plain hierarchical"
         line = {
             "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": args.path, "data": "synthetic",
             "config": {"workload": "800x800 pinhole frame (focal 1111.111) from a random camera on "
-                                   "the radius-4 sphere, 4096-ray chunks, 64 coarse + 128 fine "
-                                   "samples, random-init coarse+fine 8x256 MLPs",
-                       "rays_per_step_per_gpu": R, "path": f"{args.path} plain hierarchical",
+                                   "the radius-4 sphere, 4096-ray chunks, 64 stratified + 128 fine "
+                                   "samples; scene = one random-init 8x256 network (sigma head x4, "
+                                   "bias -0.5, xyz encoding cut above 2^5 pi) as coarse and fine",
+                       "rays_per_step_per_gpu": R, "path": path,
                        "l2": "512 MB buffer written between timed steps"},
-            "plain_fp32": {"value": plain_value, "unit": "rays/s",
-                           "speedup": value / plain_value},
-            "image_vs_plain_fp32": {"psnr_db": psnr_vs_plain, "max_abs_rgb": max_abs_vs_plain},
-            "roofline": {"kernel": f"mlp_{args.path} fine-pass launch ({rows} rows)", "bound": bound,
+            "plain_fp32": {"value": world * R / (plain_ms / 1000.0), "unit": "rays/s",
+                           "speedup": plain_ms / ms},
+            "bf16_plain": {"value": world * R / (bf16_ms / 1000.0), "unit": "rays/s"},
+            "quality": quality,
+            "proposal": prop_info,
+            "train_step": train,
+            "roofline": {"kernel": f"mlp_{args.path} fine-pass launch ({nrows} rows)", "bound": bound,
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None, "peak_source": src,
                          "traffic": traffic, "launch_ms": k_ms},

@@ -162,7 +162,7 @@ int nerfgb_render_rays(const void *packed_coarse, const void *packed_fine,
 /* ---- learned proposal sampler (not in the reference) ------------------- */
 
 /* Parameters of the proposal network: a 2x64 ReLU MLP on the L=6 positional
- * encoding of xyz (39 inputs) with a softplus density output. Flat float32
+ * encoding of xyz (39 inputs) with a ReLU density output. Flat float32
  * blob of 6,785 values: W1 [39,64], b1 [64], W2 [64,64], b2 [64], W3 [64],
  * b3 [1]. */
 long long nerfgb_proposal_param_count(void);
@@ -177,10 +177,25 @@ int nerfgb_proposal_backward(const float *params, const float *xyz,
                              const float *grad_sigma, long long n,
                              float *grad_params, void *stream);
 
+/* Volume-rendering weights [R, n_bins] of the proposal's densities sigma
+ * [R*n_bins] at t_vals [R, n_bins]: compute_weights (ray_utils.py:426-482)
+ * except that the last interval is the previous spacing instead of 1e10,
+ * so the last bin's weight stays differentiable and can be 0. */
+int nerfgb_proposal_weights(const float *sigma, const float *t_vals,
+                            int n_rays, int n_bins, int trans_mode,
+                            float *weights, void *stream);
+
+/* dL/dsigma [R*n_bins] of nerfgb_proposal_weights given dL/dweights. */
+int nerfgb_proposal_weights_backward(const float *sigma, const float *t_vals,
+                                     const float *grad_weights, int n_rays,
+                                     int n_bins, float *grad_sigma,
+                                     void *stream);
+
 /* nerfgb_render_rays with the proposal network in place of the coarse MLP:
  * its density at the Sc stratified samples, composited as the coarse pass
  * is, gives the PDF of the fine sampler; the fine MLP then runs on the
- * Sc + Sf sorted samples. Outputs the fine rgb/depth/acc maps. Same
+ * Sc + Sf sorted samples. The proposal's weights are those of
+ * nerfgb_proposal_weights. Outputs the fine rgb/depth/acc maps. Same
  * workspace size as nerfgb_render_rays. */
 int nerfgb_render_rays_proposal(const float *proposal_params,
                                 const void *packed_fine, int precision,

@@ -48,6 +48,8 @@ SIGNATURES = {
     "nerfgb_proposal_param_count": (LL, []),
     "nerfgb_proposal_forward": (I, [P, P, LL, P, P]),
     "nerfgb_proposal_backward": (I, [P, P, P, LL, P, P]),
+    "nerfgb_proposal_weights": (I, [P, P, I, I, I, P, P]),
+    "nerfgb_proposal_weights_backward": (I, [P, P, P, I, I, P, P]),
     "nerfgb_render_rays_proposal": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
                                         P, P, P, P, P, P]),
     "nerfgb_composite_backward": (I, [P, P, P, P, P, I, I, I, P, P, P]),

@@ -1,6 +1,11 @@
 // Learned proposal sampler (not in the reference): a 2x64 ReLU MLP on the
 // L=6 positional encoding of xyz (39 inputs, the concatenation convention of
-// nerf/core/model.py:323-330) with a softplus density output. At inference
+// nerf/core/model.py:323-330) with a softplus density output. Its weights
+// are composited over finite bins: the last interval is the previous
+// spacing, not the reference's 1e10 (ray_utils.py:465-468). With 1e10, any
+// positive density in the last bin takes all remaining transmittance and
+// d(alpha_last)/d(sigma) vanishes, so a learned density could neither avoid
+// nor be taught to avoid piling every ray's fine samples into that bin. At inference
 // its density at the 64 stratified samples, composited exactly as the coarse
 // pass is (ray_utils.py:426-482), replaces the coarse MLP's weights as the
 // PDF of the inverse-transform fine sampler (ray_utils.py:276-406).
@@ -218,6 +223,27 @@ int launch_proposal_forward(const float *params, const float *xyz, long long n, 
 using namespace nerfgb;
 
 extern "C" long long nerfgb_proposal_param_count(void) { return prop::kParams; }
+
+extern "C" int nerfgb_proposal_weights(const float *sigma, const float *t_vals, int n_rays, int n_bins, int trans_mode,
+                                       float *weights, void *stream) {
+  if (n_rays < 0 || n_bins < 2) return NERFGB_E_INVALID_ARG;
+  if (n_bins > 2048) return NERFGB_E_UNSUPPORTED;
+  if (trans_mode != NERFGB_TRANS_CUMPROD && trans_mode != NERFGB_TRANS_LOGSUM) return NERFGB_E_UNSUPPORTED;
+  if (n_rays == 0) return NERFGB_OK;
+  if (!sigma || !t_vals || !weights) return NERFGB_E_INVALID_ARG;
+  return launch_composite(nullptr, sigma, t_vals, n_rays, n_bins, 0, trans_mode, -1.0f, weights, nullptr, nullptr,
+                          nullptr, as_stream(stream));
+}
+
+extern "C" int nerfgb_proposal_weights_backward(const float *sigma, const float *t_vals, const float *grad_weights,
+                                                int n_rays, int n_bins, float *grad_sigma, void *stream) {
+  if (n_rays < 0 || n_bins < 2) return NERFGB_E_INVALID_ARG;
+  if (n_bins > 2048) return NERFGB_E_UNSUPPORTED;
+  if (n_rays == 0) return NERFGB_OK;
+  if (!sigma || !t_vals || !grad_weights || !grad_sigma) return NERFGB_E_INVALID_ARG;
+  return launch_composite_bwd(sigma, t_vals, nullptr, nullptr, grad_weights, n_rays, n_bins, 0, -1.0f, grad_sigma,
+                              nullptr, as_stream(stream));
+}
 
 extern "C" int nerfgb_proposal_forward(const float *params, const float *xyz, long long n, float *sigma,
                                        void *stream) {

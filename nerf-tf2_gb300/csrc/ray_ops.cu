@@ -6,6 +6,7 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "mlp_internal.cuh"
 
 namespace nerfgb {
 
@@ -100,7 +101,7 @@ constexpr int kCompWarps = 4;
 
 __global__ void __launch_bounds__(32 * kCompWarps)
     composite_kernel(const float *__restrict__ rgb, const float *__restrict__ sigma,
-                     const float *__restrict__ t, int R, int S, int white_bg, int mode,
+                     const float *__restrict__ t, int R, int S, int white_bg, int mode, float last_delta,
                      float *__restrict__ weights, float *__restrict__ pred_rgb,
                      float *__restrict__ pred_depth, float *__restrict__ acc_map) {
   extern __shared__ float smem[];
@@ -119,8 +120,11 @@ __global__ void __launch_bounds__(32 * kCompWarps)
     // Per-sample alpha and transmittance factor.
     float loc_prod = 1.0f;
     CSum loc{0.0f, 0.0f};
+    // Last interval: 1e10 as the reference (:462-468), or (last_delta < 0)
+    // the previous spacing.
+    const float dlast = last_delta >= 0.0f ? last_delta : (S > 1 ? fsub(s_t[S - 1], s_t[S - 2]) : 1e10f);
     for (int j = j0; j < j1; ++j) {
-      float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : 1e10f;   // :462-468
+      float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : dlast;   // :462-468
       float alpha = fsub(1.0f, expf(fmul(-s_sig[j], delta)));         // :423
       float fac = fadd(fsub(1.0f, alpha), 1e-10f);                    // :480
       if (mode == NERFGB_TRANS_CUMPROD) {
@@ -156,7 +160,7 @@ __global__ void __launch_bounds__(32 * kCompWarps)
     float run_prod = ex_prod;
     CSum run = ex;
     for (int j = j0; j < j1; ++j) {
-      float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : 1e10f;
+      float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : dlast;
       float alpha = fsub(1.0f, expf(fmul(-s_sig[j], delta)));
       float fac = fadd(fsub(1.0f, alpha), 1e-10f);
       float T;
@@ -169,10 +173,12 @@ __global__ void __launch_bounds__(32 * kCompWarps)
       }
       float w = fmul(alpha, T);                                       // :480
       if (weights) weights[base + j] = w;
-      const float *c = rgb + 3 * (base + j);
-      pr = fadd(pr, fmul(w, c[0]));                                   // :534
-      pg = fadd(pg, fmul(w, c[1]));
-      pb = fadd(pb, fmul(w, c[2]));
+      if (rgb) {
+        const float *c = rgb + 3 * (base + j);
+        pr = fadd(pr, fmul(w, c[0]));                                 // :534
+        pg = fadd(pg, fmul(w, c[1]));
+        pb = fadd(pb, fmul(w, c[2]));
+      }
       pd = fadd(pd, fmul(s_t[j], w));                                 // :537
       pa = fadd(pa, w);                                               // :540
     }
@@ -183,7 +189,7 @@ __global__ void __launch_bounds__(32 * kCompWarps)
       pd = fadd(pd, __shfl_xor_sync(0xffffffffu, pd, off));
       pa = fadd(pa, __shfl_xor_sync(0xffffffffu, pa, off));
     }
-    if (lane == 0) {
+    if (lane == 0 && pred_rgb) {
       if (white_bg) {                                                 // :542-544
         float bg = fsub(1.0f, pa);
         pr = fadd(pr, bg);
@@ -383,6 +389,25 @@ extern "C" int nerfgb_positional_encode(const float *x, long long n, int L, floa
   return launch_status();
 }
 
+namespace nerfgb {
+int launch_composite(const float *sample_rgb, const float *sigma, const float *t_vals, int n_rays, int n_samples,
+                     int white_bg, int trans_mode, float last_delta, float *weights, float *pred_rgb,
+                     float *pred_depth, float *acc_map, cudaStream_t stream) {
+  size_t smem = (size_t)kCompWarps * 2 * (n_samples + 1) * sizeof(float);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(composite_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return NERFGB_E_CUDA;
+  int sms = num_sms();
+  int blocks = (n_rays + kCompWarps - 1) / kCompWarps;
+  int cap = (sms > 0 ? sms : 148) * 16;
+  composite_kernel<<<blocks < cap ? blocks : cap, 32 * kCompWarps, smem, stream>>>(
+      sample_rgb, sigma, t_vals, n_rays, n_samples, white_bg, trans_mode, last_delta, weights, pred_rgb,
+      pred_depth, acc_map);
+  return launch_status();
+}
+}  // namespace nerfgb
+
 extern "C" int nerfgb_composite(const float *sample_rgb, const float *sigma, const float *t_vals,
                                 int n_rays, int n_samples, int white_bg, int trans_mode,
                                 float *weights, float *pred_rgb, float *pred_depth, float *acc_map,
@@ -394,18 +419,8 @@ extern "C" int nerfgb_composite(const float *sample_rgb, const float *sigma, con
   if (n_rays == 0) return NERFGB_OK;
   if (!sample_rgb || !sigma || !t_vals || !pred_rgb || !pred_depth || !acc_map)
     return NERFGB_E_INVALID_ARG;
-  size_t smem = (size_t)kCompWarps * 2 * (n_samples + 1) * sizeof(float);
-  if (smem > 48 * 1024 &&
-      cudaFuncSetAttribute(composite_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
-          cudaSuccess)
-    return NERFGB_E_CUDA;
-  int sms = num_sms();
-  int blocks = (n_rays + kCompWarps - 1) / kCompWarps;
-  int cap = (sms > 0 ? sms : 148) * 16;
-  composite_kernel<<<blocks < cap ? blocks : cap, 32 * kCompWarps, smem, as_stream(stream)>>>(
-      sample_rgb, sigma, t_vals, n_rays, n_samples, white_bg, trans_mode, weights, pred_rgb,
-      pred_depth, acc_map);
-  return launch_status();
+  return launch_composite(sample_rgb, sigma, t_vals, n_rays, n_samples, white_bg, trans_mode, 1e10f, weights,
+                          pred_rgb, pred_depth, acc_map, as_stream(stream));
 }
 
 extern "C" int nerfgb_sigma_to_alpha(const float *sigma, const float *diffs, long long n, float *alpha,

@@ -133,10 +133,7 @@ extern "C" int nerfgb_render_rays_proposal(const float *proposal_params, const v
   // The proposal density at the stratified samples replaces the coarse MLP.
   if ((rc = launch_proposal_forward(proposal_params, w.xyz_c, (long long)R * Sc, w.sig_c, st)) != NERFGB_OK)
     return rc;
-  if (cudaMemsetAsync(w.rgb_c, 0, sizeof(float) * 3 * (size_t)R * Sc, st) != cudaSuccess) return NERFGB_E_CUDA;
-  if ((rc = nerfgb_composite(w.rgb_c, w.sig_c, w.t_c, R, Sc, 0, trans_mode, w.w_c, w.map_rgb_c, w.map_depth_c,
-                             w.map_acc_c, stream)) != NERFGB_OK)
-    return rc;
+  if ((rc = nerfgb_proposal_weights(w.sig_c, w.t_c, R, Sc, trans_mode, w.w_c, stream)) != NERFGB_OK) return rc;
   if ((rc = nerfgb_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, uf, R, Sc, Sf, w.xyz_f,
                                nullptr, w.t_f, nullptr, nullptr, stream)) != NERFGB_OK)
     return rc;

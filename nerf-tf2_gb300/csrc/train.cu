@@ -6,6 +6,7 @@
 #include <math.h>
 
 #include "common.cuh"
+#include "mlp_internal.cuh"
 
 namespace nerfgb {
 
@@ -23,7 +24,7 @@ constexpr int kCbWarps = 4;
 __global__ void __launch_bounds__(32 * kCbWarps)
     composite_bwd_kernel(const float *__restrict__ sigma, const float *__restrict__ t,
                          const float *__restrict__ rgb, const float *__restrict__ grad_map,
-                         const float *__restrict__ grad_w, int R, int S, int white_bg,
+                         const float *__restrict__ grad_w, int R, int S, int white_bg, float last_delta,
                          float *__restrict__ grad_sigma, float *__restrict__ grad_rgb) {
   extern __shared__ float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -47,10 +48,11 @@ __global__ void __launch_bounds__(32 * kCbWarps)
     }
     const float Gbg = white_bg ? (G0 + G1 + G2) : 0.0f;
     const int j0 = min(lane * k, S), j1 = min(j0 + k, S);
+    const float dlast = last_delta >= 0.0f ? last_delta : (S > 1 ? s_t[S - 1] - s_t[S - 2] : 1e10f);
     // Exclusive transmittance product across lanes.
     float loc = 1.0f;
     for (int j = j0; j < j1; ++j) {
-      const float d = (j < S - 1) ? s_t[j + 1] - s_t[j] : 1e10f;
+      const float d = (j < S - 1) ? s_t[j + 1] - s_t[j] : dlast;
       loc *= expf(-s_sig[j] * d) + 1e-10f;  // (1 - a) + 1e-10 with 1 - a = exp(-s d)
     }
     float inc = loc;
@@ -63,7 +65,7 @@ __global__ void __launch_bounds__(32 * kCbWarps)
     // Forward sweep: T_i, g_i and the lane's sum of g_i w_i.
     float gw_sum = 0.0f;
     for (int j = j0; j < j1; ++j) {
-      const float d = (j < S - 1) ? s_t[j + 1] - s_t[j] : 1e10f;
+      const float d = (j < S - 1) ? s_t[j + 1] - s_t[j] : dlast;
       const float e = expf(-s_sig[j] * d);
       float g = grad_w ? grad_w[base + j] : 0.0f;
       if (grad_map) {
@@ -85,7 +87,7 @@ __global__ void __launch_bounds__(32 * kCbWarps)
     if (lane == 31) after = 0.0f;
     // Backward sweep over the segment.
     for (int j = j1 - 1; j >= j0; --j) {
-      const float d = (j < S - 1) ? s_t[j + 1] - s_t[j] : 1e10f;
+      const float d = (j < S - 1) ? s_t[j + 1] - s_t[j] : dlast;
       const float e = expf(-s_sig[j] * d);
       const float w = (1.0f - e) * s_T[j];
       const float g = s_g[j];
@@ -154,8 +156,8 @@ static int grid_cap(long long n, int block) {
 }
 
 int launch_composite_bwd(const float *sigma, const float *t, const float *rgb, const float *grad_map,
-                         const float *grad_w, int R, int S, int white_bg, float *grad_sigma, float *grad_rgb,
-                         cudaStream_t stream) {
+                         const float *grad_w, int R, int S, int white_bg, float last_delta, float *grad_sigma,
+                         float *grad_rgb, cudaStream_t stream) {
   size_t smem = (size_t)kCbWarps * 4 * (S + 1) * sizeof(float);
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(composite_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
@@ -165,7 +167,7 @@ int launch_composite_bwd(const float *sigma, const float *t, const float *rgb, c
   int blocks = (R + kCbWarps - 1) / kCbWarps;
   int cap = (sms > 0 ? sms : 148) * 16;
   composite_bwd_kernel<<<blocks < cap ? blocks : cap, 32 * kCbWarps, smem, stream>>>(
-      sigma, t, rgb, grad_map, grad_w, R, S, white_bg, grad_sigma, grad_rgb);
+      sigma, t, rgb, grad_map, grad_w, R, S, white_bg, last_delta, grad_sigma, grad_rgb);
   return launch_status();
 }
 
@@ -184,7 +186,7 @@ extern "C" int nerfgb_composite_backward(const float *sigma, const float *t_vals
       (grad_rgb_map && !sample_rgb))
     return NERFGB_E_INVALID_ARG;
   return launch_composite_bwd(sigma, t_vals, sample_rgb, grad_rgb_map, grad_weights, n_rays, n_samples,
-                              white_bg, grad_sigma, grad_sample_rgb, as_stream(stream));
+                              white_bg, 1e10f, grad_sigma, grad_sample_rgb, as_stream(stream));
 }
 
 extern "C" int nerfgb_mse_loss(const float *pred, const float *target, long long n, float scale, float *loss,

@@ -57,6 +57,19 @@ class ProposalNetwork:
         return grad_params
 
 
+def proposal_weights(sigma, t_vals, trans_mode=None):
+    """Weights [R, S] of proposal densities: compute_weights with the last
+    interval equal to the previous spacing (not 1e10), so the last bin's
+    weight can be 0 and is differentiable."""
+    t_vals = as_cuda(t_vals, name="t_vals")
+    R, S = t_vals.shape
+    sigma = as_cuda(sigma, shape=(R * S,), name="sigma")
+    w = empty(R, S)
+    mode = ray_utils.DEFAULT_TRANS_MODE if trans_mode is None else trans_mode
+    _lib.call("nerfgb_proposal_weights", ptr(sigma), ptr(t_vals), R, S, int(mode), ptr(w), stream())
+    return w
+
+
 def adam_step(params, m, v, grads, step, lr, beta1=0.9, beta2=0.999, eps=1e-7):
     """Keras Adam step (TensorFlow ApplyAdam) on flat device tensors."""
     _lib.call("nerfgb_adam_step", ptr(params), ptr(m), ptr(v), ptr(grads), params.numel(),
@@ -100,14 +113,13 @@ class ProposalTrainer:
         d = ray_utils.create_input_batch_coarse_model(self.params, rays_o, rays_d, near, far, u_vals=u_coarse)
         xyz, t = d["xyz_inputs"], d["t_vals"]
         sigma = self.prop(xyz)
-        w = ray_utils.compute_weights(sigma, t, S, trans_mode=self.trans_mode)
+        w = proposal_weights(sigma, t, self.trans_mode)
         gw = empty(R, S)
         self.loss.zero_()
         _lib.call("nerfgb_envelope_loss", ptr(w), ptr(w_target), R, S, ctypes.c_float(self.lam),
                   ptr(self.loss), ptr(gw), stream())
         gs = empty(R * S)
-        _lib.call("nerfgb_composite_backward", ptr(sigma), ptr(t), None, None, ptr(gw), R, S, 0, ptr(gs), None,
-                  stream())
+        _lib.call("nerfgb_proposal_weights_backward", ptr(sigma), ptr(t), ptr(gw), R, S, ptr(gs), stream())
         self.grads.zero_()
         self.prop.backward(xyz, gs, self.grads)
         self.step_count += 1

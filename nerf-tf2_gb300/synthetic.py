@@ -70,3 +70,42 @@ def frame_rays(seed, H=800, W=800, focal=1111.111, radius=4.0, near=2.0, far=6.0
     n = o.shape[0]
     return (np.ascontiguousarray(o, np.float32), d.astype(np.float32),
             np.full((n, 1), near, np.float32), np.full((n, 1), far, np.float32))
+
+
+def sparse_scene_blob(seed, sigma_scale=4.0, sigma_bias=-0.5, max_freq_log2=None):
+    """Parameters of a random-init NeRF network whose density is concentrated
+    in sparse blobs: Glorot weights (the Keras default) with the sigma head's
+    kernel scaled by `sigma_scale` and its bias set to `sigma_bias`. Used as
+    both the coarse and the fine network (a trained NeRF's coarse and fine
+    networks model the same scene), it gives a scene in which hierarchical
+    sampling matters, unlike a plain random init whose density is noise.
+    With `max_freq_log2` = m, the xyz encoding inputs of frequency 2^l pi,
+    l >= m, are cut from dense_0 and from the dense_5 skip (a band-limited
+    scene, like a real object whose extent is coarser than its detail)."""
+    from .weights import glorot_blob, offsets
+    blob = glorot_blob(seed)
+    off = offsets()
+    ko, bo, i, o = off["sigma"]
+    blob[ko:ko + i * o] *= sigma_scale
+    blob[bo] = sigma_bias
+    if max_freq_log2 is not None:
+        for layer, row0 in (("dense_0", 0), ("dense_5", 256)):
+            ko, bo, i, o = off[layer]
+            W = blob[ko:ko + i * o].reshape(i, o)
+            for c in range(3):
+                for l in range(max_freq_log2, 10):
+                    W[row0 + 3 + c * 20 + 2 * l:row0 + 3 + c * 20 + 2 * l + 2, :] = 0.0
+    return blob
+
+
+def training_rays(seed, n_frames, rays_per_frame, H=800, W=800, focal=1111.111):
+    """`rays_per_frame` random pixels from each of `n_frames` random cameras
+    (the reference's sample-mode batches, base_dataset.py:555-621)."""
+    rng = np.random.default_rng(seed)
+    parts = [[], [], [], []]
+    for f in range(n_frames):
+        o, d, n, fr = frame_rays(seed * 1000 + f, H, W, focal)
+        idx = rng.choice(o.shape[0], rays_per_frame, replace=False)
+        for k, a in enumerate((o, d, n, fr)):
+            parts[k].append(a[idx])
+    return tuple(np.concatenate(p) for p in parts)

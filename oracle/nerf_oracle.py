@@ -380,7 +380,7 @@ def philox_uniform(seed, offset, n):
 # Gradients (the reference takes them with tf.GradientTape, model.py:148-171)
 # ---------------------------------------------------------------------------
 def composite_backward(sigma, t_vals, sample_rgb, grad_rgb_map=None, grad_weights=None,
-                       white_bg=False):
+                       white_bg=False, last_delta=1e10):
     """Analytic gradient of compute_weights/post_process_model_output
     (ray_utils.py:426-551) w.r.t. sigma [R*S] and sample_rgb [R*S,3], given
     dL/dpred_rgb [R,3] and/or dL/dweights [R,S]."""
@@ -389,7 +389,8 @@ def composite_backward(sigma, t_vals, sample_rgb, grad_rgb_map=None, grad_weight
     R, S = t.shape
     sig = np.asarray(sigma, dtype).reshape(R, S)
     rgb = np.asarray(sample_rgb, dtype).reshape(R, S, 3)
-    delta = np.concatenate([t[:, 1:] - t[:, :-1], np.full((R, 1), dtype(1e10), dtype)], 1)
+    dl = t[:, -1:] - t[:, -2:-1] if last_delta is None else np.full((R, 1), dtype(last_delta), dtype)
+    delta = np.concatenate([t[:, 1:] - t[:, :-1], dl], 1)
     e = np.exp(-sig * delta)
     alpha = 1 - e
     fac = dtype(1) - alpha + dtype(1e-10)
@@ -408,6 +409,18 @@ def composite_backward(sigma, t_vals, sample_rgb, grad_rgb_map=None, grad_weight
     d_alpha = g * T - suffix / fac
     d_sigma = d_alpha * delta * e
     return d_sigma.reshape(-1), d_rgb.reshape(-1, 3)
+
+
+def proposal_weights(sigma, t_vals):
+    """compute_weights with the last interval = the previous spacing."""
+    t = np.asarray(t_vals)
+    dtype = t.dtype.type
+    R, S = t.shape
+    delta = np.concatenate([t[:, 1:] - t[:, :-1], t[:, -1:] - t[:, -2:-1]], 1)
+    alpha = 1 - np.exp(-np.asarray(sigma, dtype).reshape(R, S) * delta)
+    fac = dtype(1) - alpha + dtype(1e-10)
+    T = np.concatenate([np.ones((R, 1), dtype), np.cumprod(fac, axis=1)[:, :-1]], 1)
+    return alpha * T
 
 
 def apply_adam(var, m, v, grad, step, lr, beta1=0.9, beta2=0.999, eps=1e-7):
@@ -429,7 +442,9 @@ def lr_schedule(step):
 
 # ---------------------------------------------------------------------------
 # Proposal network (not in the reference): 2x64 ReLU MLP on the L=6 encoding
-# of xyz (39 inputs, model.py:330 concatenation convention), softplus density.
+# of xyz (39 inputs, model.py:330 concatenation convention), softplus density;
+# its weights are composited over finite bins (last interval = the previous
+# spacing instead of ray_utils.py:465's 1e10).
 # Flat blob: W1 [39,64], b1 [64], W2 [64,64], b2 [64], W3 [64], b3 [1].
 # ---------------------------------------------------------------------------
 PROP_SHAPES = (("W1", (39, 64)), ("b1", (64,)), ("W2", (64, 64)), ("b2", (64,)),

@@ -31,6 +31,21 @@ def test_composite_backward_fd(oracle):
         assert abs(fd - dc.reshape(-1)[i]) < 1e-7
 
 
+def test_proposal_weights_backward_fd(oracle):
+    rng = np.random.default_rng(5)
+    R, S = 2, 8
+    t = np.sort(rng.uniform(2, 6, (R, S)), 1)
+    sig = rng.exponential(1.0, R * S)
+    gw = rng.normal(size=(R, S))
+    ds, _ = oracle.composite_backward(sig, t, np.zeros((R * S, 3)), None, gw, False, last_delta=None)
+    for i in range(R * S):
+        a, b = sig.copy(), sig.copy()
+        a[i] += 1e-6
+        b[i] -= 1e-6
+        fd = (np.sum(gw * oracle.proposal_weights(a, t)) - np.sum(gw * oracle.proposal_weights(b, t))) / 2e-6
+        assert abs(fd - ds[i]) < 1e-7
+
+
 def test_mlp_backward_fd(oracle):
     rng = np.random.default_rng(1)
     p = oracle.glorot_params(3, np.float64)
