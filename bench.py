@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--path", default="bf16", choices=["bf16", "fp32"])
+    ap.add_argument("--path", default="bf16", choices=["bf16", "fp8", "fp32"])
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -56,6 +56,7 @@ def parse():
     ap.add_argument("--proposal", type=int, default=1, help="1: BF16 + learned proposal (headline)")
     ap.add_argument("--proposal-steps", type=int, default=2000)
     ap.add_argument("--train-steps", type=int, default=3)
+    ap.add_argument("--sweep", type=int, default=1, help="1: FP32/BF16/FP8 sweep at 65536 rays x 256")
     return ap.parse_args()
 
 
@@ -345,6 +346,24 @@ def main():
     if os.path.exists(tr_path):
         traffic = json.load(open(tr_path)).get(f"mlp_{args.path}_fine_chunk_bytes")
 
+    # precision sweep: 65,536 rays x (64 coarse + 192 fine) samples, every MLP
+    # precision, compensated log-sum transmittance; error against the FP32
+    # path on the same uniforms (the FP64 oracle comparison is in the tests)
+    sweep = None
+    if args.sweep:
+        p5 = ng.make_params(N_coarse=SC, N_fine=192)
+        o5, d5, n5, f5 = [x[:65536] for x in rays]
+        out5, rate5 = {}, {}
+        for prec in ("fp32", "bf16", "fp8"):
+            m5 = ng.NeRF(p5, precision=prec, coarse_params=blob, fine_params=blob)
+            sms = timed_steps(lambda i: m5.render(o5, d5, n5, f5, chunk=16384, seed=50 + i), 2 if prec != "fp32" else 1, 1)
+            rate5[prec] = 65536 / (sms / 1000.0)
+            out5[prec] = m5.render(o5, d5, n5, f5, chunk=16384, seed=77)["rgb"]
+        sweep = {"workload": "65536 rays x (64 coarse + 192 fine) samples, one frame's first 65536 rays",
+                 **{prec: {"rays_per_s": rate5[prec],
+                           "max_abs_rgb_vs_fp32": float((out5[prec] - out5["fp32"]).abs().max()),
+                           "psnr_vs_fp32_db": ng.psnr(out5["fp32"], out5[prec])} for prec in rate5}}
+
     # training step (model.py:127-180): 4096 rays of the scene's renders
     train = None
     if args.train_steps > 0:
@@ -381,6 +400,7 @@ def main():
             "quality": quality,
             "proposal": prop_info,
             "train_step": train,
+            "precision_sweep": sweep,
             "roofline": {"kernel": f"mlp_{args.path} fine-pass launch ({nrows} rows)", "bound": bound,
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None, "peak_source": src,

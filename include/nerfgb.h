@@ -42,6 +42,8 @@ extern "C" {
 /* MLP arithmetic precision. */
 #define NERFGB_PREC_FP32 0 /* FP32 SIMT, FP32 accumulate                      */
 #define NERFGB_PREC_BF16 1 /* BF16 tcgen05 GEMMs, FP32 accumulate (TMEM)      */
+#define NERFGB_PREC_FP8 2  /* FP8-e4m3 tcgen05 GEMMs (per-output-channel weight
+                              scales), FP32 accumulate (TMEM)               */
 
 /* Transmittance evaluation in the compositor. */
 #define NERFGB_TRANS_CUMPROD 0 /* sequential FP32 product, as written          */

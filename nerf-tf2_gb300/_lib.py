@@ -25,6 +25,7 @@ E_DEVICE = -5
 E_SCRATCH_LIMIT = -6
 PREC_FP32 = 0
 PREC_BF16 = 1
+PREC_FP8 = 2
 TRANS_CUMPROD = 0
 TRANS_LOGSUM = 1
 

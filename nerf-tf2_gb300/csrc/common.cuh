@@ -77,6 +77,17 @@ constexpr int kActsEncDir = 64 + 9 * 256;     // 2368
 constexpr int kActsLd = kActsEncDir + 32 + 128;  // 2528
 NG_HD int acts_offset(int g) { return g < 9 ? 64 + 256 * g : kActsEncDir + 32; }
 
+// FP8 pack: the same chunks as BF16 with one byte per weight, e4m3 of
+// W[k][n] / scale[n] (per output channel, scale = max_k |W[k][n]| / 448);
+// core matrices hold 16 K-elements: chunk (n, k) byte offset
+// (k/16)*(N*16) + n*16 + (k%16). Then the FP32 table, then the scales
+// [kBiasElems] (same indexing as the biases).
+constexpr long long kFp8WBytes = kGemmWElems;
+constexpr long long kFp8TableOff = (kFp8WBytes + 1023) / 1024 * 1024;  // bytes
+constexpr long long kFp8ScaleOff = kFp8TableOff + (long long)kTableElems * 4;
+constexpr long long kFp8PackBytes = kFp8ScaleOff + (long long)kBiasElems * 4;
+constexpr float kE4M3Max = 448.0f;
+
 // ---------------------------------------------------------------------------
 // Correctly rounded fp32 arithmetic, never fused into FMA. The reference's
 // TensorFlow ops are separate elementwise kernels, so each step rounds.

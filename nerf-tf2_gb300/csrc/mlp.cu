@@ -8,6 +8,7 @@
 // double-buffered with cp.async. Each thread accumulates an 8x8 register
 // block: 8 rows x (4 + 4) columns.
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 
 #include "common.cuh"
 #include "mlp_internal.cuh"
@@ -29,6 +30,12 @@ __global__ void pack_kernel(const float *__restrict__ flat, int precision, unsig
     float v = (k < gemm_k(g)) ? flat[flat_offset(L) + (long long)k * N + n] : 0.0f;
     if (precision == NERFGB_PREC_FP32) {
       reinterpret_cast<float *>(out)[i] = v;
+    } else if (precision == NERFGB_PREC_FP8) {
+      const float sc = reinterpret_cast<const float *>(out + kFp8ScaleOff)[bias_offset(g) + n];
+      int c = k >> 5, kk = k & 31;
+      long long byte = gemm_w_offset(g) + (long long)c * (32 * N) + (kk >> 4) * (N * 16) + n * 16 + (kk & 15);
+      __nv_fp8_e4m3 q(sc > 0.0f ? v / sc : 0.0f);
+      out[byte] = *reinterpret_cast<unsigned char *>(&q);
     } else {
       int c = k >> 5, kk = k & 31;
       long long byte = gemm_w_offset(g) * 2 + (long long)c * (32 * N * 2) + (kk >> 3) * (N * 16) + n * 16 +
@@ -56,8 +63,21 @@ __global__ void pack_kernel(const float *__restrict__ flat, int precision, unsig
     v = flat[flat_offset(11) + 128 * 3 + (t - kRgbBOff)];
   }
   float *table = reinterpret_cast<float *>(
-      out + (precision == NERFGB_PREC_FP32 ? kFp32TableOff * 4 : kBf16TableOff));
+      out + (precision == NERFGB_PREC_FP32 ? kFp32TableOff * 4
+                                            : precision == NERFGB_PREC_BF16 ? kBf16TableOff : kFp8TableOff));
   table[t] = v;
+}
+
+// FP8 per-output-channel scales: scale[g][n] = max_k |W_g[k][n]| / 448.
+__global__ void fp8_scale_kernel(const float *__restrict__ flat, unsigned char *__restrict__ out) {
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= kBiasElems) return;
+  int g = 0;
+  while (g + 1 < kNumGemm && e >= bias_offset(g + 1)) ++g;
+  const int n = e - bias_offset(g), N = gemm_n(g), L = flat_idx_of_gemm(g);
+  float m = 0.0f;
+  for (int k = 0; k < gemm_k(g); ++k) m = fmaxf(m, fabsf(flat[flat_offset(L) + (long long)k * N + n]));
+  reinterpret_cast<float *>(out + kFp8ScaleOff)[e] = m / kE4M3Max;
 }
 
 // ---------------------------------------------------------------------------
@@ -286,12 +306,19 @@ extern "C" long long nerfgb_mlp_param_count(void) { return kParamCount; }
 extern "C" long long nerfgb_mlp_packed_bytes(int precision) {
   if (precision == NERFGB_PREC_FP32) return kFp32PackBytes;
   if (precision == NERFGB_PREC_BF16) return kBf16PackBytes;
+  if (precision == NERFGB_PREC_FP8) return kFp8PackBytes;
   return -1;
 }
 
 extern "C" int nerfgb_mlp_pack(const float *params, int precision, void *packed, void *stream) {
-  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16) return NERFGB_E_UNSUPPORTED;
+  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16 && precision != NERFGB_PREC_FP8)
+    return NERFGB_E_UNSUPPORTED;
   if (!params || !packed || !aligned(packed, 256) || !aligned(params, 4)) return NERFGB_E_INVALID_ARG;
+  if (precision == NERFGB_PREC_FP8) {
+    fp8_scale_kernel<<<(kBiasElems + 255) / 256, 256, 0, as_stream(stream)>>>(
+        params, reinterpret_cast<unsigned char *>(packed));
+    if (launch_status() != NERFGB_OK) return NERFGB_E_CUDA;
+  }
   long long total = kGemmWElems + kTableElems;
   pack_kernel<<<(int)((total + 255) / 256), 256, 0, as_stream(stream)>>>(
       params, precision, reinterpret_cast<unsigned char *>(packed));
@@ -332,11 +359,14 @@ extern "C" int nerfgb_mlp_forward(const void *packed, int precision, const float
                                   long long n_rows, int rows_per_dir, float *rgb, float *sigma,
                                   int *err_word, void *stream) {
   if (n_rows < 0 || rows_per_dir < 1) return NERFGB_E_INVALID_ARG;
-  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16) return NERFGB_E_UNSUPPORTED;
+  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16 && precision != NERFGB_PREC_FP8)
+    return NERFGB_E_UNSUPPORTED;
   if (n_rows == 0) return NERFGB_OK;
   if (!packed || !xyz || !dirs || !rgb || !sigma || !aligned(packed, 256)) return NERFGB_E_INVALID_ARG;
   if (precision == NERFGB_PREC_FP32)
     return launch_mlp_fp32(packed, xyz, dirs, n_rows, rows_per_dir, rgb, sigma, as_stream(stream));
   if (!err_word) return NERFGB_E_INVALID_ARG;
+  if (precision == NERFGB_PREC_FP8)
+    return launch_mlp_fp8(packed, xyz, dirs, n_rows, rows_per_dir, rgb, sigma, err_word, as_stream(stream));
   return launch_mlp_bf16(packed, xyz, dirs, n_rows, rows_per_dir, rgb, sigma, err_word, as_stream(stream));
 }

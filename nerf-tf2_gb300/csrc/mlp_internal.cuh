@@ -16,6 +16,10 @@ int launch_mlp_fp32_store(const void *packed, const float *xyz, const float *dir
 int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,
                     float *rgb, float *sigma, int *err_word, cudaStream_t stream);
 
+// FP8-e4m3 tcgen05 forward (mlp_tc.cu).
+int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,
+                   float *rgb, float *sigma, int *err_word, cudaStream_t stream);
+
 // Proposal network forward (proposal.cu).
 int launch_proposal_forward(const float *params, const float *xyz, long long n, float *sigma, cudaStream_t stream);
 

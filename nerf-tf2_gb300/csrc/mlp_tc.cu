@@ -31,6 +31,7 @@
 // *err_word = NERFGB_E_TIMEOUT, raises an abort flag that every role polls,
 // drains its own bulk copies and MMAs (bounded), frees TMEM and returns.
 #include <cuda_bf16.h>
+#include <cuda_fp8.h>
 #include <stdint.h>
 
 #include "common.cuh"
@@ -40,24 +41,34 @@ namespace nerfgb {
 namespace tc {
 
 constexpr int kRows = 256;          // rows per CTA tile
-constexpr uint32_t kRingBytes = 48 * 1024;  // weight ring: kRingBytes / (N*KCH*2) stages
 constexpr int kThreads = 18 * 32;
 
-constexpr uint32_t kRingOff = 0;
-constexpr uint32_t kEncOff = 48 * 1024;   // + s * 16K
-constexpr uint32_t kActOff = 80 * 1024;   // + s * 64K
-constexpr uint32_t kTableOff = 208 * 1024;
-constexpr uint32_t kMiscOff = kTableOff + ((kTableElems * 4 + 127) / 128) * 128;
-// misc: full[4] empty[4] accf[2] actr[2] drain (8 B each), tmem slot, abort flag
-constexpr uint32_t kBarFull = kMiscOff;          // [8]
-constexpr uint32_t kBarEmpty = kMiscOff + 64;    // [8]
-constexpr uint32_t kBarAccf = kMiscOff + 128;    // [2]
-constexpr uint32_t kBarActr = kMiscOff + 144;    // [2]
-constexpr uint32_t kBarDrain = kMiscOff + 160;
-constexpr uint32_t kTmemSlot = kMiscOff + 168;
-constexpr uint32_t kAbort = kMiscOff + 172;
-constexpr uint32_t kSigPart = kMiscOff + 192;  // float [2][128]
-constexpr uint32_t kSmemBytes = kSigPart + 2 * 128 * 4;
+// Shared-memory layout. Operands take E = 2 (BF16) or 1 (FP8) bytes per
+// element. TSMEM: the bias/head table (and, for FP8, the per-channel weight
+// scales) live in shared memory; otherwise they are read through L1.
+template <bool TSMEM, bool F8>
+struct Layout {
+  static constexpr uint32_t kE = F8 ? 1 : 2;
+  static constexpr uint32_t kEncBytes = 128 * 64 * kE;   // per sub-tile
+  static constexpr uint32_t kActBytes = 128 * 256 * kE;  // per sub-tile
+  static constexpr uint32_t kTableBytes =
+      TSMEM ? ((kTableElems + (F8 ? kBiasElems : 0)) * 4 + 127) / 128 * 128 : 0;
+  static constexpr uint32_t kRingBytes = F8 ? 112 * 1024 : TSMEM ? 48 * 1024 : 64 * 1024;
+  static constexpr uint32_t kRingOff = 0;
+  static constexpr uint32_t kEncOff = kRingBytes;               // + s * kEncBytes
+  static constexpr uint32_t kActOff = kEncOff + 2 * kEncBytes;  // + s * kActBytes
+  static constexpr uint32_t kTableOff = kActOff + 2 * kActBytes;
+  static constexpr uint32_t kMiscOff = kTableOff + kTableBytes;
+  static constexpr uint32_t kBarFull = kMiscOff;         // [16]
+  static constexpr uint32_t kBarEmpty = kMiscOff + 128;  // [16]
+  static constexpr uint32_t kBarAccf = kMiscOff + 256;   // [2]
+  static constexpr uint32_t kBarActr = kMiscOff + 272;   // [2]
+  static constexpr uint32_t kBarDrain = kMiscOff + 288;
+  static constexpr uint32_t kTmemSlot = kMiscOff + 296;
+  static constexpr uint32_t kAbort = kMiscOff + 300;
+  static constexpr uint32_t kSigPart = kMiscOff + 320;  // float [2][128]
+  static constexpr uint32_t kSmemBytes = kSigPart + 2 * 128 * 4;
+};
 
 constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
 
@@ -106,6 +117,14 @@ __device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t adesc, uint64_t
       "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
       : "memory");
 }
+__device__ __forceinline__ void tc_mma_f8(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+  asm volatile(
+      "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+      "tcgen05.mma.cta_group::1.kind::f8f6f4 [%0], %1, %2, %3, p;\n}\n" ::"r"(d_tmem),
+      "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
 __device__ __forceinline__ void named_sync(int id, int threads) {
   asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(threads) : "memory");
 }
@@ -148,6 +167,20 @@ __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
   return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
+// Instruction descriptor of kind::f8f6f4: E4M3 A and B (format 0, K-major),
+// FP32 D.
+__host__ __device__ constexpr uint32_t idesc_e4m3(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Four floats to four E4M3 bytes (round to nearest, saturate to +-448),
+// v0 in the lowest byte.
+__device__ __forceinline__ uint32_t pack_e4m3x4(float v0, float v1, float v2, float v3) {
+  const uint32_t lo = __nv_cvt_float2_to_fp8x2(make_float2(v0, v1), __NV_SATFINITE, __NV_E4M3);
+  const uint32_t hi = __nv_cvt_float2_to_fp8x2(make_float2(v2, v3), __NV_SATFINITE, __NV_E4M3);
+  return lo | (hi << 16);
+}
+
 __device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
   __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
   return *reinterpret_cast<uint32_t *>(&p);
@@ -161,6 +194,32 @@ __device__ __forceinline__ uint32_t pack_bf16_relu(float lo, float hi) {
 
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
+}
+
+// Stores v[0..32) as the K-elements [k0, k0+32) of row r of a 128-row operand
+// region (K-major core matrices of 16 bytes: 8 BF16 or 16 E4M3 elements;
+// element (r, k) at (k / KW) * 2048 + r * 16 + (k % KW) * E).
+template <bool F8, bool RELU>
+__device__ __forceinline__ void store_row32(uint32_t region, int r, int k0, float (&v)[32]) {
+  if (RELU) {
+#pragma unroll
+    for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.0f);
+  }
+  if (F8) {
+#pragma unroll
+    for (int g = 0; g < 2; ++g)
+      st_shared_v4(region + (uint32_t)(k0 / 16 + g) * 2048u + r * 16,
+                   pack_e4m3x4(v[16 * g], v[16 * g + 1], v[16 * g + 2], v[16 * g + 3]),
+                   pack_e4m3x4(v[16 * g + 4], v[16 * g + 5], v[16 * g + 6], v[16 * g + 7]),
+                   pack_e4m3x4(v[16 * g + 8], v[16 * g + 9], v[16 * g + 10], v[16 * g + 11]),
+                   pack_e4m3x4(v[16 * g + 12], v[16 * g + 13], v[16 * g + 14], v[16 * g + 15]));
+  } else {
+#pragma unroll
+    for (int g = 0; g < 4; ++g)
+      st_shared_v4(region + (uint32_t)(k0 / 8 + g) * 2048u + r * 16, pack_bf16(v[8 * g], v[8 * g + 1]),
+                   pack_bf16(v[8 * g + 2], v[8 * g + 3]), pack_bf16(v[8 * g + 4], v[8 * g + 5]),
+                   pack_bf16(v[8 * g + 6], v[8 * g + 7]));
+  }
 }
 
 // Bounded wait: returns false (after flagging) on timeout or abort.
@@ -182,7 +241,7 @@ __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile
 // Positional encodings written as BF16 A-operand rows.
 // ---------------------------------------------------------------------------
 // enc_xyz columns [32*HF, 32*HF + 32) of row r (63 values, column 63 = 0).
-template <int HF>
+template <int HF, bool F8>
 __device__ __forceinline__ void write_enc_xyz(uint32_t enc, int r, const float (&x)[3]) {
   float v[32];
 #pragma unroll
@@ -202,14 +261,11 @@ __device__ __forceinline__ void write_enc_xyz(uint32_t enc, int r, const float (
     if (ks >= 32 * HF && ks < 32 * HF + 32) v[ks - 32 * HF] = s;
     if (ks + 1 >= 32 * HF && ks + 1 < 32 * HF + 32) v[ks + 1 - 32 * HF] = co;
   }
-#pragma unroll
-  for (int g = 0; g < 4; ++g)
-    st_shared_v4(enc + (uint32_t)(HF * 4 + g) * 2048u + r * 16, pack_bf16(v[8 * g], v[8 * g + 1]),
-                 pack_bf16(v[8 * g + 2], v[8 * g + 3]), pack_bf16(v[8 * g + 4], v[8 * g + 5]),
-                 pack_bf16(v[8 * g + 6], v[8 * g + 7]));
+  store_row32<F8, false>(enc, r, 32 * HF, v);
 }
 
-// enc_dir (27 values, 5 zero pad) into K-groups 0..3 of the enc region.
+// enc_dir (27 values, 5 zero pad) into K-elements 0..31 of the enc region.
+template <bool F8>
 __device__ __forceinline__ void write_enc_dir(uint32_t enc, int r, const float (&d)[3]) {
   float v[32];
 #pragma unroll
@@ -225,11 +281,7 @@ __device__ __forceinline__ void write_enc_dir(uint32_t enc, int r, const float (
     v[3 + 2 * p] = s;
     v[4 + 2 * p] = co;
   }
-#pragma unroll
-  for (int g = 0; g < 4; ++g)
-    st_shared_v4(enc + (uint32_t)g * 2048u + r * 16, pack_bf16(v[8 * g], v[8 * g + 1]),
-                 pack_bf16(v[8 * g + 2], v[8 * g + 3]), pack_bf16(v[8 * g + 4], v[8 * g + 5]),
-                 pack_bf16(v[8 * g + 6], v[8 * g + 7]));
+  store_row32<F8, false>(enc, r, 0, v);
 }
 
 // ---------------------------------------------------------------------------
@@ -239,21 +291,42 @@ __device__ __forceinline__ void write_enc_dir(uint32_t enc, int r, const float (
 // runs A(g) then B(g), each streaming the layer's weights (epilogues overlap
 // MMAs); otherwise A and B share every chunk in lockstep (half the weight
 // traffic, epilogues exposed).
-template <int KCH, int NST, bool PINGPONG>
+// F8: E4M3 operands (kind::f8f6f4, K = 32 per MMA) with per-output-channel
+// weight scales applied in the epilogue; else BF16 (kind::f16, K = 16).
+template <int KCH, int NST, bool PINGPONG, bool TSMEM, bool F8>
 __global__ void __launch_bounds__(kThreads, 1)
-    mlp_bf16_kernel(const uint8_t *__restrict__ packed, const float *__restrict__ xyz,
+    mlp_tc_kernel(const uint8_t *__restrict__ packed, const float *__restrict__ xyz,
                     const float *__restrict__ dirs, long long n, int rpd, float *__restrict__ rgb_out,
                     float *__restrict__ sigma_out, int *__restrict__ err) {
+  using L = Layout<TSMEM, F8>;
+  constexpr uint32_t kE = L::kE;           // bytes per operand element
+  constexpr int KW = 16 / kE;              // K-elements per core-matrix row
+  constexpr int KM = F8 ? 32 : 16;         // K per MMA instruction
+  constexpr uint32_t kRingOff = L::kRingOff, kEncOff = L::kEncOff, kActOff = L::kActOff;
+  constexpr uint32_t kBarFull = L::kBarFull, kBarEmpty = L::kBarEmpty, kBarAccf = L::kBarAccf;
+  constexpr uint32_t kBarActr = L::kBarActr, kBarDrain = L::kBarDrain, kTmemSlot = L::kTmemSlot;
+  constexpr uint32_t kAbort = L::kAbort, kSigPart = L::kSigPart;
+  static_assert(NST * 256 * KCH * kE <= L::kRingBytes && NST <= 16, "ring does not fit");
+  constexpr uint32_t kStageBytes = 256 * KCH * kE;
   extern __shared__ __align__(1024) uint8_t smem[];
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kAbort);
-  float *table = reinterpret_cast<float *>(smem + kTableOff);
+  constexpr long long kTabOff = F8 ? kFp8TableOff : kBf16TableOff;
+  const float *table = TSMEM ? reinterpret_cast<const float *>(smem + L::kTableOff)
+                             : reinterpret_cast<const float *>(packed + kTabOff);
+  // FP8 scales follow the table (shared) or sit at kFp8ScaleOff (global).
+  const float *scales = TSMEM ? table + kTableElems : reinterpret_cast<const float *>(packed + kFp8ScaleOff);
   const long long ntiles = (n + kRows - 1) / kRows;
 
-  {  // bias and head table -> shared memory
-    const float4 *src = reinterpret_cast<const float4 *>(packed + kBf16TableOff);
-    for (int i = threadIdx.x; i < kTableElems / 4; i += kThreads) reinterpret_cast<float4 *>(table)[i] = src[i];
+  if (TSMEM) {  // bias and head table (and scales) -> shared memory
+    const float4 *src = reinterpret_cast<const float4 *>(packed + kTabOff);
+    float4 *dst = reinterpret_cast<float4 *>(smem + L::kTableOff);
+    for (int i = threadIdx.x; i < kTableElems / 4; i += kThreads) dst[i] = src[i];
+    if (F8) {
+      const float4 *ssrc = reinterpret_cast<const float4 *>(packed + kFp8ScaleOff);
+      for (int i = threadIdx.x; i < kBiasElems / 4; i += kThreads) dst[kTableElems / 4 + i] = ssrc[i];
+    }
   }
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; ++s) {
@@ -290,9 +363,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       bool ok = true, issued = false;
       for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         for (int g = 0; g < kNumGemm && ok; ++g) {
-          const uint32_t bytes = (uint32_t)gemm_n(g) * KCH * 2u;
-          const uint8_t *lsrc = packed + gemm_w_offset(g) * 2;
-          const int nch = gemm_kp(g) / KCH;
+          const int N = gemm_n(g), Kp = gemm_kp(g);
+          const uint8_t *lsrc = packed + gemm_w_offset(g) * kE;
+          const int nch = (Kp + KCH - 1) / KCH;  // the last chunk may be 32 K
           for (int s = 0; s < (PINGPONG ? 2 : 1) && ok; ++s) {
             for (int c = 0; c < nch; ++c, ++q) {
               if ((int)(q % NST) != st) continue;
@@ -300,8 +373,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ok = false;
                 break;
               }
+              const int kc = Kp - c * KCH < KCH ? Kp - c * KCH : KCH;
+              const uint32_t bytes = (uint32_t)N * kc * kE;
               mbar_expect_tx(sbase + kBarFull + 8 * st, bytes);
-              bulk_g2s(sbase + kRingOff + st * (256 * KCH * 2), lsrc + (long long)c * bytes, bytes,
+              bulk_g2s(sbase + kRingOff + st * kStageBytes, lsrc + (long long)c * KCH * N * kE, bytes,
                        sbase + kBarFull + 8 * st);
               issued = true;
               phase ^= 1;
@@ -327,8 +402,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         for (int g = 0; g < kNumGemm && ok; ++g) {
           const int N = gemm_n(g);
-          const uint32_t idesc = idesc_bf16(128, N);
-          const int nch = gemm_kp(g) / KCH;
+          const uint32_t idesc = F8 ? idesc_e4m3(128, N) : idesc_bf16(128, N);
+          const int Kp = gemm_kp(g);
+          const int nch = (Kp + KCH - 1) / KCH;  // the last chunk may be 32 K
           // PINGPONG: pass s serves sub-tile s. Lockstep: one pass serves both.
           for (int pass = 0; pass < (PINGPONG ? 2 : 1) && ok; ++pass) {
             const int s_lo = PINGPONG ? pass : 0, s_hi = PINGPONG ? pass : 1;
@@ -347,19 +423,26 @@ __global__ void __launch_bounds__(kThreads, 1)
                 break;
               }
               tc_fence_after();
-              const uint32_t wst = sbase + kRingOff + stage * (256 * KCH * 2);
-              // K rows [k0, k0 + KCH) of this layer's input: enc_xyz for dense_0,
-              // [h | enc_xyz] for dense_5, [bottleneck | enc_dir] for dense_9.
-              const int k0 = c * KCH;
-              const bool from_enc = (g == 0) || ((g == 5 || g == 9) && k0 >= 256);
-              const int kg0 = (g == 0 || !from_enc) ? k0 / 8 : (k0 - 256) / 8;
+              const uint32_t wst = sbase + kRingOff + stage * kStageBytes;
+              const int kc = Kp - c * KCH < KCH ? Kp - c * KCH : KCH;
 #pragma unroll
-              for (int ks = 0; ks < KCH / 16; ++ks) {
+              for (int ks = 0; ks < KCH / KM; ++ks) {
+                if (ks * KM >= kc) break;
+                // K rows [kk, kk + KM) of this layer's input: enc_xyz for
+                // dense_0, [h | enc_xyz] for dense_5, [bottleneck | enc_dir] for
+                // dense_9. Each MMA spans two core-matrix K-groups.
+                const int kk = c * KCH + ks * KM;
+                const bool from_enc = (g == 0) || ((g == 5 || g == 9) && kk >= 256);
+                const int kgA = (g == 0 || !from_enc) ? kk / KW : (kk - 256) / KW;
                 const uint64_t bdesc = smem_desc(wst + (uint32_t)(2 * ks) * (N * 16), N * 16, 128);
                 for (int s = s_lo; s <= s_hi; ++s) {
-                  const uint32_t region = from_enc ? sbase + kEncOff + s * 16384u : sbase + kActOff + s * 65536u;
-                  const uint64_t adesc = smem_desc(region + (uint32_t)(kg0 + 2 * ks) * 2048u, 2048, 128);
-                  tc_mma(tmem + s * 256, adesc, bdesc, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+                  const uint32_t region =
+                      from_enc ? sbase + kEncOff + s * L::kEncBytes : sbase + kActOff + s * L::kActBytes;
+                  const uint64_t adesc = smem_desc(region + (uint32_t)kgA * 2048u, 2048, 128);
+                  if (F8)
+                    tc_mma_f8(tmem + s * 256, adesc, bdesc, idesc, (c > 0 || ks > 0) ? 1u : 0u);
+                  else
+                    tc_mma(tmem + s * 256, adesc, bdesc, idesc, (c > 0 || ks > 0) ? 1u : 0u);
                 }
               }
               issued_any = 1;
@@ -387,8 +470,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     const int ew = warp - 2;
     const int s = ew >> 3, hf = (ew >> 2) & 1, qd = warp & 3;
     const int r = 32 * qd + lane;  // row within the sub-tile (= TMEM lane)
-    const uint32_t enc = sbase + kEncOff + s * 16384u;
-    const uint32_t act = sbase + kActOff + s * 65536u;
+    const uint32_t enc = sbase + kEncOff + s * L::kEncBytes;
+    const uint32_t act = sbase + kActOff + s * L::kActBytes;
     const uint32_t trow = tmem + ((uint32_t)(32 * qd) << 16) + s * 256 + hf * 128;
     const uint32_t bar_accf = sbase + kBarAccf + 8 * s, bar_actr = sbase + kBarActr + 8 * s;
     float *sig_part = reinterpret_cast<float *>(smem + kSigPart) + s * 128;
@@ -401,9 +484,9 @@ __global__ void __launch_bounds__(kThreads, 1)
 #pragma unroll
       for (int c = 0; c < 3; ++c) x[c] = valid ? xyz[grow * 3 + c] : 0.0f;
       if (hf == 0)
-        write_enc_xyz<0>(enc, r, x);
+        write_enc_xyz<0, F8>(enc, r, x);
       else
-        write_enc_xyz<1>(enc, r, x);
+        write_enc_xyz<1, F8>(enc, r, x);
       fence_proxy_async();
       tc_fence_before();
       mbar_arrive(bar_actr);
@@ -423,27 +506,59 @@ __global__ void __launch_bounds__(kThreads, 1)
             uint32_t raw[32];
             tmem_ld32(trow + j * 32, raw);
             const int col0 = hf * 128 + j * 32;
-            float b[32];
-#pragma unroll
-            for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4 *>(b + i) = *reinterpret_cast<const float4 *>(bias + col0 + i);
-            tmem_wait32(raw);
             float v[32];
+            if (F8) {
+              // acc * scale[col] + bias[col] (per-output-channel weight scale)
+              tmem_wait32(raw);
 #pragma unroll
-            for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(raw[i]) + b[i];
+              for (int i = 0; i < 32; i += 4) {
+                const float4 b4 = *reinterpret_cast<const float4 *>(bias + col0 + i);
+                const float4 s4 = *reinterpret_cast<const float4 *>(scales + bias_offset(g) + col0 + i);
+                v[i] = fmaf(__uint_as_float(raw[i]), s4.x, b4.x);
+                v[i + 1] = fmaf(__uint_as_float(raw[i + 1]), s4.y, b4.y);
+                v[i + 2] = fmaf(__uint_as_float(raw[i + 2]), s4.z, b4.z);
+                v[i + 3] = fmaf(__uint_as_float(raw[i + 3]), s4.w, b4.w);
+              }
+            } else {
+              float b[32];
+#pragma unroll
+              for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4 *>(b + i) = *reinterpret_cast<const float4 *>(bias + col0 + i);
+              tmem_wait32(raw);
+#pragma unroll
+              for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(raw[i]) + b[i];
+            }
             if (g == 7) {
-              const float *ws = table + kSigmaWOff + col0;
 #pragma unroll
-              for (int i = 0; i < 32; ++i) sig = fmaf(fmaxf(v[i], 0.0f), ws[i], sig);
+              for (int i = 0; i < 32; i += 4) {
+                const float4 w4 = *reinterpret_cast<const float4 *>(table + kSigmaWOff + col0 + i);
+                sig = fmaf(fmaxf(v[i], 0.0f), w4.x, sig);
+                sig = fmaf(fmaxf(v[i + 1], 0.0f), w4.y, sig);
+                sig = fmaf(fmaxf(v[i + 2], 0.0f), w4.z, sig);
+                sig = fmaf(fmaxf(v[i + 3], 0.0f), w4.w, sig);
+              }
             }
             if (g == 9) {
-              const float *wr = table + kRgbWOff + col0 * 3;
 #pragma unroll
-              for (int i = 0; i < 32; ++i) {
-                const float h = fmaxf(v[i], 0.0f);
-                rgb_acc[0] = fmaf(h, wr[3 * i], rgb_acc[0]);
-                rgb_acc[1] = fmaf(h, wr[3 * i + 1], rgb_acc[1]);
-                rgb_acc[2] = fmaf(h, wr[3 * i + 2], rgb_acc[2]);
+              for (int i = 0; i < 32; i += 4) {
+                // rows col0+i .. col0+i+3 of the [128][3] rgb kernel: 12 floats
+                const float *wr = table + kRgbWOff + (col0 + i) * 3;
+                const float4 a4 = *reinterpret_cast<const float4 *>(wr);
+                const float4 b4 = *reinterpret_cast<const float4 *>(wr + 4);
+                const float4 c4 = *reinterpret_cast<const float4 *>(wr + 8);
+                const float w12[12] = {a4.x, a4.y, a4.z, a4.w, b4.x, b4.y, b4.z, b4.w, c4.x, c4.y, c4.z, c4.w};
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                  const float h = fmaxf(v[i + q], 0.0f);
+                  rgb_acc[0] = fmaf(h, w12[3 * q], rgb_acc[0]);
+                  rgb_acc[1] = fmaf(h, w12[3 * q + 1], rgb_acc[1]);
+                  rgb_acc[2] = fmaf(h, w12[3 * q + 2], rgb_acc[2]);
+                }
               }
+            } else if (F8) {
+              if (g == 8)  // dense_8 is linear (model.py:377-378)
+                store_row32<true, false>(act, r, col0, v);
+              else
+                store_row32<true, true>(act, r, col0, v);
             } else if (g == 8) {  // dense_8 is linear (model.py:377-378)
 #pragma unroll
               for (int kg = 0; kg < 4; ++kg)
@@ -472,7 +587,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           float d[3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) d[c] = dirs[dr * 3 + c];
-          write_enc_dir(enc, r, d);
+          write_enc_dir<F8>(enc, r, d);
         }
         if (g == 9) {
           if (hf == 0 && valid) {
@@ -499,28 +614,38 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 }  // namespace tc
 
-template <int KCH, int NST, bool PP>
+template <int KCH, int NST, bool PP, bool TSMEM, bool F8>
 static int launch_variant(const void *packed, const float *xyz, const float *dirs, long long n, int rpd,
                           float *rgb, float *sigma, int *err_word, cudaStream_t stream) {
-  static_assert(NST * 256 * KCH * 2 <= (int)tc::kRingBytes && NST <= 8, "ring does not fit");
-  auto kern = tc::mlp_bf16_kernel<KCH, NST, PP>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tc::kSmemBytes) != cudaSuccess)
+  constexpr uint32_t smem = tc::Layout<TSMEM, F8>::kSmemBytes;
+  static_assert(smem <= 227 * 1024, "shared memory");
+  auto kern = tc::mlp_tc_kernel<KCH, NST, PP, TSMEM, F8>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return NERFGB_E_CUDA;
   const long long ntiles = (n + tc::kRows - 1) / tc::kRows;
   const int sms = num_sms();
   if (sms <= 0) return NERFGB_E_DEVICE;
   const int grid = (int)(ntiles < sms ? ntiles : sms);
-  kern<<<grid, tc::kThreads, tc::kSmemBytes, stream>>>(reinterpret_cast<const uint8_t *>(packed), xyz, dirs, n,
-                                                          rpd, rgb, sigma, err_word);
+  kern<<<grid, tc::kThreads, smem, stream>>>(reinterpret_cast<const uint8_t *>(packed), xyz, dirs, n, rpd, rgb,
+                                             sigma, err_word);
   return launch_status();
 }
 
 int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
                     float *sigma, int *err_word, cudaStream_t stream) {
-  // Lockstep, 32-K chunks, 3 stages: a 48 KB ring cannot cover the bulk-copy
-  // round trip for the ping-pong schedule's weight rate (64 B/clk/SM), while
-  // lockstep needs half of it.
-  return launch_variant<32, 3, false>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
+  // Lockstep, 32-K chunks, 3 stages, tables in shared memory: a 48 KB ring
+  // cannot cover the bulk-copy round trip at the ping-pong schedule's weight
+  // rate (64 B/clk/SM); lockstep needs half of it.
+  return launch_variant<32, 3, false, true, false>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
+}
+
+int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
+                   float *sigma, int *err_word, cudaStream_t stream) {
+  // FP8 halves every operand: 112 KB of ring, 7 stages of 64-K chunks
+  // (16 KB per bulk copy; a copy costs ~200-250 cycles whatever its size up to
+  // 16 KB, so chunks are made as large as the ring allows). Lockstep measured
+  // 8% faster than ping-pong here.
+  return launch_variant<64, 7, false, true, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
 }
 
 }  // namespace nerfgb

@@ -36,6 +36,7 @@ static RenderWs carve(void *base, int R, int Sc, int Sf) {
 int launch_mlp(const void *packed, int precision, const float *xyz, const float *dirs, long long n, int rpd,
                float *rgb, float *sigma, int *err_word, cudaStream_t stream) {
   if (precision == NERFGB_PREC_FP32) return launch_mlp_fp32(packed, xyz, dirs, n, rpd, rgb, sigma, stream);
+  if (precision == NERFGB_PREC_FP8) return launch_mlp_fp8(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
   return launch_mlp_bf16(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
 }
 
@@ -56,12 +57,13 @@ extern "C" int nerfgb_render_rays(const void *packed_coarse, const void *packed_
                                   float *acc_coarse, float *rgb_fine, float *depth_fine, float *acc_fine,
                                   void *workspace, int *err_word, void *stream) {
   if (n_rays < 0 || n_coarse < 2 || n_fine < 1) return NERFGB_E_INVALID_ARG;
-  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16) return NERFGB_E_UNSUPPORTED;
+  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16 && precision != NERFGB_PREC_FP8)
+    return NERFGB_E_UNSUPPORTED;
   if (n_rays == 0) return NERFGB_OK;
   if (!packed_coarse || !packed_fine || !rays_o || !rays_d || !near || !far || !rgb_fine || !depth_fine ||
       !acc_fine || !workspace || !aligned(workspace, 256))
     return NERFGB_E_INVALID_ARG;
-  if (precision == NERFGB_PREC_BF16 && !err_word) return NERFGB_E_INVALID_ARG;
+  if (precision != NERFGB_PREC_FP32 && !err_word) return NERFGB_E_INVALID_ARG;
   cudaStream_t st = as_stream(stream);
   const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
   RenderWs w = carve(workspace, R, Sc, Sf);
@@ -107,12 +109,13 @@ extern "C" int nerfgb_render_rays_proposal(const float *proposal_params, const v
                                            float *rgb_fine, float *depth_fine, float *acc_fine, void *workspace,
                                            int *err_word, void *stream) {
   if (n_rays < 0 || n_coarse < 2 || n_fine < 1) return NERFGB_E_INVALID_ARG;
-  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16) return NERFGB_E_UNSUPPORTED;
+  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16 && precision != NERFGB_PREC_FP8)
+    return NERFGB_E_UNSUPPORTED;
   if (n_rays == 0) return NERFGB_OK;
   if (!proposal_params || !packed_fine || !rays_o || !rays_d || !near || !far || !rgb_fine || !depth_fine ||
       !acc_fine || !workspace || !aligned(workspace, 256))
     return NERFGB_E_INVALID_ARG;
-  if (precision == NERFGB_PREC_BF16 && !err_word) return NERFGB_E_INVALID_ARG;
+  if (precision != NERFGB_PREC_FP32 && !err_word) return NERFGB_E_INVALID_ARG;
   cudaStream_t st = as_stream(stream);
   const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
   RenderWs w = carve(workspace, R, Sc, Sf);

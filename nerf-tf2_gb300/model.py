@@ -8,8 +8,9 @@
   model.py:18-125; returns ``(post_proc_CM, post_proc_FM)``.
 
 The MLP runs as one kernel per call: FP32 SIMT (``precision="fp32"``, the
-plain path) or BF16 tcgen05 GEMMs with FP32 accumulation
-(``precision="bf16"``).
+plain path), BF16 tcgen05 GEMMs (``precision="bf16"``) or FP8-e4m3 tcgen05
+GEMMs with per-output-channel weight scales (``precision="fp8"``), both
+accumulating in FP32.
 """
 import ctypes
 
@@ -19,7 +20,7 @@ from . import _lib, ray_utils
 from ._tensors import as_cuda, device, empty, ptr, stream
 from .weights import PARAM_COUNT, from_dict, glorot_blob, to_dict
 
-PRECISIONS = {"fp32": _lib.PREC_FP32, "bf16": _lib.PREC_BF16}
+PRECISIONS = {"fp32": _lib.PREC_FP32, "bf16": _lib.PREC_BF16, "fp8": _lib.PREC_FP8}
 
 
 class PositionalEncoder:

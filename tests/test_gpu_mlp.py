@@ -84,3 +84,22 @@ def test_mlp_bf16_vs_fp64(ng, oracle, cuda, n):
     assert err_rgb < 2e-2, err_rgb
     assert err_sig < 5e-2, err_sig
     assert np.abs(host(rgb) - r64).mean() < 3e-3
+
+
+@pytest.mark.parametrize("n", [4097, 300])
+def test_mlp_fp8_vs_fp64(ng, oracle, cuda, n):
+    """FP8-e4m3 operands (3 mantissa bits) with per-output-channel weight
+    scales, FP32 accumulation; bounds sized for e4m3 rounding over 10 layers."""
+    blob = biased_blob(ng, 8)
+    x, d = samples(n, 31 + n)
+    mlp = ng.get_coarse_or_fine_model("coarse", params=blob, precision="fp8")
+    rgb, sigma = mlp((dev(x), dev(d)))
+    mlp.check_device_errors()
+    r64, s64 = oracle.mlp_forward(oracle.unpack_params(blob, F64), x, d, F64)
+    err_rgb = np.abs(host(rgb) - r64)
+    assert err_rgb.max() < 6e-2, err_rgb.max()
+    assert err_rgb.mean() < 1e-2, err_rgb.mean()
+    assert np.abs(host(sigma) - s64).max() / max(1.0, np.abs(s64).max()) < 0.15
+    # and clearly coarser than BF16 on the same inputs (the FP8 path is taken)
+    r16, _ = ng.get_coarse_or_fine_model("coarse", params=blob, precision="bf16")((dev(x), dev(d)))
+    assert np.abs(host(r16) - r64).mean() < err_rgb.mean()

@@ -55,7 +55,7 @@ def test_forward_fp32_vs_fp64_oracle(ng, oracle, cuda, case):
     assert err < 2e-3, err
 
 
-@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+@pytest.mark.parametrize("precision", ["fp32", "bf16", "fp8"])
 def test_fused_render_matches_forward(ng, cuda, case, precision):
     R, o, d, n, f, uc, uf, bc, bf = case
     p = ng.make_params()
