@@ -10,10 +10,13 @@ camera on the radius-4 sphere.
     python bench.py --impl reference ...   # the reference algorithm on host cores
 
 Prints one JSON line (rank 0). `value` is whole-job rays/s of the BF16 +
-learned-proposal path with rays resident in HBM; `e2e` is the same through
-NeRF.render with the rays in pinned host memory and the rgb/depth/acc maps
-copied back every step. `plain_fp32` is the plain FP32 coarse+fine path on
-the same frame, `quality` the PSNR of both against a 64+512-sample render.
+learned-proposal path (proposal-gated: the proposal's weights decide which
+coarse samples the NeRF MLP evaluates) with rays resident in HBM; `e2e` is
+the same through NeRF.render with the rays in pinned host memory and the
+rgb/depth/acc maps copied back every step. `plain_fp32` is the plain FP32
+coarse+fine path on the same frame, `quality` the PSNR of both against a
+64+512-sample render; `proposal.replace` reports the proposal used as the
+fine sampler's PDF in place of the coarse pass.
 """
 import argparse
 import importlib
@@ -54,6 +57,8 @@ def parse():
                     help="run only the MLP kernel at the fine-pass launch shape (for ncu)")
     ap.add_argument("--rows", type=int, default=CHUNK * (SC + SF))
     ap.add_argument("--proposal", type=int, default=1, help="1: BF16 + learned proposal (headline)")
+    ap.add_argument("--proposal-mode", default="gate", choices=["gate", "replace"])
+    ap.add_argument("--gate-tau", type=float, default=1e-5)
     ap.add_argument("--proposal-steps", type=int, default=2000)
     ap.add_argument("--train-steps", type=int, default=3)
     ap.add_argument("--sweep", type=int, default=1, help="1: FP32/BF16/FP8 sweep at 65536 rays x 256")
@@ -227,7 +232,7 @@ def main():
     prop_info = None
     if args.proposal:
         t0 = time.perf_counter()
-        tr = [torch.from_numpy(x).to(dev) for x in ng.synthetic.training_rays(100 + rank, 8, 25000)]
+        tr = [torch.from_numpy(x).to(dev) for x in ng.synthetic.training_rays(100 + rank, 100, 2000)]
         g = torch.Generator(device=dev)
         g.manual_seed(0)
         uc = torch.rand(tr[0].shape[0], SC, device=dev, generator=g)
@@ -235,10 +240,17 @@ def main():
         proposal = ng.ProposalNetwork(seed=7)
         losses = ng.ProposalTrainer(proposal, params, lr=3e-3).fit(*tr, uc, w_t, steps=args.proposal_steps)
         torch.cuda.synchronize()
-        prop_info = {"train_rays": int(tr[0].shape[0]), "steps": args.proposal_steps,
+        prop_info = {"train_rays": int(tr[0].shape[0]), "train_cameras": 100, "steps": args.proposal_steps,
+                     "mode": args.proposal_mode, "gate_tau": args.gate_tau,
                      "loss_first": losses[0], "loss_last": losses[-1],
                      "train_s": round(time.perf_counter() - t0, 2)}
-    launches_per_chunk = 7 if proposal is not None else 8
+    # kernels per chunk: 2 uniform draws, coarse sample, [coarse MLP | proposal
+    # forward + weights], composite, fine sample, fine MLP, composite; the
+    # gated path adds the proposal (2), two gates and keeps both MLPs
+    prop_kw = {}
+    if proposal is not None:
+        prop_kw = {"proposal": proposal, "proposal_mode": args.proposal_mode, "gate_tau": args.gate_tau}
+    launches_per_chunk = 8 if proposal is None else (12 if args.proposal_mode == "gate" else 8)
 
     def timed_steps(fn, steps, warmup):
         for i in range(warmup):
@@ -262,7 +274,7 @@ def main():
 
     # headline: device-resident frame through the fast path
     def step(i):
-        fast.render(*rays, chunk=CHUNK, seed=1000 * i, proposal=proposal)
+        fast.render(*rays, chunk=CHUNK, seed=1000 * i, **prop_kw)
     bus = getattr(torch.cuda.get_device_properties(dev), "pci_bus_id", None)
     with ClockSampler(str(bus) if bus is not None else None) as clk:
         ms = timed_steps(step, args.steps, args.warmup)
@@ -273,7 +285,7 @@ def main():
 
     def e2e_step(i):
         dr = [h.to(dev, non_blocking=True) for h in host]
-        out = fast.render(*dr, chunk=CHUNK, seed=1000 * i, proposal=proposal)
+        out = fast.render(*dr, chunk=CHUNK, seed=1000 * i, **prop_kw)
         for k in out_host:
             out_host[k].copy_(out[k], non_blocking=True)
     e2e_ms = timed_steps(e2e_step, max(2, args.steps // 2), 1)
@@ -284,6 +296,10 @@ def main():
     plain_ms = timed_steps(lambda i: plain.render(*rays, chunk=CHUNK, seed=1000 * i), args.plain_steps, 1)
     bf16_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, seed=1000 * i), args.plain_steps, 1) \
         if proposal is not None else ms
+    other_mode = "replace" if args.proposal_mode == "gate" else "gate"
+    other_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, seed=1000 * i, proposal=proposal,
+                                                 proposal_mode=other_mode, gate_tau=args.gate_tau),
+                           args.plain_steps, 1) if proposal is not None else None
 
     # quality on every 4th image row (160k rays), same uniforms for all paths;
     # ground truth = the plain FP32 path with 512 fine samples
@@ -291,7 +307,9 @@ def main():
     sub = (rows[:, None] * W + torch.arange(W, device=dev)[None, :]).reshape(-1)
     sr = [x[sub] for x in rays]
     img_plain = plain.render(*sr, chunk=CHUNK, seed=7)
-    img_fast = fast.render(*sr, chunk=CHUNK, seed=7, proposal=proposal)
+    img_fast = fast.render(*sr, chunk=CHUNK, seed=7, **prop_kw)
+    img_other = fast.render(*sr, chunk=CHUNK, seed=7, proposal=proposal, proposal_mode=other_mode,
+                            gate_tau=args.gate_tau) if proposal is not None else None
     img_bf16 = fast.render(*sr, chunk=CHUNK, seed=7)
     gt = ng.NeRF(ng.make_params(N_coarse=SC, N_fine=512), precision="fp32", coarse_params=blob,
                  fine_params=blob).render(*sr, chunk=CHUNK, seed=9)["rgb"]
@@ -305,6 +323,11 @@ def main():
                "psnr_fast_vs_plain_db": ng.psnr(img_plain["rgb"], img_fast["rgb"]),
                "depth_mae_fast_vs_plain": float((img_plain["depth"] - img_fast["depth"]).abs().mean()),
                "mean_acc": float(img_plain["acc"].mean())}
+    if proposal is not None:
+        prop_info[other_mode] = {"rays_per_s": world * R / (other_ms / 1000.0),
+                                 "psnr_db": ng.psnr(gt, img_other["rgb"]),
+                                 "psnr_gap_db": psnr_plain - ng.psnr(gt, img_other["rgb"]),
+                                 "gate_met": bool(psnr_plain - ng.psnr(gt, img_other["rgb"]) <= 0.1)}
 
     # roofline of the dominant kernel (the MLP) at the fine-pass launch shape
     nrows = CHUNK * (SC + SF)
@@ -383,7 +406,8 @@ def main():
                          "here); OpenBLAS on all host cores"}
 
     if rank == 0:
-        path = f"{args.path}+proposal" if proposal is not None else f"{args.path} plain hierarchical"
+        path = f"{args.path}+proposal ({args.proposal_mode})" if proposal is not None \
+            else f"{args.path} plain hierarchical"
         line = {
             "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -391,7 +415,8 @@ def main():
             "config": {"workload": "800x800 pinhole frame (focal 1111.111) from a random camera on "
                                    "the radius-4 sphere, 4096-ray chunks, 64 stratified + 128 fine "
                                    "samples; scene = one random-init 8x256 network (sigma head x4, "
-                                   "bias -0.5, xyz encoding cut above 2^5 pi) as coarse and fine",
+                                   "bias -0.5, xyz encoding cut above 2^5 pi) as coarse and fine; "
+                                   "proposal 2x64 (L=6) trained on 200k rays from 100 cameras",
                        "rays_per_step_per_gpu": R, "path": path,
                        "l2": "512 MB buffer written between timed steps"},
             "plain_fp32": {"value": world * R / (plain_ms / 1000.0), "unit": "rays/s",

@@ -130,6 +130,18 @@ int nerfgb_mlp_forward(const void *packed, int precision, const float *xyz,
                        const float *dirs, long long n_rows, int rows_per_dir,
                        float *rgb, float *sigma, int *err_word, void *stream);
 
+/* nerfgb_mlp_forward through a row map: logical row k in [0, n) reads xyz
+ * row row_map[k] and dirs row row_map[k] / rows_per_dir and writes rgb/sigma
+ * row row_map[k]; n = min(*n_rows_dev, n_rows_max) read on the device (the
+ * count a gate kernel left there). row_map NULL: the identity; n_rows_dev
+ * NULL: n = n_rows_max. Rows not mapped are left untouched. */
+int nerfgb_mlp_forward_mapped(const void *packed, int precision,
+                              const float *xyz, const float *dirs,
+                              long long n_rows_max, int rows_per_dir,
+                              const int *row_map, const int *n_rows_dev,
+                              float *rgb, float *sigma, int *err_word,
+                              void *stream);
+
 /* ---- uniforms -------------------------------------------------------- */
 
 /* Fills out[0..n) with uniforms in [0,1) from Philox4x32-10 keyed by seed;
@@ -164,7 +176,7 @@ int nerfgb_render_rays(const void *packed_coarse, const void *packed_fine,
 /* ---- learned proposal sampler (not in the reference) ------------------- */
 
 /* Parameters of the proposal network: a 2x64 ReLU MLP on the L=6 positional
- * encoding of xyz (39 inputs) with a ReLU density output. Flat float32
+ * encoding of xyz (39 inputs) with a softplus density output. Flat float32
  * blob of 6,785 values: W1 [39,64], b1 [64], W2 [64,64], b2 [64], W3 [64],
  * b3 [1]. */
 long long nerfgb_proposal_param_count(void);
@@ -210,6 +222,46 @@ int nerfgb_render_rays_proposal(const float *proposal_params,
                                 int trans_mode, float *rgb_fine,
                                 float *depth_fine, float *acc_fine,
                                 void *workspace, int *err_word, void *stream);
+
+/* Coarse sample gate: sample (r, j) is on where weights[r*S + j] > tau (NaN:
+ * off). Writes mask [R*S] (0/1), appends the on samples' indices r*S + j to
+ * row_map (rays in any order, each ray's samples in order) and adds their
+ * number to *count (device; zero it first). */
+int nerfgb_gate_coarse(const float *weights, int n_rays, int n_samples,
+                       float tau, unsigned char *mask, int *row_map,
+                       int *count, void *stream);
+
+/* Fine sample gate over the sorted coarse+fine union [R, n_samples]: member
+ * j is on where it is a fine draw (sort_perm >= n_coarse) or its coarse
+ * sample's mask is on. Appends r*n_samples + j to row_map, adds to *count. */
+int nerfgb_gate_fine(const int *sort_perm, const unsigned char *mask_coarse,
+                     int n_rays, int n_coarse, int n_samples, int *row_map,
+                     int *count, void *stream);
+
+/* Workspace bytes of nerfgb_render_rays_gated (more than
+ * nerfgb_render_workspace_bytes: the gates' masks and row maps). */
+long long nerfgb_render_gated_workspace_bytes(int n_rays, int n_coarse,
+                                              int n_fine);
+
+/* The proposal-gated render: the coarse -> fine chain of nerfgb_render_rays,
+ * with the proposal deciding which samples the NeRF MLP evaluates. Coarse
+ * samples whose proposal weight (nerfgb_proposal_weights of the proposal
+ * density at the stratified samples) is at most gate_tau get sigma = 0 and
+ * are not evaluated, in the coarse pass and again in the fine pass's sorted
+ * union; fine draws are always evaluated. gate_tau < 0 evaluates every
+ * sample and reproduces nerfgb_render_rays' fine maps bit for bit. */
+int nerfgb_render_rays_gated(const float *proposal_params,
+                             const void *packed_coarse,
+                             const void *packed_fine, int precision,
+                             const float *rays_o, const float *rays_d,
+                             const float *near, const float *far,
+                             const float *u_coarse, const float *u_fine,
+                             unsigned long long seed, int n_rays,
+                             int n_coarse, int n_fine, int perturb,
+                             int lin_inv_depth, int white_bg, int trans_mode,
+                             float gate_tau, float *rgb_fine,
+                             float *depth_fine, float *acc_fine,
+                             void *workspace, int *err_word, void *stream);
 
 /* ---- training --------------------------------------------------------- */
 

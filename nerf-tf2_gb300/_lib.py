@@ -42,6 +42,7 @@ SIGNATURES = {
     "nerfgb_sigma_to_alpha": (I, [P, P, LL, P, P]),
     "nerfgb_positional_encode": (I, [P, LL, I, P, P]),
     "nerfgb_mlp_forward": (I, [P, I, P, P, LL, I, P, P, P, P]),
+    "nerfgb_mlp_forward_mapped": (I, [P, I, P, P, LL, I, P, P, P, P, P, P]),
     "nerfgb_uniform": (I, [ULL, ULL, LL, P, P]),
     "nerfgb_render_workspace_bytes": (LL, [I, I, I]),
     "nerfgb_render_rays": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
@@ -53,6 +54,11 @@ SIGNATURES = {
     "nerfgb_proposal_weights_backward": (I, [P, P, P, I, I, P, P]),
     "nerfgb_render_rays_proposal": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
                                         P, P, P, P, P, P]),
+    "nerfgb_gate_coarse": (I, [P, I, I, F, P, P, P, P]),
+    "nerfgb_gate_fine": (I, [P, P, I, I, I, P, P, P]),
+    "nerfgb_render_gated_workspace_bytes": (LL, [I, I, I]),
+    "nerfgb_render_rays_gated": (I, [P, P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I, F,
+                                     P, P, P, P, P, P]),
     "nerfgb_composite_backward": (I, [P, P, P, P, P, I, I, I, P, P, P]),
     "nerfgb_mse_loss": (I, [P, P, LL, F, P, P, P]),
     "nerfgb_envelope_loss": (I, [P, P, I, I, F, P, P, P]),

@@ -17,7 +17,8 @@ CSRC = HERE / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = HERE / "_build"
 LIB = HERE / "libnerfgb.so"
-SOURCES = ["ray_ops.cu", "mlp.cu", "mlp_tc.cu", "render.cu", "render_noalloc.cu", "train.cu", "proposal.cu", "mlp_train.cu"]
+SOURCES = ["ray_ops.cu", "mlp.cu", "mlp_tc.cu", "render.cu", "render_noalloc.cu", "train.cu", "proposal.cu",
+           "mlp_train.cu", "gate.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -167,17 +167,21 @@ __device__ __forceinline__ void store_cols(float *__restrict__ acts, long long r
 }
 
 // STORE: also write every layer's post-activation rows to `acts` (training).
+// rm: optional row map (logical row k reads and writes physical row
+// rm.map[k]) and device row count; not used with STORE.
 template <bool STORE>
 __global__ void __launch_bounds__(256, 1)
     mlp_fp32_kernel(const float *__restrict__ pk, const float *__restrict__ xyz,
-                    const float *__restrict__ dirs, long long n, int rpd, float *__restrict__ rgb,
-                    float *__restrict__ sigma, float *__restrict__ acts) {
+                    const float *__restrict__ dirs, long long n_max, int rpd, float *__restrict__ rgb,
+                    float *__restrict__ sigma, float *__restrict__ acts, RowMap rm) {
   extern __shared__ __align__(16) float sm[];
   float *X = sm;
   float *Wb = sm + kTM * kXLD;
   const float *table = pk + kFp32TableOff;
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
+  const long long n = rm.n_dev ? min((long long)*rm.n_dev, n_max) : n_max;
   const long long ntiles = (n + kTM - 1) / kTM;
+  auto phys = [&](long long k) -> long long { return rm.map ? (long long)rm.map[k] : k; };
 
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const long long row0 = tile * kTM;
@@ -189,12 +193,13 @@ __global__ void __launch_bounds__(256, 1)
       int r = e / 33, j = e - r * 33;
       long long gr = row0 + r;
       bool valid = gr < n;
+      const long long pr = valid ? phys(gr) : 0;
       float *xr = X + r * kXLD + 256;
       if (j < 3) {
-        xr[j] = valid ? xyz[gr * 3 + j] : 0.0f;
+        xr[j] = valid ? xyz[pr * 3 + j] : 0.0f;
       } else {
         int jj = j - 3, c = jj / 10, l = jj - c * 10;
-        float xv = valid ? xyz[gr * 3 + c] : 0.0f;
+        float xv = valid ? xyz[pr * 3 + c] : 0.0f;
         float s, co;
         sincosf(fmul(xv, enc_multiplier(l)), &s, &co);
         xr[3 + c * 20 + 2 * l] = s;
@@ -252,7 +257,7 @@ __global__ void __launch_bounds__(256, 1)
         for (int e = tid; e < kTM * 15; e += 256) {
           int r = e / 15, j = e - r * 15;
           long long gr = row0 + r;
-          long long dr = (gr < n ? gr : n - 1) / rpd;
+          long long dr = phys(gr < n ? gr : n - 1) / rpd;
           float *xr = X + r * kXLD + 256;
           if (j < 3) {
             xr[j] = dirs[dr * 3 + j];
@@ -280,7 +285,7 @@ __global__ void __launch_bounds__(256, 1)
         for (int k = part * 64; k < part * 64 + 64; ++k) s = fmaf(X[r * kXLD + k], sw[k], s);
         s += __shfl_xor_sync(0xffffffffu, s, 1);
         s += __shfl_xor_sync(0xffffffffu, s, 2);
-        if (part == 0 && row0 + r < n) sigma[row0 + r] = fmaxf(s + table[kSigmaBOff], 0.0f);
+        if (part == 0 && row0 + r < n) sigma[phys(row0 + r)] = fmaxf(s + table[kSigmaBOff], 0.0f);
         __syncthreads();
       }
     }
@@ -291,7 +296,7 @@ __global__ void __launch_bounds__(256, 1)
       float s = 0.0f;
       for (int k = 0; k < 128; ++k) s = fmaf(X[r * kXLD + k], rw[k * 3 + c], s);
       s += table[kRgbBOff + c];
-      if (row0 + r < n) rgb[(row0 + r) * 3 + c] = 1.0f / (1.0f + expf(-s));
+      if (row0 + r < n) rgb[phys(row0 + r) * 3 + c] = 1.0f / (1.0f + expf(-s));
     }
     __syncthreads();
   }
@@ -327,7 +332,7 @@ extern "C" int nerfgb_mlp_pack(const float *params, int precision, void *packed,
 
 namespace nerfgb {
 int launch_mlp_fp32(const void *packed, const float *xyz, const float *dirs, long long n, int rpd,
-                    float *rgb, float *sigma, cudaStream_t stream) {
+                    float *rgb, float *sigma, cudaStream_t stream, const RowMap &rm) {
   if (cudaFuncSetAttribute(mlp_fp32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFp32Smem) !=
       cudaSuccess)
     return NERFGB_E_CUDA;
@@ -336,7 +341,7 @@ int launch_mlp_fp32(const void *packed, const float *xyz, const float *dirs, lon
   if (sms <= 0) return NERFGB_E_DEVICE;
   int grid = (int)(ntiles < sms ? ntiles : sms);
   mlp_fp32_kernel<false><<<grid, 256, kFp32Smem, stream>>>(reinterpret_cast<const float *>(packed), xyz, dirs,
-                                                            n, rpd, rgb, sigma, nullptr);
+                                                            n, rpd, rgb, sigma, nullptr, rm);
   return launch_status();
 }
 
@@ -350,7 +355,7 @@ int launch_mlp_fp32_store(const void *packed, const float *xyz, const float *dir
   if (sms <= 0) return NERFGB_E_DEVICE;
   int grid = (int)(ntiles < sms ? ntiles : sms);
   mlp_fp32_kernel<true><<<grid, 256, kFp32Smem, stream>>>(reinterpret_cast<const float *>(packed), xyz, dirs, n,
-                                                           rpd, rgb, sigma, acts);
+                                                           rpd, rgb, sigma, acts, RowMap());
   return launch_status();
 }
 }  // namespace nerfgb
@@ -369,4 +374,21 @@ extern "C" int nerfgb_mlp_forward(const void *packed, int precision, const float
   if (precision == NERFGB_PREC_FP8)
     return launch_mlp_fp8(packed, xyz, dirs, n_rows, rows_per_dir, rgb, sigma, err_word, as_stream(stream));
   return launch_mlp_bf16(packed, xyz, dirs, n_rows, rows_per_dir, rgb, sigma, err_word, as_stream(stream));
+}
+
+extern "C" int nerfgb_mlp_forward_mapped(const void *packed, int precision, const float *xyz, const float *dirs,
+                                         long long n_rows_max, int rows_per_dir, const int *row_map,
+                                         const int *n_rows_dev, float *rgb, float *sigma, int *err_word,
+                                         void *stream) {
+  if (n_rows_max < 0 || rows_per_dir < 1) return NERFGB_E_INVALID_ARG;
+  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16 && precision != NERFGB_PREC_FP8)
+    return NERFGB_E_UNSUPPORTED;
+  if (n_rows_max == 0) return NERFGB_OK;
+  if (!packed || !xyz || !dirs || !rgb || !sigma || !aligned(packed, 256)) return NERFGB_E_INVALID_ARG;
+  if (precision != NERFGB_PREC_FP32 && !err_word) return NERFGB_E_INVALID_ARG;
+  RowMap rm;
+  rm.map = row_map;
+  rm.n_dev = n_rows_dev;
+  return launch_mlp(packed, precision, xyz, dirs, n_rows_max, rows_per_dir, rgb, sigma, err_word,
+                    as_stream(stream), rm);
 }

@@ -4,9 +4,19 @@
 
 namespace nerfgb {
 
+// Optional indirection of an MLP launch's rows. Logical row k in [0, n) is
+// physical row map[k] of xyz, of the outputs and (divided by rows_per_dir)
+// of dirs; with n_dev the row count is read on the device as
+// min(*n_dev, n), so a compaction kernel can feed the MLP without a host
+// round trip. Both NULL: the identity and the host count.
+struct RowMap {
+  const int *map = nullptr;
+  const int *n_dev = nullptr;
+};
+
 // FP32 SIMT forward (mlp.cu).
 int launch_mlp_fp32(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,
-                    float *rgb, float *sigma, cudaStream_t stream);
+                    float *rgb, float *sigma, cudaStream_t stream, const RowMap &rm = RowMap());
 
 // FP32 SIMT forward that also stores every layer's activations (mlp.cu).
 int launch_mlp_fp32_store(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,
@@ -14,11 +24,25 @@ int launch_mlp_fp32_store(const void *packed, const float *xyz, const float *dir
 
 // BF16 tcgen05 forward (mlp_tc.cu).
 int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,
-                    float *rgb, float *sigma, int *err_word, cudaStream_t stream);
+                    float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm = RowMap());
 
 // FP8-e4m3 tcgen05 forward (mlp_tc.cu).
 int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,
-                   float *rgb, float *sigma, int *err_word, cudaStream_t stream);
+                   float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm = RowMap());
+
+// Dispatch on precision (render.cu).
+int launch_mlp(const void *packed, int precision, const float *xyz, const float *dirs, long long n, int rpd,
+               float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm = RowMap());
+
+// Sample gates (gate.cu). Coarse: sample (r, j) is on where w[r*S + j] > tau;
+// writes mask[r*S + j] (0/1), appends the on samples' indices r*S + j to
+// row_map (rays in any order, samples of a ray in order) and adds their
+// number to *count. Fine: sample (r, j) of the sorted union is on where it is
+// a fine draw (perm >= Sc) or its coarse sample's mask is on.
+int launch_gate_coarse(const float *w, int R, int S, float tau, unsigned char *mask, int *row_map, int *count,
+                       cudaStream_t stream);
+int launch_gate_fine(const int *perm, const unsigned char *mask_c, int R, int Sc, int S, int *row_map, int *count,
+                     cudaStream_t stream);
 
 // Proposal network forward (proposal.cu).
 int launch_proposal_forward(const float *params, const float *xyz, long long n, float *sigma, cudaStream_t stream);

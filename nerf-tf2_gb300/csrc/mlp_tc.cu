@@ -457,8 +457,8 @@ __device__ __forceinline__ void issue_tile(uint32_t sbase, uint32_t tmem, RingPo
 template <int KCH, int NST, bool PINGPONG, bool TSMEM, bool F8>
 __global__ void __launch_bounds__(kThreads, 1)
     mlp_tc_kernel(const uint8_t *__restrict__ packed, const float *__restrict__ xyz,
-                    const float *__restrict__ dirs, long long n, int rpd, float *__restrict__ rgb_out,
-                    float *__restrict__ sigma_out, int *__restrict__ err) {
+                    const float *__restrict__ dirs, long long n_max, int rpd, float *__restrict__ rgb_out,
+                    float *__restrict__ sigma_out, int *__restrict__ err, RowMap rm) {
   using L = Layout<TSMEM, F8>;
   constexpr uint32_t kE = L::kE;           // bytes per operand element
   constexpr uint32_t kRingOff = L::kRingOff, kEncOff = L::kEncOff, kActOff = L::kActOff;
@@ -476,7 +476,11 @@ __global__ void __launch_bounds__(kThreads, 1)
                              : reinterpret_cast<const float *>(packed + kTabOff);
   // FP8 scales follow the table (shared) or sit at kFp8ScaleOff (global).
   const float *scales = TSMEM ? table + kTableElems : reinterpret_cast<const float *>(packed + kFp8ScaleOff);
+  // Row count (device-side with a row map from a compaction kernel) and the
+  // physical row of logical row k.
+  const long long n = rm.n_dev ? min((long long)*rm.n_dev, n_max) : n_max;
   const long long ntiles = (n + kRows - 1) / kRows;
+  auto phys = [&](long long k) -> long long { return rm.map ? (long long)rm.map[k] : k; };
 
   if (TSMEM) {  // bias and head table (and scales) -> shared memory
     const float4 *src = reinterpret_cast<const float4 *>(packed + kTabOff);
@@ -585,9 +589,10 @@ __global__ void __launch_bounds__(kThreads, 1)
     for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
       const long long grow = tile * kRows + s * 128 + r;
       const bool valid = grow < n;
+      const long long prow = phys(valid ? grow : n - 1);
       float x[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) x[c] = valid ? xyz[grow * 3 + c] : 0.0f;
+      for (int c = 0; c < 3; ++c) x[c] = valid ? xyz[prow * 3 + c] : 0.0f;
       if (hf == 0)
         write_enc_xyz<0, F8>(enc, r, x);
       else
@@ -684,11 +689,11 @@ __global__ void __launch_bounds__(kThreads, 1)
           // sigma = ReLU(h7 . w + b) (model.py:374-375), halves summed in FP32.
           if (hf == 1) sig_part[r] = sig;
           named_sync(1 + s, 256);
-          if (hf == 0 && valid) sigma_out[grow] = fmaxf(sig + sig_part[r] + table[kSigmaBOff], 0.0f);
+          if (hf == 0 && valid) sigma_out[prow] = fmaxf(sig + sig_part[r] + table[kSigmaBOff], 0.0f);
         }
         if (g == 8 && hf == 0) {
           // enc_dir into the enc region (enc_xyz was last read by dense_5).
-          const long long dr = (valid ? grow : n - 1) / rpd;
+          const long long dr = prow / rpd;
           float d[3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) d[c] = dirs[dr * 3 + c];
@@ -698,7 +703,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (hf == 0 && valid) {
 #pragma unroll
             for (int c = 0; c < 3; ++c)
-              rgb_out[grow * 3 + c] = 1.0f / (1.0f + expf(-(rgb_acc[c] + table[kRgbBOff + c])));
+              rgb_out[prow * 3 + c] = 1.0f / (1.0f + expf(-(rgb_acc[c] + table[kRgbBOff + c])));
           }
         } else {
           fence_proxy_async();
@@ -721,7 +726,7 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 template <int KCH, int NST, bool PP, bool TSMEM, bool F8>
 static int launch_variant(const void *packed, const float *xyz, const float *dirs, long long n, int rpd,
-                          float *rgb, float *sigma, int *err_word, cudaStream_t stream) {
+                          float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm) {
   constexpr uint32_t smem = tc::Layout<TSMEM, F8>::kSmemBytes;
   static_assert(smem <= 227 * 1024, "shared memory");
   auto kern = tc::mlp_tc_kernel<KCH, NST, PP, TSMEM, F8>;
@@ -732,26 +737,26 @@ static int launch_variant(const void *packed, const float *xyz, const float *dir
   if (sms <= 0) return NERFGB_E_DEVICE;
   const int grid = (int)(ntiles < sms ? ntiles : sms);
   kern<<<grid, tc::kThreads, smem, stream>>>(reinterpret_cast<const uint8_t *>(packed), xyz, dirs, n, rpd, rgb,
-                                             sigma, err_word);
+                                             sigma, err_word, rm);
   return launch_status();
 }
 
 int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
-                    float *sigma, int *err_word, cudaStream_t stream) {
+                    float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm) {
   // Ping-pong, 64-K chunks, 2 stages of 32 KB, bias/head table read through
   // L1 so that the ring gets 64 KB. Measured on 786,432 rows: 0.93 ms, against
   // 0.95 (32-K, 3 stages, table in shared memory) and 0.98 (lockstep): the
   // ping-pong schedule hides the epilogue behind the other sub-tile's MMAs but
   // streams every weight byte twice, so it wants the deepest ring.
-  return launch_variant<64, 2, true, false, false>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
+  return launch_variant<64, 2, true, false, false>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream, rm);
 }
 
 int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
-                   float *sigma, int *err_word, cudaStream_t stream) {
+                   float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm) {
   // FP8 halves every operand: 112 KB of ring, 7 stages of 64-K chunks
   // (16 KB per bulk copy). Ping-pong: 0.68 ms on 786,432 rows against 0.83
   // for lockstep; at half the weight bytes the doubled stream fits the ring.
-  return launch_variant<64, 7, true, true, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
+  return launch_variant<64, 7, true, true, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream, rm);
 }
 
 }  // namespace nerfgb

@@ -34,10 +34,11 @@ static RenderWs carve(void *base, int R, int Sc, int Sf) {
 }
 
 int launch_mlp(const void *packed, int precision, const float *xyz, const float *dirs, long long n, int rpd,
-               float *rgb, float *sigma, int *err_word, cudaStream_t stream) {
-  if (precision == NERFGB_PREC_FP32) return launch_mlp_fp32(packed, xyz, dirs, n, rpd, rgb, sigma, stream);
-  if (precision == NERFGB_PREC_FP8) return launch_mlp_fp8(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
-  return launch_mlp_bf16(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream);
+               float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm) {
+  if (precision == NERFGB_PREC_FP32) return launch_mlp_fp32(packed, xyz, dirs, n, rpd, rgb, sigma, stream, rm);
+  if (precision == NERFGB_PREC_FP8)
+    return launch_mlp_fp8(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream, rm);
+  return launch_mlp_bf16(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream, rm);
 }
 
 }  // namespace nerfgb
@@ -142,6 +143,121 @@ extern "C" int nerfgb_render_rays_proposal(const float *proposal_params, const v
     return rc;
   if ((rc = launch_mlp(packed_fine, precision, w.xyz_f, rays_d, (long long)R * S, S, w.rgb_f, w.sig_f, err_word,
                        st)) != NERFGB_OK)
+    return rc;
+  return nerfgb_composite(w.rgb_f, w.sig_f, w.t_f, R, S, white_bg, trans_mode, nullptr, rgb_fine, depth_fine,
+                          acc_fine, stream);
+}
+
+// ---------------------------------------------------------------------------
+// Proposal-gated render: the plain coarse -> fine chain, with the learned
+// proposal deciding which samples the NeRF MLP evaluates. Coarse samples
+// whose proposal weight (finite-bin compositing of the proposal density) is
+// at most gate_tau get sigma = 0 and are not evaluated, in the coarse pass
+// and again as members of the fine pass's sorted union; the fine draws are
+// always evaluated. With gate_tau < 0 every sample is evaluated and the
+// result equals nerfgb_render_rays bit for bit.
+// ---------------------------------------------------------------------------
+namespace nerfgb {
+
+struct GateWs {
+  float *sig_p, *w_p;
+  unsigned char *mask_c;
+  int *map_c, *map_f, *perm, *counts;
+  long long bytes;
+};
+
+static GateWs carve_gate(void *base, int R, int Sc, int Sf) {
+  GateWs g{};
+  const long long r = R, S = Sc + Sf;
+  long long off = carve(nullptr, R, Sc, Sf).bytes;
+  auto take = [&](long long bytes) -> char * {
+    char *p = base ? static_cast<char *>(base) + off : nullptr;
+    off += align256(bytes);
+    return p;
+  };
+  g.sig_p = reinterpret_cast<float *>(take(r * Sc * 4));
+  g.w_p = reinterpret_cast<float *>(take(r * Sc * 4));
+  g.mask_c = reinterpret_cast<unsigned char *>(take(r * Sc));
+  g.map_c = reinterpret_cast<int *>(take(r * Sc * 4));
+  g.map_f = reinterpret_cast<int *>(take(r * S * 4));
+  g.perm = reinterpret_cast<int *>(take(r * S * 4));
+  g.counts = reinterpret_cast<int *>(take(2 * 4));
+  g.bytes = off;
+  return g;
+}
+
+}  // namespace nerfgb
+
+extern "C" long long nerfgb_render_gated_workspace_bytes(int n_rays, int n_coarse, int n_fine) {
+  if (n_rays < 0 || n_coarse < 1 || n_fine < 0) return -1;
+  return carve_gate(nullptr, n_rays, n_coarse, n_fine).bytes;
+}
+
+extern "C" int nerfgb_render_rays_gated(const float *proposal_params, const void *packed_coarse,
+                                        const void *packed_fine, int precision, const float *rays_o,
+                                        const float *rays_d, const float *near, const float *far,
+                                        const float *u_coarse, const float *u_fine, unsigned long long seed,
+                                        int n_rays, int n_coarse, int n_fine, int perturb, int lin_inv_depth,
+                                        int white_bg, int trans_mode, float gate_tau, float *rgb_fine,
+                                        float *depth_fine, float *acc_fine, void *workspace, int *err_word,
+                                        void *stream) {
+  if (n_rays < 0 || n_coarse < 2 || n_fine < 1) return NERFGB_E_INVALID_ARG;
+  if (precision != NERFGB_PREC_FP32 && precision != NERFGB_PREC_BF16 && precision != NERFGB_PREC_FP8)
+    return NERFGB_E_UNSUPPORTED;
+  if ((long long)n_rays * (n_coarse + n_fine) > 0x7fffffffLL) return NERFGB_E_INVALID_ARG;
+  if (n_rays == 0) return NERFGB_OK;
+  if (!proposal_params || !packed_coarse || !packed_fine || !rays_o || !rays_d || !near || !far || !rgb_fine ||
+      !depth_fine || !acc_fine || !workspace || !aligned(workspace, 256))
+    return NERFGB_E_INVALID_ARG;
+  if (precision != NERFGB_PREC_FP32 && !err_word) return NERFGB_E_INVALID_ARG;
+  cudaStream_t st = as_stream(stream);
+  const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
+  RenderWs w = carve(workspace, R, Sc, Sf);
+  GateWs g = carve_gate(workspace, R, Sc, Sf);
+  int rc;
+  const float *uc = u_coarse, *uf = u_fine;
+  // Uniforms: the counters of nerfgb_render_rays, so equal seeds give equal draws.
+  if (perturb && !uc) {
+    if ((rc = nerfgb_uniform(seed, 0, (long long)R * Sc, w.u_c, stream)) != NERFGB_OK) return rc;
+    uc = w.u_c;
+  }
+  if (!uf) {
+    if ((rc = nerfgb_uniform(seed, (unsigned long long)R * Sc, (long long)R * Sf, w.u_f, stream)) != NERFGB_OK)
+      return rc;
+    uf = w.u_f;
+  }
+  if ((rc = nerfgb_coarse_sample(rays_o, rays_d, near, far, uc, R, Sc, perturb, lin_inv_depth, w.xyz_c, nullptr,
+                                 w.t_c, w.edges, w.widths, stream)) != NERFGB_OK)
+    return rc;
+  // Proposal weights over the coarse bins, then the coarse gate.
+  if ((rc = launch_proposal_forward(proposal_params, w.xyz_c, (long long)R * Sc, g.sig_p, st)) != NERFGB_OK)
+    return rc;
+  if ((rc = nerfgb_proposal_weights(g.sig_p, w.t_c, R, Sc, trans_mode, g.w_p, stream)) != NERFGB_OK) return rc;
+  if (cudaMemsetAsync(g.counts, 0, 2 * sizeof(int), st) != cudaSuccess ||
+      cudaMemsetAsync(w.sig_c, 0, (size_t)R * Sc * sizeof(float), st) != cudaSuccess ||
+      cudaMemsetAsync(w.sig_f, 0, (size_t)R * S * sizeof(float), st) != cudaSuccess ||
+      cudaMemsetAsync(w.rgb_f, 0, (size_t)R * S * 3 * sizeof(float), st) != cudaSuccess)
+    return NERFGB_E_CUDA;
+  if ((rc = launch_gate_coarse(g.w_p, R, Sc, gate_tau, g.mask_c, g.map_c, g.counts, st)) != NERFGB_OK) return rc;
+  RowMap rm_c;
+  rm_c.map = g.map_c;
+  rm_c.n_dev = g.counts;
+  if ((rc = launch_mlp(packed_coarse, precision, w.xyz_c, rays_d, (long long)R * Sc, Sc, w.rgb_c, w.sig_c,
+                       err_word, st, rm_c)) != NERFGB_OK)
+    return rc;
+  // Coarse weights exactly as the plain chain computes them (last interval 1e10).
+  if ((rc = launch_composite(nullptr, w.sig_c, w.t_c, R, Sc, white_bg, trans_mode, 1e10f, w.w_c, nullptr, nullptr,
+                             nullptr, st)) != NERFGB_OK)
+    return rc;
+  if ((rc = nerfgb_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, uf, R, Sc, Sf, w.xyz_f,
+                               nullptr, w.t_f, nullptr, g.perm, stream)) != NERFGB_OK)
+    return rc;
+  if ((rc = launch_gate_fine(g.perm, g.mask_c, R, Sc, S, g.map_f, g.counts + 1, st)) != NERFGB_OK) return rc;
+  RowMap rm_f;
+  rm_f.map = g.map_f;
+  rm_f.n_dev = g.counts + 1;
+  if ((rc = launch_mlp(packed_fine, precision, w.xyz_f, rays_d, (long long)R * S, S, w.rgb_f, w.sig_f, err_word,
+                       st, rm_f)) != NERFGB_OK)
     return rc;
   return nerfgb_composite(w.rgb_f, w.sig_f, w.t_f, R, S, white_bg, trans_mode, nullptr, rgb_fine, depth_fine,
                           acc_fine, stream);

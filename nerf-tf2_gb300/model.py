@@ -249,13 +249,20 @@ class NeRF:
 
     # -- fused inference ----------------------------------------------------
     def render(self, rays_o, rays_d, near, far, *, chunk=4096, u_coarse=None, u_fine=None, seed=0,
-               precision=None, return_coarse=False, proposal=None):
+               precision=None, return_coarse=False, proposal=None, proposal_mode="replace",
+               gate_tau=1e-5):
         """Fine (and optionally coarse) rgb/depth/acc maps for every ray, in
         chunks of `chunk` rays (the reference renders 4096-ray batches,
         base_dataset.py:853-857). Uniforms come from Philox keyed by `seed`
-        when not supplied. With `proposal` (a ProposalNetwork) the proposal's
-        weights replace the coarse MLP's as the fine sampler's PDF and no
-        coarse maps are produced."""
+        when not supplied. With `proposal` (a ProposalNetwork) no coarse maps
+        are produced, and `proposal_mode` says how the proposal is used:
+        "replace": its weights replace the coarse MLP's as the fine sampler's
+        PDF (the coarse MLP does not run); "gate": the coarse and fine MLPs
+        run as in the plain chain but skip the coarse samples whose proposal
+        weight is at most `gate_tau` (sigma = 0 there)."""
+        if proposal is not None and proposal_mode not in ("replace", "gate"):
+            raise ValueError(f"proposal_mode must be 'replace' or 'gate', not {proposal_mode!r}")
+        gated = proposal is not None and proposal_mode == "gate"
         prec = PRECISIONS[precision or self.precision]
         rays_o = as_cuda(rays_o, name="rays_o")
         R = rays_o.shape[0]
@@ -271,15 +278,28 @@ class NeRF:
                for k in (["rgb", "depth", "acc"] + (["rgb_coarse", "depth_coarse", "acc_coarse"]
                                                      if return_coarse else []))}
         lib = _lib.lib()
-        ws = torch.empty(lib.nerfgb_render_workspace_bytes(min(chunk, R), Sc, Sf), dtype=torch.uint8,
-                         device=rays_o.device)
+        ws_bytes = (lib.nerfgb_render_gated_workspace_bytes if gated else lib.nerfgb_render_workspace_bytes)(
+            min(chunk, R), Sc, Sf)
+        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=rays_o.device)
         pc, pf = self.coarse_model.packed(precision), self.fine_model.packed(precision)
         for s in range(0, R, chunk):
             e = min(R, s + chunk)
             sl = slice(s, e)
+            if proposal is not None and return_coarse:
+                raise ValueError("the proposal paths have no coarse maps")
+            if gated:
+                _lib.call("nerfgb_render_rays_gated", ptr(proposal.params), ptr(pc), ptr(pf), prec,
+                          ptr(rays_o[sl]), ptr(rays_d[sl]), ptr(near[sl]), ptr(far[sl]),
+                          ptr(u_coarse[sl]) if u_coarse is not None else None,
+                          ptr(u_fine[sl]) if u_fine is not None else None,
+                          ctypes.c_ulonglong(int(seed) + s), e - s, Sc, Sf,
+                          int(bool(self.params.sampling.perturb)),
+                          int(bool(self.params.sampling.lin_inv_depth)), int(self.white_bg),
+                          int(self.trans_mode), ctypes.c_float(gate_tau), ptr(out["rgb"][sl]),
+                          ptr(out["depth"][sl]), ptr(out["acc"][sl]), ptr(ws),
+                          ptr(self.coarse_model.err_word), stream())
+                continue
             if proposal is not None:
-                if return_coarse:
-                    raise ValueError("the proposal path has no coarse maps")
                 _lib.call("nerfgb_render_rays_proposal", ptr(proposal.params), ptr(pf), prec,
                           ptr(rays_o[sl]), ptr(rays_d[sl]), ptr(near[sl]), ptr(far[sl]),
                           ptr(u_coarse[sl]) if u_coarse is not None else None,

@@ -98,14 +98,21 @@ def sparse_scene_blob(seed, sigma_scale=4.0, sigma_bias=-0.5, max_freq_log2=None
     return blob
 
 
-def training_rays(seed, n_frames, rays_per_frame, H=800, W=800, focal=1111.111):
+def training_rays(seed, n_frames, rays_per_frame, H=800, W=800, focal=1111.111, near=2.0, far=6.0):
     """`rays_per_frame` random pixels from each of `n_frames` random cameras
-    (the reference's sample-mode batches, base_dataset.py:555-621)."""
+    (the reference's sample-mode batches, base_dataset.py:555-621). Only the
+    chosen pixels' rays are computed; they equal frame_rays' rows."""
     rng = np.random.default_rng(seed)
-    parts = [[], [], [], []]
+    K = intrinsic(H, W, focal)
+    parts = [[], []]
     for f in range(n_frames):
-        o, d, n, fr = frame_rays(seed * 1000 + f, H, W, focal)
-        idx = rng.choice(o.shape[0], rays_per_frame, replace=False)
-        for k, a in enumerate((o, d, n, fr)):
-            parts[k].append(a[idx])
-    return tuple(np.concatenate(p) for p in parts)
+        c2w = random_pose(seed * 1000 + f)
+        idx = rng.choice(H * W, rays_per_frame, replace=False)
+        u, v = (idx % W).astype(np.float64), (idx // W).astype(np.float64)
+        dirs = np.stack([(u - K[0, 2]) / K[0, 0], (v - K[1, 2]) / K[1, 1], np.ones_like(u)], -1)
+        d = _normalize(dirs @ c2w[:3, :3].T)
+        parts[0].append(np.broadcast_to(c2w[:3, 3], d.shape).astype(np.float32))
+        parts[1].append(d.astype(np.float32))
+    o, d = np.concatenate(parts[0]), np.concatenate(parts[1])
+    n = o.shape[0]
+    return o, d, np.full((n, 1), near, np.float32), np.full((n, 1), far, np.float32)

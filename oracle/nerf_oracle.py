@@ -507,6 +507,50 @@ def prop_loss(w_prop, w_target, lam=3.0):
     return float(np.sum(rho * diff * diff) / R), 2 * rho * diff / R
 
 
+# ---------------------------------------------------------------------------
+# Proposal-gated render (not in the reference): the chain of nerf_forward in
+# which the coarse samples whose proposal weight is at most tau have sigma 0,
+# in the coarse pass and again in the fine pass's sorted union (fine draws
+# are always evaluated; a skipped sample's rgb is 0).
+# ---------------------------------------------------------------------------
+def gate_coarse(w_prop, tau):
+    """On/off of each coarse sample [R, Sc]: w_prop > tau (NaN: off)."""
+    return np.asarray(w_prop) > tau
+
+
+def gate_fine(sort_perm, mask_c):
+    """On/off of each member of the sorted union [R, S]: a fine draw
+    (sort_perm >= Sc) or a coarse sample whose gate is on."""
+    mask_c = np.asarray(mask_c, bool)
+    Sc = mask_c.shape[1]
+    perm = np.asarray(sort_perm)
+    on_c = np.take_along_axis(mask_c, np.minimum(perm, Sc - 1), axis=1)
+    return (perm >= Sc) | on_c
+
+
+def nerf_render_gated(params, prop_blob, p_coarse, p_fine, rays_o, rays_d, near, far,
+                      u_coarse, u_fine, tau, dtype=F32):
+    """Returns (fine post_process_model_output, coarse mask [R,Sc], union
+    mask [R,S], proposal weights [R,Sc])."""
+    d_cm = create_input_batch_coarse_model(params, rays_o, rays_d, near, far, u_coarse, dtype)
+    t_c = d_cm["t_vals"]
+    Sc = t_c.shape[1]
+    w_p = proposal_weights(prop_forward(prop_blob, d_cm["xyz_inputs"], dtype), t_c)
+    m_c = gate_coarse(w_p, tau)
+    _, sig_c = mlp_forward(p_coarse, d_cm["xyz_inputs"], d_cm["dir_inputs"], dtype)
+    sig_c = np.where(m_c.reshape(-1), sig_c.reshape(-1), dtype(0))
+    w_c = compute_weights(sig_c, t_c, Sc)
+    d_fm = create_input_batch_fine_model(params, rays_o, rays_d, w_c, d_cm["bin_data"], t_c,
+                                         u_fine, dtype, return_indices=True)
+    rgb_f, sig_f = mlp_forward(p_fine, d_fm["xyz_inputs"], d_fm["dir_inputs"], dtype)
+    m_f = gate_fine(d_fm["sort_perm"], m_c)
+    on = m_f.reshape(-1)
+    sig_f = np.where(on, sig_f.reshape(-1), dtype(0))
+    rgb_f = np.where(on[:, None], rgb_f, dtype(0))
+    pp = post_process_model_output(rgb_f, sig_f, d_fm["t_vals"], params.system.white_bg)
+    return pp, m_c, m_f, w_p
+
+
 def mlp_backward(p, xyz, dirs, d_rgb, d_sigma, dtype=F64):
     """Gradient of sum(d_rgb * rgb + d_sigma * sigma) of mlp_forward
     (model.py:334-394) w.r.t. every layer: {name: (dW, db)}."""

@@ -282,3 +282,43 @@ def test_get_rays_matches_package(oracle, ng):
     o2, d2 = ng.synthetic.get_rays(8, 10, K, pose)
     np.testing.assert_allclose(d1, d2, rtol=1e-15)
     np.testing.assert_allclose(o1, o2)
+
+
+# --- proposal-gated render ---------------------------------------------------
+def test_gate_fine_hand_case(oracle):
+    # Sc = 2 coarse samples (perm 0, 1), fine draws perm 2, 3; coarse 1 gated off
+    perm = np.array([[0, 2, 1, 3], [1, 0, 3, 2]])
+    m_c = np.array([[True, False], [True, False]])
+    want = np.array([[True, True, False, True], [False, True, True, True]])
+    assert np.array_equal(oracle.gate_fine(perm, m_c), want)
+    assert not oracle.gate_coarse(np.array([np.nan, 0.5, 0.1]), 0.1).tolist()[0]
+    assert oracle.gate_coarse(np.array([np.nan, 0.5, 0.1]), 0.1).tolist() == [False, True, False]
+
+
+def test_gated_render_all_on_is_forward(oracle, ng):
+    """tau < 0 keeps every sample: the gated chain is nerf_forward's fine pass."""
+    p = params(ng)
+    o, d, n, f = ng.synthetic.sphere_rays(6, 8)
+    rng = np.random.default_rng(9)
+    uc, uf = rng.random((6, 64)), rng.random((6, 128))
+    pc, pf = oracle.glorot_params(1, F64), oracle.glorot_params(2, F64)
+    blob = ng.proposal.glorot_blob(4)
+    got, m_c, m_f, w_p = oracle.nerf_render_gated(p, blob, pc, pf, o, d, n, f, uc, uf, -1.0, F64)
+    _, want = oracle.nerf_forward(p, pc, pf, o, d, n, f, uc, uf, F64)
+    assert m_c.all() and m_f.all() and w_p.shape == (6, 64)
+    for k in ("pred_rgb", "pred_depth", "acc_map", "weights"):
+        np.testing.assert_array_equal(got[k], want[k])
+
+
+def test_gated_render_skips_gated_samples(oracle, ng):
+    """Gating every coarse sample off leaves only the fine draws, which the
+    fine sampler then places from a flat PDF (all coarse weights 0)."""
+    p = params(ng)
+    o, d, n, f = ng.synthetic.sphere_rays(4, 10)
+    rng = np.random.default_rng(11)
+    uc, uf = rng.random((4, 64)), rng.random((4, 128))
+    pc, pf = oracle.glorot_params(1, F64), oracle.glorot_params(2, F64)
+    blob = ng.proposal.glorot_blob(4)
+    got, m_c, m_f, _ = oracle.nerf_render_gated(p, blob, pc, pf, o, d, n, f, uc, uf, 10.0, F64)
+    assert not m_c.any() and m_f.sum() == 4 * 128
+    assert np.all(got["weights"][~m_f] == 0)
