@@ -392,10 +392,14 @@ def main():
     if args.train_steps > 0:
         batch = [torch.from_numpy(x[:4096]).to(dev) for x in ng.synthetic.training_rays(500 + rank, 4, 1024)]
         target = plain.render(*batch, seed=3)["rgb"]
-        student = ng.NeRF(params, precision="fp32", seed=60)
-        tms = timed_steps(lambda i: student.train_step((tuple(batch), (target,))), args.train_steps, 1)
-        train = {"rays_per_s": 4096 / (tms / 1000.0), "ms_per_step": tms, "batch_rays": 4096,
-                 "precision": "fp32 (GEMMs and master weights)"}
+        train = {"batch_rays": 4096, "master_weights": "fp32"}
+        for tp in ("bf16", "fp32"):
+            student = ng.NeRF(params, precision=tp, seed=60)
+            tms = timed_steps(lambda i: student.train_step((tuple(batch), (target,))), args.train_steps, 1)
+            student.coarse_model.check_device_errors()
+            train[tp] = {"rays_per_s": 4096 / (tms / 1000.0), "ms_per_step": tms,
+                         "gemms": "BF16 tensor cores (tcgen05 forward, cuBLASLt backward), FP32 accumulation"
+                         if tp == "bf16" else "FP32 SIMT"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

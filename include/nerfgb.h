@@ -322,6 +322,29 @@ int nerfgb_mlp_backward(const void *packed, const float *acts, long long n_rows,
                         const float *d_rgb, const float *d_sigma,
                         float *grad_params, void *workspace, void *stream);
 
+/* ---- BF16 training (tensor cores, FP32 master weights) ------------------ */
+
+/* nerfgb_mlp_forward with the BF16 pack that also writes the BF16 activation
+ * tape: [n_rows][nerfgb_mlp_acts_floats_per_row()] BF16 values (uint16
+ * bits) at the FP32 tape's columns, each the operand the next layer's GEMM
+ * read. err_word: caller-zeroed device int32. */
+int nerfgb_mlp_forward_train_bf16(const void *packed_bf16, const float *xyz,
+                                  const float *dirs, long long n_rows,
+                                  int rows_per_dir, float *rgb, float *sigma,
+                                  void *tape, int *err_word, void *stream);
+
+/* Workspace bytes of nerfgb_mlp_backward_bf16 for n_rows rows. */
+long long nerfgb_mlp_backward_bf16_workspace_bytes(long long n_rows);
+
+/* nerfgb_mlp_backward from a BF16 tape: every dX and dW product is a BF16
+ * GEMM with FP32 accumulation (cuBLASLt), against a BF16 copy of the FP32
+ * master weights in packed_fp32 (the FP32 pack); bias and head gradients
+ * in FP32. grad_params accumulates (zero it first). */
+int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tape,
+                             long long n_rows, const float *d_rgb,
+                             const float *d_sigma, float *grad_params,
+                             void *workspace, void *stream);
+
 /* ---- fused render without allocation --------------------------------- */
 
 /* Size of the built-in scratch array of nerfgb_render_rays_noalloc: 16 MiB,

@@ -1,6 +1,7 @@
 // Launchers shared between the MLP translation units.
 #pragma once
 #include <cuda_runtime.h>
+#include <stdint.h>
 
 namespace nerfgb {
 
@@ -25,6 +26,19 @@ int launch_mlp_fp32_store(const void *packed, const float *xyz, const float *dir
 // BF16 tcgen05 forward (mlp_tc.cu).
 int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,
                     float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm = RowMap());
+
+// BF16 tcgen05 forward that also writes the BF16 activation tape (kActsLd
+// values per row, the FP32 tape's columns) for the BF16 backward (mlp_tc.cu).
+int launch_mlp_bf16_train(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,
+                          float *rgb, float *sigma, uint16_t *tape, int *err_word, cudaStream_t stream);
+
+// Backward of the sigma and rgb heads (mlp_train.cu) from an FP32 or a BF16
+// activation tape: dz9 [n][256] (128 used) = dL/d(dense_9 pre-activation),
+// dsp [n] = dL/d(sigma pre-activation), head gradients into grads.
+int launch_head_bwd(const float *table, const float *tape, long long n, const float *d_rgb, const float *d_sigma,
+                    float *dz9, float *dsp, float *grads, cudaStream_t stream);
+int launch_head_bwd(const float *table, const uint16_t *tape, long long n, const float *d_rgb,
+                    const float *d_sigma, float *dz9, float *dsp, float *grads, cudaStream_t stream);
 
 // FP8-e4m3 tcgen05 forward (mlp_tc.cu).
 int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,

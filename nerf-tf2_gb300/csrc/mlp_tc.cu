@@ -193,6 +193,17 @@ __device__ __forceinline__ uint32_t pack_bf16_relu(float lo, float hi) {
   asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
   return d;
 }
+// 32 BF16 values (16 packed pairs) to 64 contiguous bytes of the activation
+// tape (16-byte aligned).
+__device__ __forceinline__ void tape_store32(uint16_t *dst, const uint32_t (&u)[16]) {
+  uint4 *p = reinterpret_cast<uint4 *>(dst);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) p[q] = make_uint4(u[4 * q], u[4 * q + 1], u[4 * q + 2], u[4 * q + 3]);
+}
+__device__ __forceinline__ void pack32_bf16(const float (&v)[32], uint32_t (&u)[16]) {
+#pragma unroll
+  for (int i = 0; i < 16; ++i) u[i] = pack_bf16(v[2 * i], v[2 * i + 1]);
+}
 
 __device__ __forceinline__ void st_shared_v4(uint32_t addr, uint32_t a, uint32_t b, uint32_t c, uint32_t d) {
   asm volatile("st.shared.v4.b32 [%0], {%1,%2,%3,%4};" ::"r"(addr), "r"(a), "r"(b), "r"(c), "r"(d) : "memory");
@@ -243,8 +254,9 @@ __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile
 // Positional encodings written as BF16 A-operand rows.
 // ---------------------------------------------------------------------------
 // enc_xyz columns [32*HF, 32*HF + 32) of row r (63 values, column 63 = 0).
+// tape_dst (BF16 path only, may be NULL): the same 32 values to the tape.
 template <int HF, bool F8>
-__device__ __forceinline__ void write_enc_xyz(uint32_t enc, int r, const float (&x)[3]) {
+__device__ __forceinline__ void write_enc_xyz(uint32_t enc, int r, const float (&x)[3], uint16_t *tape_dst) {
   float v[32];
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = 0.0f;
@@ -263,12 +275,17 @@ __device__ __forceinline__ void write_enc_xyz(uint32_t enc, int r, const float (
     if (ks >= 32 * HF && ks < 32 * HF + 32) v[ks - 32 * HF] = s;
     if (ks + 1 >= 32 * HF && ks + 1 < 32 * HF + 32) v[ks + 1 - 32 * HF] = co;
   }
+  if (!F8 && tape_dst) {
+    uint32_t u[16];
+    pack32_bf16(v, u);
+    tape_store32(tape_dst, u);
+  }
   store_row32<F8, false>(enc, r, 32 * HF, v);
 }
 
 // enc_dir (27 values, 5 zero pad) into K-elements 0..31 of the enc region.
 template <bool F8>
-__device__ __forceinline__ void write_enc_dir(uint32_t enc, int r, const float (&d)[3]) {
+__device__ __forceinline__ void write_enc_dir(uint32_t enc, int r, const float (&d)[3], uint16_t *tape_dst) {
   float v[32];
 #pragma unroll
   for (int i = 0; i < 32; ++i) v[i] = 0.0f;
@@ -282,6 +299,11 @@ __device__ __forceinline__ void write_enc_dir(uint32_t enc, int r, const float (
     sincosf(fmul(d[c], enc_multiplier(l)), &s, &co);
     v[3 + 2 * p] = s;
     v[4 + 2 * p] = co;
+  }
+  if (!F8 && tape_dst) {
+    uint32_t u[16];
+    pack32_bf16(v, u);
+    tape_store32(tape_dst, u);
   }
   store_row32<F8, false>(enc, r, 0, v);
 }
@@ -454,11 +476,15 @@ __device__ __forceinline__ void issue_tile(uint32_t sbase, uint32_t tmem, RingPo
 // traffic, epilogues exposed).
 // F8: E4M3 operands (kind::f8f6f4, K = 32 per MMA) with per-output-channel
 // weight scales applied in the epilogue; else BF16 (kind::f16, K = 16).
-template <int KCH, int NST, bool PINGPONG, bool TSMEM, bool F8>
+// STORE (BF16 only, training): every layer's BF16 activations (the operands
+// the next layer's MMAs read) and the encodings also go to `tape`, kActsLd
+// BF16 values per row at the columns of the FP32 tape (acts_offset).
+template <int KCH, int NST, bool PINGPONG, bool TSMEM, bool F8, bool STORE>
 __global__ void __launch_bounds__(kThreads, 1)
     mlp_tc_kernel(const uint8_t *__restrict__ packed, const float *__restrict__ xyz,
                     const float *__restrict__ dirs, long long n_max, int rpd, float *__restrict__ rgb_out,
-                    float *__restrict__ sigma_out, int *__restrict__ err, RowMap rm) {
+                    float *__restrict__ sigma_out, int *__restrict__ err, RowMap rm, uint16_t *__restrict__ tape) {
+  static_assert(!(STORE && F8), "the activation tape is BF16");
   using L = Layout<TSMEM, F8>;
   constexpr uint32_t kE = L::kE;           // bytes per operand element
   constexpr uint32_t kRingOff = L::kRingOff, kEncOff = L::kEncOff, kActOff = L::kActOff;
@@ -593,10 +619,11 @@ __global__ void __launch_bounds__(kThreads, 1)
       float x[3];
 #pragma unroll
       for (int c = 0; c < 3; ++c) x[c] = valid ? xyz[prow * 3 + c] : 0.0f;
+      uint16_t *trow_tape = (STORE && valid) ? tape + grow * kActsLd : nullptr;
       if (hf == 0)
-        write_enc_xyz<0, F8>(enc, r, x);
+        write_enc_xyz<0, F8>(enc, r, x, trow_tape ? trow_tape + kActsEncXyz : nullptr);
       else
-        write_enc_xyz<1, F8>(enc, r, x);
+        write_enc_xyz<1, F8>(enc, r, x, trow_tape ? trow_tape + kActsEncXyz + 32 : nullptr);
       fence_proxy_async();
       tc_fence_before();
       mbar_arrive(bar_actr);
@@ -648,6 +675,12 @@ __global__ void __launch_bounds__(kThreads, 1)
               }
             }
             if (g == 9) {
+              if (STORE && trow_tape) {
+                uint32_t u[16];
+#pragma unroll
+                for (int i = 0; i < 16; ++i) u[i] = pack_bf16_relu(v[2 * i], v[2 * i + 1]);
+                tape_store32(trow_tape + acts_offset(9) + col0, u);
+              }
 #pragma unroll
               for (int i = 0; i < 32; i += 4) {
                 // rows col0+i .. col0+i+3 of the [128][3] rgb kernel: 12 floats
@@ -669,6 +702,21 @@ __global__ void __launch_bounds__(kThreads, 1)
                 store_row32<true, false>(act, r, col0, v);
               else
                 store_row32<true, true>(act, r, col0, v);
+            } else if (STORE) {
+              // BF16 operands of the next layer, to shared memory and the tape
+              uint32_t u[16];
+              if (g == 8) {  // dense_8 is linear (model.py:377-378)
+#pragma unroll
+                for (int i = 0; i < 16; ++i) u[i] = pack_bf16(v[2 * i], v[2 * i + 1]);
+              } else {
+#pragma unroll
+                for (int i = 0; i < 16; ++i) u[i] = pack_bf16_relu(v[2 * i], v[2 * i + 1]);
+              }
+#pragma unroll
+              for (int kg = 0; kg < 4; ++kg)
+                st_shared_v4(act + (uint32_t)(col0 / 8 + kg) * 2048u + r * 16, u[4 * kg], u[4 * kg + 1],
+                             u[4 * kg + 2], u[4 * kg + 3]);
+              if (trow_tape) tape_store32(trow_tape + acts_offset(g) + col0, u);
             } else if (g == 8) {  // dense_8 is linear (model.py:377-378)
 #pragma unroll
               for (int kg = 0; kg < 4; ++kg)
@@ -697,7 +745,7 @@ __global__ void __launch_bounds__(kThreads, 1)
           float d[3];
 #pragma unroll
           for (int c = 0; c < 3; ++c) d[c] = dirs[dr * 3 + c];
-          write_enc_dir<F8>(enc, r, d);
+          write_enc_dir<F8>(enc, r, d, trow_tape ? trow_tape + kActsEncDir : nullptr);
         }
         if (g == 9) {
           if (hf == 0 && valid) {
@@ -724,12 +772,13 @@ __global__ void __launch_bounds__(kThreads, 1)
 
 }  // namespace tc
 
-template <int KCH, int NST, bool PP, bool TSMEM, bool F8>
+template <int KCH, int NST, bool PP, bool TSMEM, bool F8, bool STORE = false>
 static int launch_variant(const void *packed, const float *xyz, const float *dirs, long long n, int rpd,
-                          float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm) {
+                          float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm,
+                          uint16_t *tape = nullptr) {
   constexpr uint32_t smem = tc::Layout<TSMEM, F8>::kSmemBytes;
   static_assert(smem <= 227 * 1024, "shared memory");
-  auto kern = tc::mlp_tc_kernel<KCH, NST, PP, TSMEM, F8>;
+  auto kern = tc::mlp_tc_kernel<KCH, NST, PP, TSMEM, F8, STORE>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
     return NERFGB_E_CUDA;
   const long long ntiles = (n + tc::kRows - 1) / tc::kRows;
@@ -737,7 +786,7 @@ static int launch_variant(const void *packed, const float *xyz, const float *dir
   if (sms <= 0) return NERFGB_E_DEVICE;
   const int grid = (int)(ntiles < sms ? ntiles : sms);
   kern<<<grid, tc::kThreads, smem, stream>>>(reinterpret_cast<const uint8_t *>(packed), xyz, dirs, n, rpd, rgb,
-                                             sigma, err_word, rm);
+                                             sigma, err_word, rm, tape);
   return launch_status();
 }
 
@@ -749,6 +798,13 @@ int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, lon
   // ping-pong schedule hides the epilogue behind the other sub-tile's MMAs but
   // streams every weight byte twice, so it wants the deepest ring.
   return launch_variant<64, 2, true, false, false>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream, rm);
+}
+
+int launch_mlp_bf16_train(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
+                          float *sigma, uint16_t *tape, int *err_word, cudaStream_t stream) {
+  // The inference schedule plus the tape stores.
+  return launch_variant<64, 2, true, false, false, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream,
+                                                         RowMap(), tape);
 }
 
 int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,

@@ -23,8 +23,18 @@ constexpr int kDzLd = 256;  // row stride of the dZ buffers
 // ---------------------------------------------------------------------------
 // Heads
 // ---------------------------------------------------------------------------
+// Four tape values as FP32: the FP32 tape, or the BF16 tape of the
+// tensor-core training forward.
+__device__ __forceinline__ float4 tape4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ float4 tape4(const uint16_t *p) {
+  const uint2 u = *reinterpret_cast<const uint2 *>(p);
+  return make_float4(__uint_as_float(u.x << 16), __uint_as_float(u.x & 0xffff0000u), __uint_as_float(u.y << 16),
+                     __uint_as_float(u.y & 0xffff0000u));
+}
+
+template <typename T>
 __global__ void __launch_bounds__(256)
-    head_bwd_kernel(const float *__restrict__ table, const float *__restrict__ acts, long long n,
+    head_bwd_kernel(const float *__restrict__ table, const T *__restrict__ acts, long long n,
                     const float *__restrict__ d_rgb, const float *__restrict__ d_sigma, float *__restrict__ dz9,
                     float *__restrict__ dsp_out, float *__restrict__ grads) {
   extern __shared__ __align__(16) float hsm[];
@@ -43,13 +53,13 @@ __global__ void __launch_bounds__(256)
     for (int e = tid; e < kTM * 32; e += 256) {
       const int r = e >> 5, q = e & 31;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (row0 + r < n) v = *reinterpret_cast<const float4 *>(acts + (row0 + r) * kActsLd + acts_offset(9) + 4 * q);
+      if (row0 + r < n) v = tape4(acts + (row0 + r) * kActsLd + acts_offset(9) + 4 * q);
       *reinterpret_cast<float4 *>(&sH9[r][4 * q]) = v;
     }
     for (int e = tid; e < kTM * 64; e += 256) {
       const int r = e >> 6, q = e & 63;
       float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (row0 + r < n) v = *reinterpret_cast<const float4 *>(acts + (row0 + r) * kActsLd + acts_offset(7) + 4 * q);
+      if (row0 + r < n) v = tape4(acts + (row0 + r) * kActsLd + acts_offset(7) + 4 * q);
       *reinterpret_cast<float4 *>(&sH7[r][4 * q]) = v;
     }
     __syncthreads();
@@ -269,6 +279,31 @@ static int persistent_grid(long long n) {
   return (int)(tiles < cap ? tiles : cap);
 }
 
+}  // namespace train
+
+template <typename T>
+static int launch_head_bwd_t(const float *table, const T *tape, long long n, const float *d_rgb,
+                             const float *d_sigma, float *dz9, float *dsp, float *grads, cudaStream_t st) {
+  using namespace train;
+  if (cudaFuncSetAttribute(head_bwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHeadSmem) !=
+      cudaSuccess)
+    return NERFGB_E_CUDA;
+  head_bwd_kernel<T><<<persistent_grid(n), 256, kHeadSmem, st>>>(table, tape, n, d_rgb, d_sigma, dz9, dsp, grads);
+  return launch_status();
+}
+
+int launch_head_bwd(const float *table, const float *tape, long long n, const float *d_rgb, const float *d_sigma,
+                    float *dz9, float *dsp, float *grads, cudaStream_t st) {
+  return launch_head_bwd_t(table, tape, n, d_rgb, d_sigma, dz9, dsp, grads, st);
+}
+
+int launch_head_bwd(const float *table, const uint16_t *tape, long long n, const float *d_rgb,
+                    const float *d_sigma, float *dz9, float *dsp, float *grads, cudaStream_t st) {
+  return launch_head_bwd_t(table, tape, n, d_rgb, d_sigma, dz9, dsp, grads, st);
+}
+
+namespace train {
+
 static int launch_dw(const float *acts, int in_off, int K, const float *dz, int N, long long n, float *grads,
                      int flat_layer, int k_dst0, bool bias, cudaStream_t st) {
   const int out = flat_out(flat_layer);
@@ -325,12 +360,7 @@ extern "C" int nerfgb_mlp_backward(const void *packed, const float *acts, long l
   float *bufB = bufA + n * kDzLd;
   float *dsp = bufB + n * kDzLd;
   int rc;
-  if (cudaFuncSetAttribute(head_bwd_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHeadSmem) !=
-      cudaSuccess)
-    return NERFGB_E_CUDA;
-  head_bwd_kernel<<<persistent_grid(n), 256, kHeadSmem, st>>>(table, acts, n, d_rgb, d_sigma, bufA, dsp,
-                                                              grad_params);
-  if ((rc = launch_status()) != NERFGB_OK) return rc;
+  if ((rc = launch_head_bwd(table, acts, n, d_rgb, d_sigma, bufA, dsp, grad_params, st)) != NERFGB_OK) return rc;
   // dense_9 (flat 10): input [bottleneck | enc_dir], output 128.
   if ((rc = launch_dw(acts, acts_offset(8), 256, bufA, 128, n, grad_params, 10, 0, true, st)) != NERFGB_OK) return rc;
   if ((rc = launch_dw(acts, kActsEncDir, 27, bufA, 128, n, grad_params, 10, 256, false, st)) != NERFGB_OK) return rc;

@@ -1,0 +1,265 @@
+// BF16 backward of the NeRF MLP (nerf/core/model.py:334-394; the gradient
+// tf.GradientTape takes at model.py:148-170) with FP32 master weights.
+//
+// The forward is the tensor-core BF16 kernel with its tape (mlp_tc.cu,
+// STORE): each layer's BF16 activations are exactly the operands its
+// successor's MMAs read. The backward runs the layers of mlp_train.cu from
+// the heads down, with every product a BF16 GEMM accumulating in FP32:
+//   prep    z = dX (+ dpre_sigma * ws at dense_7) * [h > 0]  (FP32)
+//           dz = bf16(z), db += column sums of z
+//   dW      grads[k][n] += sum_m In[m][k] dz[m][n]   (In = the tape's BF16 input columns)
+//   dX      dX[m][k] = sum_n dz[m][n] W[k][n], k < 256 (W = BF16 copy of the FP32 master weights)
+// The two products are plain GEMMs and go to cuBLASLt; everything around
+// them (heads, masks, bias sums, conversion) is in this library's kernels.
+#include <cublasLt.h>
+#include <cuda_bf16.h>
+
+#include <mutex>
+
+#include "common.cuh"
+#include "mlp_internal.cuh"
+
+namespace nerfgb {
+namespace train16 {
+
+constexpr int kDzLd = 256;                    // row stride of the dZ buffers
+constexpr long long kLtWsBytes = 32ll << 20;  // cuBLASLt workspace
+constexpr int kPrepRows = 1024;               // rows per prep block
+
+static cublasLtHandle_t lt_handle() {
+  static std::mutex mu;
+  static cublasLtHandle_t handles[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
+  std::lock_guard<std::mutex> lock(mu);
+  if (!handles[dev] && cublasLtCreate(&handles[dev]) != CUBLAS_STATUS_SUCCESS) handles[dev] = nullptr;
+  return handles[dev];
+}
+
+// Largest power of two (<= 256) dividing the address.
+static uint32_t align_of(const void *p) {
+  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
+  uint32_t al = 256;
+  while (al > 1 && (a % al) != 0) al >>= 1;
+  return al;
+}
+
+// C (FP32, column-major m x n, ldc) = op(A) op(B) + beta C; A, B BF16
+// column-major with leading dimensions lda, ldb.
+static int gemm(cublasOperation_t ta, cublasOperation_t tb, long long m, long long n, long long k, const void *A,
+                long long lda, const void *B, long long ldb, float beta, float *C, long long ldc, void *ws,
+                cudaStream_t st) {
+  if (m == 0 || n == 0) return NERFGB_OK;
+  cublasLtHandle_t h = lt_handle();
+  if (!h) return NERFGB_E_CUDA;
+  cublasLtMatmulDesc_t op = nullptr;
+  cublasLtMatrixLayout_t la = nullptr, lb = nullptr, lc = nullptr;
+  cublasLtMatmulPreference_t pref = nullptr;
+  int rc = NERFGB_E_CUDA;
+  const float alpha = 1.0f;
+  const uint64_t ws_bytes = (uint64_t)kLtWsBytes;
+  cublasLtMatmulHeuristicResult_t res{};
+  int nres = 0;
+  if (cublasLtMatmulDescCreate(&op, CUBLAS_COMPUTE_32F, CUDA_R_32F) != CUBLAS_STATUS_SUCCESS) goto done;
+  if (cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSA, &ta, sizeof(ta)) != CUBLAS_STATUS_SUCCESS ||
+      cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSB, &tb, sizeof(tb)) != CUBLAS_STATUS_SUCCESS)
+    goto done;
+  if (cublasLtMatrixLayoutCreate(&la, CUDA_R_16BF, ta == CUBLAS_OP_N ? m : k, ta == CUBLAS_OP_N ? k : m, lda) !=
+          CUBLAS_STATUS_SUCCESS ||
+      cublasLtMatrixLayoutCreate(&lb, CUDA_R_16BF, tb == CUBLAS_OP_N ? k : n, tb == CUBLAS_OP_N ? n : k, ldb) !=
+          CUBLAS_STATUS_SUCCESS ||
+      cublasLtMatrixLayoutCreate(&lc, CUDA_R_32F, m, n, ldc) != CUBLAS_STATUS_SUCCESS)
+    goto done;
+  if (cublasLtMatmulPreferenceCreate(&pref) != CUBLAS_STATUS_SUCCESS ||
+      cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &ws_bytes,
+                                           sizeof(ws_bytes)) != CUBLAS_STATUS_SUCCESS)
+    goto done;
+  {
+    // the heuristic assumes 256-byte aligned operands unless told otherwise
+    // (gradient blocks of the flat parameter blob are only 4-byte aligned)
+    const uint32_t al[3] = {align_of(A), align_of(B), align_of(C)};
+    const cublasLtMatmulPreferenceAttributes_t at[4] = {
+        CUBLASLT_MATMUL_PREF_MIN_ALIGNMENT_A_BYTES, CUBLASLT_MATMUL_PREF_MIN_ALIGNMENT_B_BYTES,
+        CUBLASLT_MATMUL_PREF_MIN_ALIGNMENT_C_BYTES, CUBLASLT_MATMUL_PREF_MIN_ALIGNMENT_D_BYTES};
+    for (int i = 0; i < 4; ++i)
+      if (cublasLtMatmulPreferenceSetAttribute(pref, at[i], &al[i < 3 ? i : 2], sizeof(uint32_t)) !=
+          CUBLAS_STATUS_SUCCESS)
+        goto done;
+  }
+  if (cublasLtMatmulAlgoGetHeuristic(h, op, la, lb, lc, lc, pref, 1, &res, &nres) != CUBLAS_STATUS_SUCCESS ||
+      nres < 1)
+    goto done;
+  if (cublasLtMatmul(h, op, &alpha, A, la, B, lb, &beta, C, lc, C, lc, &res.algo, ws, (size_t)ws_bytes, st) ==
+      CUBLAS_STATUS_SUCCESS)
+    rc = NERFGB_OK;
+done:
+  if (pref) cublasLtMatmulPreferenceDestroy(pref);
+  if (lc) cublasLtMatrixLayoutDestroy(lc);
+  if (lb) cublasLtMatrixLayoutDestroy(lb);
+  if (la) cublasLtMatrixLayoutDestroy(la);
+  if (op) cublasLtMatmulDescDestroy(op);
+  return rc;
+}
+
+__global__ void to_bf16_kernel(const float *__restrict__ src, __nv_bfloat16 *__restrict__ dst, long long n) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = __float2bfloat16_rn(src[i]);
+}
+
+// z = raw (+ dsp * ws) (* [tape act > 0]) over N columns; dz = bf16(z);
+// db[n] += sum_m z. One thread per column, kPrepRows rows per block.
+template <bool MASK, bool SIG>
+__global__ void __launch_bounds__(256)
+    prep_kernel(const float *__restrict__ raw, long long M, int N, const uint16_t *__restrict__ tape, int act_off,
+                const float *__restrict__ dsp, const float *__restrict__ ws, __nv_bfloat16 *__restrict__ dz,
+                float *__restrict__ db) {
+  const int c = threadIdx.x;
+  if (c >= N) return;
+  const long long m0 = (long long)blockIdx.x * kPrepRows;
+  const long long m1 = m0 + kPrepRows < M ? m0 + kPrepRows : M;
+  const float w = SIG ? ws[c] : 0.0f;
+  float sum = 0.0f;
+  for (long long m = m0; m < m1; ++m) {
+    float z = raw[m * kDzLd + c];
+    if (SIG) z = fmaf(dsp[m], w, z);
+    if (MASK) {
+      const uint16_t a = tape[m * kActsLd + act_off + c];
+      if (a == 0 || (a & 0x8000u)) z = 0.0f;  // ReLU output <= 0
+    }
+    dz[m * kDzLd + c] = __float2bfloat16_rn(z);
+    sum += z;
+  }
+  atomicAdd(db + c, sum);
+}
+
+struct Ws {
+  float *bufA, *bufB, *dsp;
+  __nv_bfloat16 *dz, *wb;
+  void *lt;
+  long long bytes;
+};
+
+static long long a256(long long b) { return (b + 255) / 256 * 256; }
+
+static Ws carve(void *base, long long n) {
+  Ws w{};
+  long long off = 0;
+  auto take = [&](long long bytes) -> char * {
+    char *p = base ? static_cast<char *>(base) + off : nullptr;
+    off += a256(bytes);
+    return p;
+  };
+  w.bufA = reinterpret_cast<float *>(take(n * kDzLd * 4));
+  w.bufB = reinterpret_cast<float *>(take(n * kDzLd * 4));
+  w.dsp = reinterpret_cast<float *>(take(n * 4));
+  w.dz = reinterpret_cast<__nv_bfloat16 *>(take(n * kDzLd * 2));
+  w.wb = reinterpret_cast<__nv_bfloat16 *>(take(kGemmWElems * 2));
+  w.lt = take(kLtWsBytes);
+  w.bytes = off;
+  return w;
+}
+
+template <bool MASK, bool SIG>
+static int prep(const float *raw, long long M, int N, const uint16_t *tape, int act_off, const float *dsp,
+                const float *ws, __nv_bfloat16 *dz, float *db, cudaStream_t st) {
+  const long long blocks = (M + kPrepRows - 1) / kPrepRows;
+  prep_kernel<MASK, SIG><<<(unsigned)blocks, 256, 0, st>>>(raw, M, N, tape, act_off, dsp, ws, dz, db);
+  return launch_status();
+}
+
+// grads (flat layer fl, rows [k_dst0, k_dst0 + K)) += In^T dz, In = tape
+// columns [in_off, in_off + K).
+static int dW(const uint16_t *tape, int in_off, int K, const __nv_bfloat16 *dz, int N, long long M, float *grads,
+              int fl, int k_dst0, void *lt, cudaStream_t st) {
+  return gemm(CUBLAS_OP_N, CUBLAS_OP_T, N, K, M, dz, kDzLd, tape + in_off, kActsLd, 1.0f,
+              grads + flat_offset(fl) + (long long)k_dst0 * N, N, lt, st);
+}
+
+// out [M][256] = dz [M][N] W_g[0:256][N]^T.
+static int dX(const __nv_bfloat16 *wb, int g, const __nv_bfloat16 *dz, long long M, float *out, void *lt,
+              cudaStream_t st) {
+  const int N = gemm_n(g);
+  return gemm(CUBLAS_OP_T, CUBLAS_OP_N, 256, M, N, wb + gemm_w_offset(g), N, dz, kDzLd, 0.0f, out, kDzLd, lt, st);
+}
+
+static float *bias_grad(float *grads, int fl) { return grads + flat_offset(fl) + (long long)flat_in(fl) * flat_out(fl); }
+
+}  // namespace train16
+}  // namespace nerfgb
+
+using namespace nerfgb;
+
+extern "C" long long nerfgb_mlp_backward_bf16_workspace_bytes(long long n_rows) {
+  if (n_rows < 0) return -1;
+  return train16::carve(nullptr, n_rows).bytes;
+}
+
+extern "C" int nerfgb_mlp_forward_train_bf16(const void *packed_bf16, const float *xyz, const float *dirs,
+                                             long long n_rows, int rows_per_dir, float *rgb, float *sigma,
+                                             void *tape, int *err_word, void *stream) {
+  if (n_rows < 0 || rows_per_dir < 1) return NERFGB_E_INVALID_ARG;
+  if (n_rows == 0) return NERFGB_OK;
+  if (!packed_bf16 || !xyz || !dirs || !rgb || !sigma || !tape || !err_word || !aligned(packed_bf16, 256) ||
+      !aligned(tape, 16))
+    return NERFGB_E_INVALID_ARG;
+  return launch_mlp_bf16_train(packed_bf16, xyz, dirs, n_rows, rows_per_dir, rgb, sigma,
+                               reinterpret_cast<uint16_t *>(tape), err_word, as_stream(stream));
+}
+
+extern "C" int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tape, long long n_rows,
+                                        const float *d_rgb, const float *d_sigma, float *grad_params,
+                                        void *workspace, void *stream) {
+  using namespace train16;
+  if (n_rows < 0) return NERFGB_E_INVALID_ARG;
+  if (n_rows == 0) return NERFGB_OK;
+  if (!packed_fp32 || !tape || !d_rgb || !grad_params || !workspace || !aligned(packed_fp32, 256) ||
+      !aligned(tape, 16) || !aligned(workspace, 256))
+    return NERFGB_E_INVALID_ARG;
+  cudaStream_t st = as_stream(stream);
+  const long long M = n_rows;
+  const float *W = reinterpret_cast<const float *>(packed_fp32);  // FP32 pack: [Kp][N] blocks, then the table
+  const float *table = W + kFp32TableOff;
+  const uint16_t *tp = reinterpret_cast<const uint16_t *>(tape);
+  Ws w = carve(workspace, M);
+  int rc;
+  to_bf16_kernel<<<(unsigned)((kGemmWElems + 255) / 256), 256, 0, st>>>(W, w.wb, kGemmWElems);
+  if ((rc = launch_status()) != NERFGB_OK) return rc;
+  // heads -> dZ9 (masked by [h9 > 0]) and dpre_sigma
+  if ((rc = launch_head_bwd(table, tp, M, d_rgb, d_sigma, w.bufA, w.dsp, grad_params, st)) != NERFGB_OK) return rc;
+  // dense_9 (flat 10): input [bottleneck | enc_dir], 128 outputs
+  if ((rc = prep<false, false>(w.bufA, M, 128, tp, 0, nullptr, nullptr, w.dz, bias_grad(grad_params, 10), st)) !=
+      NERFGB_OK)
+    return rc;
+  if ((rc = dW(tp, acts_offset(8), 256, w.dz, 128, M, grad_params, 10, 0, w.lt, st)) != NERFGB_OK) return rc;
+  if ((rc = dW(tp, kActsEncDir, 27, w.dz, 128, M, grad_params, 10, 256, w.lt, st)) != NERFGB_OK) return rc;
+  if ((rc = dX(w.wb, 9, w.dz, M, w.bufB, w.lt, st)) != NERFGB_OK) return rc;
+  // dense_8 (flat 9): linear, input h7
+  if ((rc = prep<false, false>(w.bufB, M, 256, tp, 0, nullptr, nullptr, w.dz, bias_grad(grad_params, 9), st)) !=
+      NERFGB_OK)
+    return rc;
+  if ((rc = dW(tp, acts_offset(7), 256, w.dz, 256, M, grad_params, 9, 0, w.lt, st)) != NERFGB_OK) return rc;
+  if ((rc = dX(w.wb, 8, w.dz, M, w.bufA, w.lt, st)) != NERFGB_OK) return rc;
+  // dense_7 .. dense_0
+  float *cur = w.bufA, *nxt = w.bufB;
+  for (int l = 7; l >= 0; --l) {
+    float *db = bias_grad(grad_params, l);
+    rc = (l == 7) ? prep<true, true>(cur, M, 256, tp, acts_offset(7), w.dsp, table + kSigmaWOff, w.dz, db, st)
+                  : prep<true, false>(cur, M, 256, tp, acts_offset(l), nullptr, nullptr, w.dz, db, st);
+    if (rc != NERFGB_OK) return rc;
+    if (l == 0) {
+      if ((rc = dW(tp, kActsEncXyz, 63, w.dz, 256, M, grad_params, 0, 0, w.lt, st)) != NERFGB_OK) return rc;
+      break;
+    }
+    if (l == 5) {
+      if ((rc = dW(tp, acts_offset(4), 256, w.dz, 256, M, grad_params, 5, 0, w.lt, st)) != NERFGB_OK) return rc;
+      if ((rc = dW(tp, kActsEncXyz, 63, w.dz, 256, M, grad_params, 5, 256, w.lt, st)) != NERFGB_OK) return rc;
+    } else {
+      if ((rc = dW(tp, acts_offset(l - 1), 256, w.dz, 256, M, grad_params, l, 0, w.lt, st)) != NERFGB_OK) return rc;
+    }
+    if ((rc = dX(w.wb, l, w.dz, M, nxt, w.lt, st)) != NERFGB_OK) return rc;
+    float *t = cur;
+    cur = nxt;
+    nxt = t;
+  }
+  return NERFGB_OK;
+}

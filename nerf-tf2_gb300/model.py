@@ -98,28 +98,42 @@ class NerfMLP:
 
     call = __call__
 
-    def forward_train(self, xyz, dirs, rows_per_dir=1):
-        """FP32 forward that also returns the stored activations for
-        ``backward`` (the tape of tf.GradientTape, model.py:148)."""
+    def forward_train(self, xyz, dirs, rows_per_dir=1, precision="fp32"):
+        """Forward that also returns the stored activations for ``backward``
+        (the tape of tf.GradientTape, model.py:148). "fp32": the FP32 kernel
+        and an FP32 tape; "bf16": the tensor-core kernel and a BF16 tape
+        (int16 tensor of BF16 bits) holding the operands its GEMMs read."""
+        if precision not in ("fp32", "bf16"):
+            raise ValueError(f"training forward precision must be fp32 or bf16, not {precision!r}")
         xyz = as_cuda(xyz, name="xyz")
         n = xyz.shape[0]
         dirs = as_cuda(dirs, shape=((n + rows_per_dir - 1) // rows_per_dir, 3), name="dir")
         rgb, sigma = empty(n, 3), empty(n, 1)
-        acts = empty(n, int(_lib.lib().nerfgb_mlp_acts_floats_per_row()))
-        _lib.call("nerfgb_mlp_forward_train", ptr(self.packed("fp32")), ptr(xyz), ptr(dirs), n,
-                  int(rows_per_dir), ptr(rgb), ptr(sigma), ptr(acts), stream())
+        ld = int(_lib.lib().nerfgb_mlp_acts_floats_per_row())
+        if precision == "bf16":
+            acts = torch.empty(n, ld, dtype=torch.int16, device=xyz.device)
+            _lib.call("nerfgb_mlp_forward_train_bf16", ptr(self.packed("bf16")), ptr(xyz), ptr(dirs), n,
+                      int(rows_per_dir), ptr(rgb), ptr(sigma), ptr(acts), ptr(self.err_word), stream())
+        else:
+            acts = empty(n, ld)
+            _lib.call("nerfgb_mlp_forward_train", ptr(self.packed("fp32")), ptr(xyz), ptr(dirs), n,
+                      int(rows_per_dir), ptr(rgb), ptr(sigma), ptr(acts), stream())
         return rgb, sigma, acts
 
     def backward(self, acts, d_rgb, d_sigma, grad_params):
         """Accumulates the parameter gradient of sum(d_rgb*rgb + d_sigma*sigma)
-        into grad_params (flat Keras layout)."""
+        into grad_params (flat Keras layout). An FP32 tape takes the FP32
+        backward; a BF16 tape (from ``forward_train(precision="bf16")``) the
+        BF16 one (BF16 GEMMs, FP32 accumulation, FP32 gradients)."""
         n = acts.shape[0]
         d_rgb = as_cuda(d_rgb, shape=(n, 3), name="d_rgb")
         d_sigma = as_cuda(d_sigma, shape=(n,), name="d_sigma")
-        ws = torch.empty(int(_lib.lib().nerfgb_mlp_backward_workspace_bytes(n)), dtype=torch.uint8,
-                         device=acts.device)
-        _lib.call("nerfgb_mlp_backward", ptr(self.packed("fp32")), ptr(acts), n, ptr(d_rgb), ptr(d_sigma),
-                  ptr(grad_params), ptr(ws), stream())
+        lib = _lib.lib()
+        bf16 = acts.dtype == torch.int16
+        nbytes = (lib.nerfgb_mlp_backward_bf16_workspace_bytes if bf16 else lib.nerfgb_mlp_backward_workspace_bytes)(n)
+        ws = torch.empty(int(nbytes), dtype=torch.uint8, device=acts.device)
+        _lib.call("nerfgb_mlp_backward_bf16" if bf16 else "nerfgb_mlp_backward", ptr(self.packed("fp32")),
+                  ptr(acts), n, ptr(d_rgb), ptr(d_sigma), ptr(grad_params), ptr(ws), stream())
         return grad_params
 
     def check_device_errors(self):
@@ -184,13 +198,17 @@ class NeRF:
             self._opt = {"step": 0, "m": [z(), z()], "v": [z(), z()], "g": [z(), z()]}
         return self._opt
 
-    def train_step(self, data, *, u_coarse=None, u_fine=None, lr=None):
-        """One step of NeRF.train_step (model.py:127-180): forward (FP32, with
-        the activation tape), loss = MSE(coarse) + MSE(fine) (:157-168),
-        gradients by the hand-written backward (compositing, then the MLP),
-        and a Keras Adam step with ExponentialDecay(5e-4, 500000, 0.1)
-        (:413-418). ``data`` = ((rays_o, rays_d, near, far), (rgb,)).
+    def train_step(self, data, *, u_coarse=None, u_fine=None, lr=None, precision=None):
+        """One step of NeRF.train_step (model.py:127-180): forward with the
+        activation tape, loss = MSE(coarse) + MSE(fine) (:157-168), gradients
+        by the hand-written backward (compositing, then the MLP), and a Keras
+        Adam step with ExponentialDecay(5e-4, 500000, 0.1) (:413-418) on the
+        FP32 master weights. ``precision``: "fp32" (FP32 GEMMs) or "bf16"
+        (BF16 tensor-core GEMMs forward and backward, FP32 accumulation);
+        default: "bf16" for a BF16 or FP8 model, else "fp32".
+        ``data`` = ((rays_o, rays_d, near, far), (rgb,)).
         Returns {"loss", "coarse_loss", "fine_loss", "psnr"} as floats."""
+        tp = precision or ("fp32" if self.precision == "fp32" else "bf16")
         (rays_o, rays_d, near, far), (rgb,) = data
         p = self.params
         rays_o = as_cuda(rays_o, name="rays_o")
@@ -202,13 +220,15 @@ class NeRF:
         d_cm = ray_utils.create_input_batch_coarse_model(p, rays_o, rays_d, near, far, u_vals=u_coarse)
         t_c = d_cm["t_vals"]
         Sc = t_c.shape[1]
-        rgb_c, sig_c, acts_c = self.coarse_model.forward_train(d_cm["xyz_inputs"], rays_d, rows_per_dir=Sc)
+        rgb_c, sig_c, acts_c = self.coarse_model.forward_train(d_cm["xyz_inputs"], rays_d, rows_per_dir=Sc,
+                                                               precision=tp)
         pp_c = ray_utils.post_process_model_output(rgb_c, sig_c, t_c, self.white_bg, trans_mode=self.trans_mode)
         d_fm = ray_utils.create_input_batch_fine_model(p, rays_o, rays_d, pp_c["weights"], d_cm["bin_data"],
                                                        t_c, u_vals=u_fine)
         t_f = d_fm["t_vals"]
         S = t_f.shape[1]
-        rgb_f, sig_f, acts_f = self.fine_model.forward_train(d_fm["xyz_inputs"], rays_d, rows_per_dir=S)
+        rgb_f, sig_f, acts_f = self.fine_model.forward_train(d_fm["xyz_inputs"], rays_d, rows_per_dir=S,
+                                                             precision=tp)
         pp_f = ray_utils.post_process_model_output(rgb_f, sig_f, t_f, self.white_bg, trans_mode=self.trans_mode)
         loss = torch.zeros(3, device=rays_o.device)
         grads_map = []

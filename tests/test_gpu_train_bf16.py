@@ -1,0 +1,92 @@
+"""BF16 training (tensor-core GEMMs, FP32 master weights): the tape of the
+BF16 forward and the BF16 backward against the oracle's float64 chain on the
+same tape (the gradient tf.GradientTape takes at nerf/core/model.py:148-170)."""
+import numpy as np
+import pytest
+import torch
+
+from test_gpu_backward import biased_blob, compare, dev, flat_grads, host
+
+pytestmark = pytest.mark.gpu
+F32, F64 = np.float32, np.float64
+
+
+def tape64(acts):
+    """The BF16 tape (int16 bits) as float64."""
+    assert acts.dtype == torch.int16
+    return acts.view(torch.bfloat16).float().cpu().numpy().astype(F64)
+
+
+@pytest.mark.parametrize("n", [300, 2048])
+def test_mlp_backward_bf16_vs_oracle(ng, oracle, cuda, n):
+    blob = biased_blob(ng, 3)
+    rng = np.random.default_rng(n)
+    x = rng.uniform(-3, 3, (n, 3)).astype(F32)
+    d = rng.normal(size=(n, 3))
+    d = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(F32)
+    dr = rng.normal(size=(n, 3)).astype(F32)
+    ds = rng.normal(size=(n,)).astype(F32)
+    mlp = ng.get_coarse_or_fine_model("fine", params=blob, precision="bf16")
+    X, D = dev(x), dev(d)
+    rgb, sig, acts = mlp.forward_train(X, D, precision="bf16")
+    r2, s2 = mlp((X, D))
+    mlp.check_device_errors()
+    assert torch.equal(rgb, r2) and torch.equal(sig, s2)  # the tape does not change the forward
+    # the tape: BF16 activations within BF16 rounding of the fp32 oracle's
+    # (relative L2 per activation, 8 layers of 8-bit-mantissa operands)
+    _, _, a32 = oracle.mlp_forward(oracle.unpack_params(blob, F32), x, d, F32, cache=True)
+    tape = oracle.acts_from_tape(tape64(acts))
+    for k in ("enc_xyz", "h0", "h4", "h7", "bott", "enc_dir", "h9"):
+        err = np.linalg.norm(tape[k] - a32[k]) / np.linalg.norm(a32[k])
+        assert err < 2e-2, (k, err)
+    g = torch.zeros(ng.weights.PARAM_COUNT, device="cuda")
+    mlp.backward(acts, dev(dr), dev(ds), g)
+    # float64 chain on the same tape (same ReLU masks); the GPU rounds dZ and
+    # W to BF16 for every product (8-bit mantissa, ~10 layers deep)
+    want = flat_grads(ng, oracle.mlp_backward_cached(oracle.unpack_params(blob, F64), tape, dr.astype(F64),
+                                                     ds.astype(F64)))
+    compare(ng, host(g), want, rel=3e-2, norm=True)
+    # and distinctly closer than zero / a scaled copy would be: the heads are FP32
+    for name in ("rgb", "sigma"):
+        ko, bo, i, o = ng.weights.offsets()[name]
+        w = want[ko:ko + i * o]
+        assert np.linalg.norm(host(g)[ko:ko + i * o] - w) / np.linalg.norm(w) < 1e-4, name
+
+
+def test_train_step_bf16_gradients_vs_oracle(ng, oracle, cuda):
+    R = 48
+    o, d, n, f = ng.synthetic.sphere_rays(R, 5)
+    rng = np.random.default_rng(6)
+    uc = rng.random((R, 64), dtype=F32)
+    uf = rng.random((R, 128), dtype=F32)
+    target = rng.random((R, 3), dtype=F32)
+    bc, bf = biased_blob(ng, 11), biased_blob(ng, 12)
+    p = ng.make_params()
+    nerf = ng.NeRF(p, precision="bf16", coarse_params=bc, fine_params=bf, trans_mode=ng._lib.TRANS_CUMPROD)
+    out = nerf.train_step(((dev(o), dev(d), dev(n), dev(f)), (dev(target),)), u_coarse=dev(uc),
+                          u_fine=dev(uf), lr=0.0)
+    nerf.coarse_model.check_device_errors()
+    assert np.isfinite(out["loss"])
+    gc, gf = (host(g) for g in nerf.gradients())
+    tape = nerf._train_state()["tape"]
+    for key, blob, got in (("coarse", bc, gc), ("fine", bf, gf)):
+        t, sig, rgb_s, acts, pred = tape[key]
+        t, sig, rgb_s, pred = (host(x).astype(F64) for x in (t, sig, rgb_s, pred))
+        _, G = oracle.mse(target.astype(F64), pred)
+        dsig, drgb = oracle.composite_backward(sig.reshape(-1), t, rgb_s, G)
+        want = flat_grads(ng, oracle.mlp_backward_cached(oracle.unpack_params(blob, F64),
+                                                         oracle.acts_from_tape(tape64(acts)), drgb, dsig))
+        compare(ng, got, want, rel=3e-2, norm=True)
+
+
+def test_train_bf16_reduces_loss(ng, cuda):
+    """Twenty BF16 steps on one batch lower the loss (Keras Adam, lr 5e-4)."""
+    R = 1024
+    rays = [dev(x) for x in ng.synthetic.sphere_rays(R, 9)]
+    teacher = ng.NeRF(ng.make_params(), precision="fp32", seed=1)
+    target = teacher.render(*rays, seed=3)["rgb"]
+    student = ng.NeRF(ng.make_params(), precision="bf16", seed=2)
+    losses = [student.train_step((tuple(rays), (target,)))["loss"] for _ in range(20)]
+    student.coarse_model.check_device_errors()
+    assert all(np.isfinite(losses))
+    assert losses[-1] < 0.8 * losses[0], losses
