@@ -403,14 +403,17 @@ __device__ __forceinline__ void issue_gemm(uint32_t sbase, uint32_t tmem, RingPo
   constexpr uint32_t idesc = F8 ? idesc_e4m3(128, N) : idesc_bf16(128, N);
   static_assert(256 % KCH == 0, "chunks must not straddle the activation/encoding split");
   const uint32_t bar_full = sbase + L::kBarFull, bar_empty = sbase + L::kBarEmpty;
-  const uint32_t ring_lo = ((sbase + L::kRingOff) >> 4) | ((uint32_t)N << 16);
+  // Descriptor start addresses are 18-bit shared-window offsets (a CTA's
+  // window address may carry bits above them, as in a cluster launch).
+  const uint32_t sw = sbase & 0x3FFFFu;
+  const uint32_t ring_lo = ((sw + L::kRingOff) >> 4) | ((uint32_t)N << 16);
   constexpr uint32_t kALbo = (2048u >> 4) << 16;
   if constexpr (KA > 0) {
-    const uint32_t act_lo = ((sbase + L::kActOff) >> 4) | kALbo;
+    const uint32_t act_lo = ((sw + L::kActOff) >> 4) | kALbo;
     issue_run<KA / KCH, KCH, N, F8, NST, kStageBytes, S_LO, S_HI, true>(
         bar_full, bar_empty, ring_lo, act_lo, act_lo + (L::kActBytes >> 4), tmem, idesc, rp, abort_flag, err);
   }
-  const uint32_t enc_lo = ((sbase + L::kEncOff) >> 4) | kALbo;
+  const uint32_t enc_lo = ((sw + L::kEncOff) >> 4) | kALbo;
   if constexpr (KE / KCH > 0)
     issue_run<KE / KCH, KCH, N, F8, NST, kStageBytes, S_LO, S_HI, KA == 0>(
         bar_full, bar_empty, ring_lo, enc_lo, enc_lo + (L::kEncBytes >> 4), tmem, idesc, rp, abort_flag, err);
