@@ -236,11 +236,11 @@ __global__ void __launch_bounds__(32 * kFineWarps)
                        const float *__restrict__ t_coarse, const float *__restrict__ u, int R, int Sc,
                        int Sf, float *__restrict__ xyz, float *__restrict__ dirs,
                        float *__restrict__ t_out, int *__restrict__ piece_idxs,
-                       int *__restrict__ sort_perm) {
+                       int *__restrict__ sort_perm, int P) {
   extern __shared__ float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = Sc + Sf;
-  const int per_warp = 4 * Sc + (Sc + 1) + 2 * S;
+  const int per_warp = 4 * Sc + (Sc + 1) + 2 * S + 2 * P;
   float *s_w = smem + warp * per_warp;  // w + 1e-5, then pdf * width
   float *s_pdf = s_w + Sc;
   float *s_left = s_pdf + Sc;
@@ -248,6 +248,8 @@ __global__ void __launch_bounds__(32 * kFineWarps)
   float *s_agg = s_wid + Sc;      // Sc + 1
   float *s_t = s_agg + Sc + 1;    // concat(t_c, t_f), S
   float *s_srt = s_t + S;         // sorted, S
+  float *s_fk = s_srt + S;        // fast path: fine keys (P, a power of two >= Sf) ...
+  int *s_fi = reinterpret_cast<int *>(s_fk + P);  // ... and their fine indices
   for (int r = blockIdx.x * kFineWarps + warp; r < R; r += gridDim.x * kFineWarps) {
     const long long rb = (long long)r * Sc;
     for (int j = lane; j < Sc; j += 32) {
@@ -301,15 +303,82 @@ __global__ void __launch_bounds__(32 * kFineWarps)
       if (piece_idxs) piece_idxs[ub + k] = first;
     }
     __syncwarp();
-    // Rank sort of concat(t_c, t_f) (:380-385): rank = number of elements
-    // that precede e in the stable order.
+    // Stable sort of concat(t_c, t_f) (:380-385).
     const long long sb = (long long)r * S;
-    for (int e = lane; e < S; e += 32) {
-      float v = s_t[e];
-      int rank = 0;
-      for (int q = 0; q < S; ++q) rank += sort_before(s_t[q], q, v, e) ? 1 : 0;
-      s_srt[rank] = v;
-      if (sort_perm) sort_perm[sb + rank] = e;
+    bool fast = false;
+    if (P > 0) {
+      // t_c non-decreasing and no NaN anywhere: the stable order is t_c in
+      // place merged with the sorted fine draws, a t_c element first on a tie.
+      bool ok = true;
+      for (int j = lane; j < Sc; j += 32) ok = ok && !isnan(s_t[j]) && (j + 1 >= Sc || s_t[j] <= s_t[j + 1]);
+      for (int k = lane; k < Sf; k += 32) ok = ok && !isnan(s_t[Sc + k]);
+      fast = __all_sync(0xffffffffu, ok);
+    }
+    if (fast) {
+      // Bitonic sort of (t_f[k], k), padded to P with (+inf, k >= Sf).
+      for (int k = lane; k < P; k += 32) {
+        s_fk[k] = k < Sf ? s_t[Sc + k] : INFINITY;
+        s_fi[k] = k;
+      }
+      __syncwarp();
+      for (int size = 2; size <= P; size <<= 1) {
+        for (int stride = size >> 1; stride > 0; stride >>= 1) {
+          for (int q = lane; q < P / 2; q += 32) {
+            const int lo = 2 * stride * (q / stride) + (q % stride), hi = lo + stride;
+            const float a = s_fk[lo], b = s_fk[hi];
+            const int ia = s_fi[lo], ib = s_fi[hi];
+            const bool b_first = b < a || (b == a && ib < ia);
+            if (b_first == ((lo & size) == 0)) {  // ascending block: b first -> swap; descending: a first -> swap
+              s_fk[lo] = b;
+              s_fk[hi] = a;
+              s_fi[lo] = ib;
+              s_fi[hi] = ia;
+            }
+          }
+          __syncwarp();
+        }
+      }
+      // t_c[i] lands after the fine draws strictly below it; the j-th
+      // sorted draw after the coarse samples at or below it.
+      for (int i = lane; i < Sc; i += 32) {
+        const float v = s_t[i];
+        int first = 0, count = Sf;  // lower_bound over s_fk[0, Sf)
+        while (count > 0) {
+          const int step = count >> 1, it = first + step;
+          if (s_fk[it] < v) {
+            first = it + 1;
+            count -= step + 1;
+          } else {
+            count = step;
+          }
+        }
+        s_srt[i + first] = v;
+        if (sort_perm) sort_perm[sb + i + first] = i;
+      }
+      for (int j = lane; j < Sf; j += 32) {
+        const float v = s_fk[j];
+        int first = 0, count = Sc;  // upper_bound over t_c
+        while (count > 0) {
+          const int step = count >> 1, it = first + step;
+          if (!(v < s_t[it])) {
+            first = it + 1;
+            count -= step + 1;
+          } else {
+            count = step;
+          }
+        }
+        s_srt[j + first] = v;
+        if (sort_perm) sort_perm[sb + j + first] = Sc + s_fi[j];
+      }
+    } else {
+      // Rank sort: rank = number of elements that precede e in the stable order.
+      for (int e = lane; e < S; e += 32) {
+        float v = s_t[e];
+        int rank = 0;
+        for (int q = 0; q < S; ++q) rank += sort_before(s_t[q], q, v, e) ? 1 : 0;
+        s_srt[rank] = v;
+        if (sort_perm) sort_perm[sb + rank] = e;
+      }
     }
     __syncwarp();
     float o0 = rays_o[3 * r], o1 = rays_o[3 * r + 1], o2 = rays_o[3 * r + 2];
@@ -444,7 +513,13 @@ extern "C" int nerfgb_fine_sample(const float *rays_o, const float *rays_d, cons
       !u_vals || !xyz || !t_vals)
     return NERFGB_E_INVALID_ARG;
   int S = n_coarse + n_fine;
-  size_t smem = (size_t)kFineWarps * (4 * n_coarse + (n_coarse + 1) + 2 * S) * sizeof(float);
+  // Fast stable sort for up to 512 fine draws: keys padded to a power of two.
+  int P = 0;
+  if (n_fine <= 512) {
+    P = 32;
+    while (P < n_fine) P <<= 1;
+  }
+  size_t smem = (size_t)kFineWarps * (4 * n_coarse + (n_coarse + 1) + 2 * S + 2 * P) * sizeof(float);
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(fine_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess)
@@ -454,7 +529,7 @@ extern "C" int nerfgb_fine_sample(const float *rays_o, const float *rays_d, cons
   int cap = (sms > 0 ? sms : 148) * 16;
   fine_sample_kernel<<<blocks < cap ? blocks : cap, 32 * kFineWarps, smem, as_stream(stream)>>>(
       rays_o, rays_d, bin_weights, left_edges, ld_left, bin_widths, t_vals_coarse, u_vals, n_rays,
-      n_coarse, n_fine, xyz, dirs, t_vals, piece_idxs, sort_perm);
+      n_coarse, n_fine, xyz, dirs, t_vals, piece_idxs, sort_perm, P);
   return launch_status();
 }
 

@@ -95,6 +95,33 @@ def test_fine_sampler_bit_exact(ng, oracle, cuda, Sf):
     assert np.array_equal(host(got["dir_inputs"]), want["dir_inputs"])
 
 
+@pytest.mark.parametrize("Sf", [128, 33, 256, 512])
+def test_fine_sampler_sort_paths(ng, oracle, cuda, Sf):
+    """The stable sort of concat(t_c, t_f) (ray_utils.py:380-385) on its fast
+    path (non-decreasing t_c, no NaN: bitonic sort of the fine draws, then a
+    merge) and its fallback (rank sort), bit-exact: ties between coarse and
+    fine depths, ties among fine draws, unsorted coarse depths, NaN."""
+    R = 200
+    p, o, d, n, f, cm, w, rng = _fine_inputs(ng, oracle, R, 11)
+    p.sampling.N_fine = Sf
+    u = rng.random((R, Sf), dtype=F32)
+    u[:, 1] = 0.0                       # t_f = near ...
+    u[:, 2] = u[:, 3] = u[:, 4]         # fine ties
+    t_c = cm["t_vals"].copy()
+    t_c[20:40, 0] = cm["bin_data"]["bin_edges"][20:40, 0]   # ... = t_c[0]: coarse/fine ties
+    t_c[40:50, 5] = t_c[40:50, 6]                           # coarse ties
+    t_c[0:10] = t_c[0:10, ::-1]                             # unsorted: rank-sort fallback
+    t_c[10:15, 7] = np.nan                                  # NaN: fallback, NaN last
+    u[15:18, 9] = np.nan
+    want = oracle.create_input_batch_fine_model(p, o, d, w, cm["bin_data"], t_c, u, return_indices=True)
+    got = ng.create_input_batch_fine_model(p, dev(o), dev(d), dev(w),
+                                           {k: dev(v) for k, v in cm["bin_data"].items()},
+                                           dev(t_c), u_vals=dev(u), return_indices=True)
+    assert np.array_equal(host(got["sort_perm"]), want["sort_perm"])
+    np.testing.assert_array_equal(host(got["t_vals"]), want["t_vals"])
+    np.testing.assert_array_equal(host(got["xyz_inputs"]), want["xyz_inputs"])
+
+
 def test_fine_sampler_pdf_mask(ng, oracle, cuda):
     """pdf < 1e-8 (ray_utils.py:372-373): zero weights over huge bins."""
     R = 40
