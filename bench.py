@@ -96,6 +96,27 @@ def dist_env():
             int(os.environ.get("WORLD_SIZE", 1)))
 
 
+def rank_frame_seed(rank):
+    """Weak scaling: rank r renders its own frame, from camera seed r (rays
+    are independent; no data-path collective)."""
+    return rank
+
+
+def max_over_ranks(total_ms, world, device):
+    """The slowest rank's summed step time (all_reduce MAX; identity at 1)."""
+    import torch
+    import torch.distributed as tdist
+    t = torch.tensor([float(total_ms)], device=device, dtype=torch.float64)
+    if world > 1:
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, units_per_rank, ms_per_step):
+    """Units per second over all ranks: every rank's units / the slowest rank's step time."""
+    return world * units_per_rank / (ms_per_step / 1000.0)
+
+
 # ---------------------------------------------------------------------------
 # CPU side: the oracle restatement of the reference algorithm
 # ---------------------------------------------------------------------------
@@ -219,7 +240,7 @@ def main():
     fast = ng.NeRF(params, precision=args.path, coarse_params=blob, fine_params=blob)
     plain = ng.NeRF(params, precision="fp32", coarse_params=blob, fine_params=blob)
     # weak scaling: every rank renders its own frame (camera seed = rank)
-    frame = ng.synthetic.frame_rays(rank, H, W, FOCAL)
+    frame = ng.synthetic.frame_rays(rank_frame_seed(rank), H, W, FOCAL)
     R = frame[0].shape[0]
     host = [torch.from_numpy(x).pin_memory() for x in frame]
     rays = [h.to(dev) for h in host]
@@ -267,10 +288,7 @@ def main():
             e1.record()
             torch.cuda.synchronize()
             times.append(e0.elapsed_time(e1))
-        t = torch.tensor([sum(times)], device=dev, dtype=torch.float64)
-        if world > 1:
-            tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        return float(t.item()) / steps
+        return max_over_ranks(sum(times), world, dev) / steps
 
     # headline: device-resident frame through the fast path
     def step(i):
@@ -278,7 +296,7 @@ def main():
     bus = getattr(torch.cuda.get_device_properties(dev), "pci_bus_id", None)
     with ClockSampler(str(bus) if bus is not None else None) as clk:
         ms = timed_steps(step, args.steps, args.warmup)
-    value = world * R / (ms / 1000.0)
+    value = whole_job_rate(world, R, ms)
 
     # end to end: pinned host rays in, maps out, through the public API
     out_host = {k: torch.empty((R, 3) if k == "rgb" else (R,), pin_memory=True) for k in ("rgb", "depth", "acc")}
