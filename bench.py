@@ -41,6 +41,9 @@ FLOP_PER_SAMPLE = 1186816          # 2 x 593,408 MAC of the 8x256 MLP + heads
 L2_FLUSH_BYTES = 512 << 20         # > 129 MB L2
 SCENE_SEED = 21
 SCENE_MAX_FREQ_LOG2 = 6  # scene band-limited to the proposal's encoding (L=6)
+WORKLOAD = ("800x800 pinhole frame (focal 1111.111) from a random camera on the radius-4 sphere, "
+            "4096-ray chunks, 64 stratified + 128 fine samples; scene = one random-init 8x256 network "
+            "(sigma head x4, bias -0.5, xyz encoding cut above 2^5 pi) as coarse and fine")
 
 
 def parse():
@@ -121,13 +124,13 @@ def whole_job_rate(world, units_per_rank, ms_per_step):
 # CPU side: the oracle restatement of the reference algorithm
 # ---------------------------------------------------------------------------
 def cpu_render_rate(ng, frame, seconds, max_rays=4096, block=128):
-    """Times the oracle's FP32 hierarchical render on consecutive 128-ray
-    blocks of the frame until `seconds` elapse. Returns (rays/s, rays)."""
+    """Times the oracle's FP32 hierarchical render of the benchmark scene on
+    consecutive 128-ray blocks of the frame until `seconds` elapse. Returns
+    (rays/s, rays)."""
     oracle = importlib.import_module("oracle")
     o, d, n, f = frame
     p = ng.make_params()
-    pc = oracle.unpack_params(ng.weights.glorot_blob(0))
-    pf = oracle.unpack_params(ng.weights.glorot_blob(1))
+    pc = pf = oracle.unpack_params(ng.synthetic.sparse_scene_blob(SCENE_SEED, max_freq_log2=SCENE_MAX_FREQ_LOG2))
     rng = np.random.default_rng(0)
     done, t0 = 0, time.perf_counter()
     while done < max_rays and (time.perf_counter() - t0) < seconds:
@@ -156,8 +159,8 @@ def reference_arm(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * per_step / rate,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "fp32",
         "data": "synthetic",
-        "config": {"workload": "800x800 frame, 4096-ray chunks, 64 coarse + 128 fine, random-init "
-                               "8x256 MLPs", "sample_rays_per_step": per_step},
+        "config": {"workload": WORKLOAD, "sample_rays_per_step": per_step,
+                   "path": "plain FP32 hierarchical (the reference's algorithm)"},
         "cpu_baseline": {"value": rate, "unit": "rays/s", "cores": cores, "kind": "port",
                          "sample": f"{per_step} rays of the frame per step; numpy FP32 restatement "
                                    "(TensorFlow 2.6 is not installable here), OpenBLAS on all cores"},
@@ -434,11 +437,7 @@ def main():
             "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": args.path, "data": "synthetic",
-            "config": {"workload": "800x800 pinhole frame (focal 1111.111) from a random camera on "
-                                   "the radius-4 sphere, 4096-ray chunks, 64 stratified + 128 fine "
-                                   "samples; scene = one random-init 8x256 network (sigma head x4, "
-                                   "bias -0.5, xyz encoding cut above 2^5 pi) as coarse and fine; "
-                                   "proposal 2x64 (L=6) trained on 200k rays from 100 cameras",
+            "config": {"workload": WORKLOAD + "; proposal 2x64 (L=6) trained on 200k rays from 100 cameras",
                        "rays_per_step_per_gpu": R, "path": path,
                        "l2": "512 MB buffer written between timed steps"},
             "plain_fp32": {"value": world * R / (plain_ms / 1000.0), "unit": "rays/s",
