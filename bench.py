@@ -56,7 +56,7 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel", default=None, choices=["mlp"],
+    ap.add_argument("--kernel", default=None, choices=["mlp", "train"],
                     help="run only the MLP kernel at the fine-pass launch shape (for ncu)")
     ap.add_argument("--rows", type=int, default=CHUNK * (SC + SF))
     ap.add_argument("--proposal", type=int, default=1, help="1: BF16 + learned proposal (headline)")
@@ -92,6 +92,33 @@ def kernel_only(args):
     ms = statistics.median(ts)
     print(json.dumps({"kernel": f"mlp_{args.path}", "rows": args.rows, "launch_ms": ms,
                       "tflops": args.rows * FLOP_PER_SAMPLE / ms / 1e9}), flush=True)
+
+
+def train_only(args):
+    """`--steps` training steps (4096 rays of the benchmark scene, precision
+    `--path`) after `--warmup` untimed ones. Prints the median step time."""
+    import torch
+    ng = importlib.import_module("nerf-tf2_gb300")
+    dev = torch.device("cuda", 0)
+    params = ng.make_params(N_coarse=SC, N_fine=SF)
+    blob = ng.synthetic.sparse_scene_blob(SCENE_SEED, max_freq_log2=SCENE_MAX_FREQ_LOG2)
+    teacher = ng.NeRF(params, precision="fp32", coarse_params=blob, fine_params=blob)
+    batch = [torch.from_numpy(x[:4096]).to(dev) for x in ng.synthetic.training_rays(500, 4, 1024)]
+    target = teacher.render(*batch, seed=3)["rgb"]
+    student = ng.NeRF(params, precision=args.path, seed=60)
+    for _ in range(args.warmup):
+        student.train_step((tuple(batch), (target,)))
+    ts = []
+    for _ in range(args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        student.train_step((tuple(batch), (target,)))
+        e1.record()
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    student.coarse_model.check_device_errors()
+    print(json.dumps({"kernel": f"train_{args.path}", "batch_rays": 4096, "step_ms": statistics.median(ts)}),
+          flush=True)
 
 
 def dist_env():
@@ -223,6 +250,8 @@ def main():
         return reference_arm(args)
     if args.kernel == "mlp":
         return kernel_only(args)
+    if args.kernel == "train":
+        return train_only(args)
     import torch
     import torch.distributed as tdist
 
@@ -344,6 +373,16 @@ def main():
                "psnr_fast_vs_plain_db": ng.psnr(img_plain["rgb"], img_fast["rgb"]),
                "depth_mae_fast_vs_plain": float((img_plain["depth"] - img_fast["depth"]).abs().mean()),
                "mean_acc": float(img_plain["acc"].mean())}
+    if proposal is not None and args.path == "bf16":
+        # the same gated path with FP8-e4m3 MLP GEMMs (per-channel scales), for reference
+        fp8 = ng.NeRF(params, precision="fp8", coarse_params=blob, fine_params=blob)
+        fp8_ms = timed_steps(lambda i: fp8.render(*rays, chunk=CHUNK, seed=1000 * i, **prop_kw), args.plain_steps, 1)
+        img_fp8 = fp8.render(*sr, chunk=CHUNK, seed=7, **prop_kw)
+        fp8.coarse_model.check_device_errors()
+        quality["fp8_" + args.proposal_mode] = {
+            "rays_per_s": whole_job_rate(world, R, fp8_ms), "psnr_db": ng.psnr(gt, img_fp8["rgb"]),
+            "psnr_gap_db": psnr_plain - ng.psnr(gt, img_fp8["rgb"]),
+            "gate_met": bool(psnr_plain - ng.psnr(gt, img_fp8["rgb"]) <= 0.1)}
     if proposal is not None:
         prop_info[other_mode] = {"rays_per_s": world * R / (other_ms / 1000.0),
                                  "psnr_db": ng.psnr(gt, img_other["rgb"]),
