@@ -5,8 +5,8 @@
 // STORE): each layer's BF16 activations are exactly the operands its
 // successor's MMAs read. The backward runs the layers of mlp_train.cu from
 // the heads down, with every product a BF16 GEMM accumulating in FP32:
-//   prep    z = dX (+ dpre_sigma * ws at dense_7) * [h > 0]  (FP32)
-//           dz = bf16(z), db += column sums of z
+//   prep    z = dX (+ dpre_sigma * ws at dense_7) * [h > 0]  (dX in BF16
+//           from the GEMM, z in FP32), dz = bf16(z), db += column sums of z
 //   dW      grads[k][n] += sum_m In[m][k] dz[m][n]   (In = the tape's BF16 input columns)
 //   dX      dX[m][k] = sum_n dz[m][n] W[k][n], k < 256 (W = BF16 copy of the FP32 master weights)
 // The two products are plain GEMMs and go to cuBLASLt; everything around
@@ -44,11 +44,11 @@ static uint32_t align_of(const void *p) {
   return al;
 }
 
-// C (FP32, column-major m x n, ldc) = op(A) op(B) + beta C; A, B BF16
-// column-major with leading dimensions lda, ldb.
+// C (column-major m x n, ldc; FP32 or BF16 per ctype) = op(A) op(B) + beta C;
+// A, B BF16 column-major with leading dimensions lda, ldb; FP32 accumulation.
 static int gemm(cublasOperation_t ta, cublasOperation_t tb, long long m, long long n, long long k, const void *A,
-                long long lda, const void *B, long long ldb, float beta, float *C, long long ldc, void *ws,
-                cudaStream_t st) {
+                long long lda, const void *B, long long ldb, float beta, void *C, cudaDataType_t ctype, long long ldc,
+                void *ws, cudaStream_t st) {
   if (m == 0 || n == 0) return NERFGB_OK;
   cublasLtHandle_t h = lt_handle();
   if (!h) return NERFGB_E_CUDA;
@@ -68,7 +68,7 @@ static int gemm(cublasOperation_t ta, cublasOperation_t tb, long long m, long lo
           CUBLAS_STATUS_SUCCESS ||
       cublasLtMatrixLayoutCreate(&lb, CUDA_R_16BF, tb == CUBLAS_OP_N ? k : n, tb == CUBLAS_OP_N ? n : k, ldb) !=
           CUBLAS_STATUS_SUCCESS ||
-      cublasLtMatrixLayoutCreate(&lc, CUDA_R_32F, m, n, ldc) != CUBLAS_STATUS_SUCCESS)
+      cublasLtMatrixLayoutCreate(&lc, ctype, m, n, ldc) != CUBLAS_STATUS_SUCCESS)
     goto done;
   if (cublasLtMatmulPreferenceCreate(&pref) != CUBLAS_STATUS_SUCCESS ||
       cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &ws_bytes,
@@ -106,35 +106,85 @@ __global__ void to_bf16_kernel(const float *__restrict__ src, __nv_bfloat16 *__r
     dst[i] = __float2bfloat16_rn(src[i]);
 }
 
-// z = raw (+ dsp * ws) (* [tape act > 0]) over N columns; dz = bf16(z);
-// db[n] += sum_m z. One thread per column, kPrepRows rows per block.
-template <bool MASK, bool SIG>
+// z = raw (+ dsp * ws) (* [tape act > 0]) over N columns (N = 128 or 256);
+// dz = bf16(z); db[n] += sum_m z. Eight columns per thread (16-byte loads
+// and stores), N / 8 threads per row, 256 threads per block over kPrepRows
+// rows; the column sums are reduced in shared memory, one atomic per column
+// per block.
+__device__ __forceinline__ void load8(const float *p, float (&v)[8]) {
+  const float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void load8(const __nv_bfloat16 *p, float (&v)[8]) {
+  const uint4 u = *reinterpret_cast<const uint4 *>(p);
+  const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    v[2 * i] = __uint_as_float(w[i] << 16);
+    v[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+  }
+}
+
+template <typename Tin, bool MASK, bool SIG>
 __global__ void __launch_bounds__(256)
-    prep_kernel(const float *__restrict__ raw, long long M, int N, const uint16_t *__restrict__ tape, int act_off,
+    prep_kernel(const Tin *__restrict__ raw, long long M, int N, const uint16_t *__restrict__ tape, int act_off,
                 const float *__restrict__ dsp, const float *__restrict__ ws, __nv_bfloat16 *__restrict__ dz,
                 float *__restrict__ db) {
-  const int c = threadIdx.x;
-  if (c >= N) return;
+  __shared__ float red[256 * 8];
+  const int tpr = N / 8;                    // threads per row
+  const int rpp = 256 / tpr;                // rows per pass
+  const int t = threadIdx.x, c0 = (t % tpr) * 8, rsub = t / tpr;
   const long long m0 = (long long)blockIdx.x * kPrepRows;
   const long long m1 = m0 + kPrepRows < M ? m0 + kPrepRows : M;
-  const float w = SIG ? ws[c] : 0.0f;
-  float sum = 0.0f;
-  for (long long m = m0; m < m1; ++m) {
-    float z = raw[m * kDzLd + c];
-    if (SIG) z = fmaf(dsp[m], w, z);
-    if (MASK) {
-      const uint16_t a = tape[m * kActsLd + act_off + c];
-      if (a == 0 || (a & 0x8000u)) z = 0.0f;  // ReLU output <= 0
-    }
-    dz[m * kDzLd + c] = __float2bfloat16_rn(z);
-    sum += z;
+  float w[8], sum[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    w[i] = SIG ? ws[c0 + i] : 0.0f;
+    sum[i] = 0.0f;
   }
-  atomicAdd(db + c, sum);
+#pragma unroll 2
+  for (long long m = m0 + rsub; m < m1; m += rpp) {
+    float z[8];
+    load8(raw + m * kDzLd + c0, z);
+    if (SIG) {
+      const float d = dsp[m];
+#pragma unroll
+      for (int i = 0; i < 8; ++i) z[i] = fmaf(d, w[i], z[i]);
+    }
+    if (MASK) {
+      const uint4 a = *reinterpret_cast<const uint4 *>(tape + m * kActsLd + act_off + c0);
+      const uint32_t aw[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const uint32_t lo = aw[i] & 0xffffu, hi = aw[i] >> 16;  // ReLU outputs: > 0 unless 0 (or -0)
+        if (lo == 0 || (lo & 0x8000u)) z[2 * i] = 0.0f;
+        if (hi == 0 || (hi & 0x8000u)) z[2 * i + 1] = 0.0f;
+      }
+    }
+    uint4 o;
+    __nv_bfloat162 p0 = __floats2bfloat162_rn(z[0], z[1]), p1 = __floats2bfloat162_rn(z[2], z[3]);
+    __nv_bfloat162 p2 = __floats2bfloat162_rn(z[4], z[5]), p3 = __floats2bfloat162_rn(z[6], z[7]);
+    o.x = *reinterpret_cast<uint32_t *>(&p0);
+    o.y = *reinterpret_cast<uint32_t *>(&p1);
+    o.z = *reinterpret_cast<uint32_t *>(&p2);
+    o.w = *reinterpret_cast<uint32_t *>(&p3);
+    *reinterpret_cast<uint4 *>(dz + m * kDzLd + c0) = o;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) sum[i] += z[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i) red[rsub * N + c0 + i] = sum[i];
+  __syncthreads();
+  for (int c = t; c < N; c += 256) {
+    float a = 0.0f;
+    for (int r = 0; r < rpp; ++r) a += red[r * N + c];
+    atomicAdd(db + c, a);
+  }
 }
 
 struct Ws {
-  float *bufA, *bufB, *dsp;
-  __nv_bfloat16 *dz, *wb;
+  float *f32, *dsp;                  // dZ9 from the heads (FP32), dpre_sigma
+  __nv_bfloat16 *raw, *dz, *wb;      // dX output, masked dZ (GEMM operand), BF16 weights
   void *lt;
   long long bytes;
 };
@@ -149,9 +199,9 @@ static Ws carve(void *base, long long n) {
     off += a256(bytes);
     return p;
   };
-  w.bufA = reinterpret_cast<float *>(take(n * kDzLd * 4));
-  w.bufB = reinterpret_cast<float *>(take(n * kDzLd * 4));
+  w.f32 = reinterpret_cast<float *>(take(n * kDzLd * 4));
   w.dsp = reinterpret_cast<float *>(take(n * 4));
+  w.raw = reinterpret_cast<__nv_bfloat16 *>(take(n * kDzLd * 2));
   w.dz = reinterpret_cast<__nv_bfloat16 *>(take(n * kDzLd * 2));
   w.wb = reinterpret_cast<__nv_bfloat16 *>(take(kGemmWElems * 2));
   w.lt = take(kLtWsBytes);
@@ -159,11 +209,11 @@ static Ws carve(void *base, long long n) {
   return w;
 }
 
-template <bool MASK, bool SIG>
-static int prep(const float *raw, long long M, int N, const uint16_t *tape, int act_off, const float *dsp,
+template <bool MASK, bool SIG, typename Tin>
+static int prep(const Tin *raw, long long M, int N, const uint16_t *tape, int act_off, const float *dsp,
                 const float *ws, __nv_bfloat16 *dz, float *db, cudaStream_t st) {
   const long long blocks = (M + kPrepRows - 1) / kPrepRows;
-  prep_kernel<MASK, SIG><<<(unsigned)blocks, 256, 0, st>>>(raw, M, N, tape, act_off, dsp, ws, dz, db);
+  prep_kernel<Tin, MASK, SIG><<<(unsigned)blocks, 256, 0, st>>>(raw, M, N, tape, act_off, dsp, ws, dz, db);
   return launch_status();
 }
 
@@ -172,14 +222,15 @@ static int prep(const float *raw, long long M, int N, const uint16_t *tape, int 
 static int dW(const uint16_t *tape, int in_off, int K, const __nv_bfloat16 *dz, int N, long long M, float *grads,
               int fl, int k_dst0, void *lt, cudaStream_t st) {
   return gemm(CUBLAS_OP_N, CUBLAS_OP_T, N, K, M, dz, kDzLd, tape + in_off, kActsLd, 1.0f,
-              grads + flat_offset(fl) + (long long)k_dst0 * N, N, lt, st);
+              grads + flat_offset(fl) + (long long)k_dst0 * N, CUDA_R_32F, N, lt, st);
 }
 
-// out [M][256] = dz [M][N] W_g[0:256][N]^T.
-static int dX(const __nv_bfloat16 *wb, int g, const __nv_bfloat16 *dz, long long M, float *out, void *lt,
+// out [M][256] (BF16) = dz [M][N] W_g[0:256][N]^T.
+static int dX(const __nv_bfloat16 *wb, int g, const __nv_bfloat16 *dz, long long M, __nv_bfloat16 *out, void *lt,
               cudaStream_t st) {
   const int N = gemm_n(g);
-  return gemm(CUBLAS_OP_T, CUBLAS_OP_N, 256, M, N, wb + gemm_w_offset(g), N, dz, kDzLd, 0.0f, out, kDzLd, lt, st);
+  return gemm(CUBLAS_OP_T, CUBLAS_OP_N, 256, M, N, wb + gemm_w_offset(g), N, dz, kDzLd, 0.0f, out, CUDA_R_16BF,
+              kDzLd, lt, st);
 }
 
 static float *bias_grad(float *grads, int fl) { return grads + flat_offset(fl) + (long long)flat_in(fl) * flat_out(fl); }
@@ -224,27 +275,26 @@ extern "C" int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tap
   int rc;
   to_bf16_kernel<<<(unsigned)((kGemmWElems + 255) / 256), 256, 0, st>>>(W, w.wb, kGemmWElems);
   if ((rc = launch_status()) != NERFGB_OK) return rc;
-  // heads -> dZ9 (masked by [h9 > 0]) and dpre_sigma
-  if ((rc = launch_head_bwd(table, tp, M, d_rgb, d_sigma, w.bufA, w.dsp, grad_params, st)) != NERFGB_OK) return rc;
+  // heads -> dZ9 (masked by [h9 > 0], FP32) and dpre_sigma
+  if ((rc = launch_head_bwd(table, tp, M, d_rgb, d_sigma, w.f32, w.dsp, grad_params, st)) != NERFGB_OK) return rc;
   // dense_9 (flat 10): input [bottleneck | enc_dir], 128 outputs
-  if ((rc = prep<false, false>(w.bufA, M, 128, tp, 0, nullptr, nullptr, w.dz, bias_grad(grad_params, 10), st)) !=
+  if ((rc = prep<false, false>(w.f32, M, 128, tp, 0, nullptr, nullptr, w.dz, bias_grad(grad_params, 10), st)) !=
       NERFGB_OK)
     return rc;
   if ((rc = dW(tp, acts_offset(8), 256, w.dz, 128, M, grad_params, 10, 0, w.lt, st)) != NERFGB_OK) return rc;
   if ((rc = dW(tp, kActsEncDir, 27, w.dz, 128, M, grad_params, 10, 256, w.lt, st)) != NERFGB_OK) return rc;
-  if ((rc = dX(w.wb, 9, w.dz, M, w.bufB, w.lt, st)) != NERFGB_OK) return rc;
+  if ((rc = dX(w.wb, 9, w.dz, M, w.raw, w.lt, st)) != NERFGB_OK) return rc;
   // dense_8 (flat 9): linear, input h7
-  if ((rc = prep<false, false>(w.bufB, M, 256, tp, 0, nullptr, nullptr, w.dz, bias_grad(grad_params, 9), st)) !=
+  if ((rc = prep<false, false>(w.raw, M, 256, tp, 0, nullptr, nullptr, w.dz, bias_grad(grad_params, 9), st)) !=
       NERFGB_OK)
     return rc;
   if ((rc = dW(tp, acts_offset(7), 256, w.dz, 256, M, grad_params, 9, 0, w.lt, st)) != NERFGB_OK) return rc;
-  if ((rc = dX(w.wb, 8, w.dz, M, w.bufA, w.lt, st)) != NERFGB_OK) return rc;
+  if ((rc = dX(w.wb, 8, w.dz, M, w.raw, w.lt, st)) != NERFGB_OK) return rc;
   // dense_7 .. dense_0
-  float *cur = w.bufA, *nxt = w.bufB;
   for (int l = 7; l >= 0; --l) {
     float *db = bias_grad(grad_params, l);
-    rc = (l == 7) ? prep<true, true>(cur, M, 256, tp, acts_offset(7), w.dsp, table + kSigmaWOff, w.dz, db, st)
-                  : prep<true, false>(cur, M, 256, tp, acts_offset(l), nullptr, nullptr, w.dz, db, st);
+    rc = (l == 7) ? prep<true, true>(w.raw, M, 256, tp, acts_offset(7), w.dsp, table + kSigmaWOff, w.dz, db, st)
+                  : prep<true, false>(w.raw, M, 256, tp, acts_offset(l), nullptr, nullptr, w.dz, db, st);
     if (rc != NERFGB_OK) return rc;
     if (l == 0) {
       if ((rc = dW(tp, kActsEncXyz, 63, w.dz, 256, M, grad_params, 0, 0, w.lt, st)) != NERFGB_OK) return rc;
@@ -256,10 +306,7 @@ extern "C" int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tap
     } else {
       if ((rc = dW(tp, acts_offset(l - 1), 256, w.dz, 256, M, grad_params, l, 0, w.lt, st)) != NERFGB_OK) return rc;
     }
-    if ((rc = dX(w.wb, l, w.dz, M, nxt, w.lt, st)) != NERFGB_OK) return rc;
-    float *t = cur;
-    cur = nxt;
-    nxt = t;
+    if ((rc = dX(w.wb, l, w.dz, M, w.raw, w.lt, st)) != NERFGB_OK) return rc;
   }
   return NERFGB_OK;
 }
