@@ -63,25 +63,44 @@ __global__ void __launch_bounds__(256)
       *reinterpret_cast<float4 *>(&sH7[r][4 * q]) = v;
     }
     __syncthreads();
-    if (tid < kTM) {
-      const int r = tid;
+    {
+      // head pre-activations: four threads per row, each a quarter of the
+      // dot products (j = part + 4i: conflict-free with the padded rows),
+      // combined by shuffles in the four-lane group
+      const int r = tid >> 2, part = tid & 3;
       const bool valid = row0 + r < n;
-      float pre[3] = {br[0], br[1], br[2]};
-      for (int j = 0; j < 128; ++j) {
+      float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, sp = 0.0f;
+#pragma unroll 8
+      for (int i = 0; i < 32; ++i) {
+        const int j = part + 4 * i;
         const float h = sH9[r][j];
-        pre[0] = fmaf(h, Wr[3 * j], pre[0]);
-        pre[1] = fmaf(h, Wr[3 * j + 1], pre[1]);
-        pre[2] = fmaf(h, Wr[3 * j + 2], pre[2]);
+        p0 = fmaf(h, Wr[3 * j], p0);
+        p1 = fmaf(h, Wr[3 * j + 1], p1);
+        p2 = fmaf(h, Wr[3 * j + 2], p2);
       }
-      for (int c = 0; c < 3; ++c) {
-        const float y = 1.0f / (1.0f + expf(-pre[c]));
-        sDRP[r][c] = valid ? d_rgb[(row0 + r) * 3 + c] * y * (1.0f - y) : 0.0f;
+#pragma unroll 8
+      for (int i = 0; i < 64; ++i) {
+        const int j = part + 4 * i;
+        sp = fmaf(sH7[r][j], ws[j], sp);
       }
-      float sp = table[kSigmaBOff];
-      for (int j = 0; j < 256; ++j) sp = fmaf(sH7[r][j], ws[j], sp);
-      const float dsp = (valid && d_sigma && sp > 0.0f) ? d_sigma[row0 + r] : 0.0f;
-      sDSP[r] = dsp;
-      if (valid) dsp_out[row0 + r] = dsp;
+#pragma unroll
+      for (int o = 1; o <= 2; o <<= 1) {
+        p0 += __shfl_xor_sync(0xffffffffu, p0, o);
+        p1 += __shfl_xor_sync(0xffffffffu, p1, o);
+        p2 += __shfl_xor_sync(0xffffffffu, p2, o);
+        sp += __shfl_xor_sync(0xffffffffu, sp, o);
+      }
+      if (part == 0) {
+        const float pre[3] = {br[0] + p0, br[1] + p1, br[2] + p2};
+        for (int c = 0; c < 3; ++c) {
+          const float y = 1.0f / (1.0f + expf(-pre[c]));
+          sDRP[r][c] = valid ? d_rgb[(row0 + r) * 3 + c] * y * (1.0f - y) : 0.0f;
+        }
+        sp += table[kSigmaBOff];
+        const float dsp = (valid && d_sigma && sp > 0.0f) ? d_sigma[row0 + r] : 0.0f;
+        sDSP[r] = dsp;
+        if (valid) dsp_out[row0 + r] = dsp;
+      }
     }
     __syncthreads();
     for (int e = tid; e < kTM * 128; e += 256) {
