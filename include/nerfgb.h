@@ -185,6 +185,12 @@ long long nerfgb_proposal_param_count(void);
 int nerfgb_proposal_forward(const float *params, const float *xyz, long long n,
                             float *sigma, void *stream);
 
+/* nerfgb_proposal_forward on tensor cores: BF16 operands, FP32 accumulation
+ * (the encoding and the last layer in FP32). The render paths use it with a
+ * BF16 or FP8 NeRF MLP, and nerfgb_proposal_forward with an FP32 one. */
+int nerfgb_proposal_forward_bf16(const float *params, const float *xyz,
+                                 long long n, float *sigma, void *stream);
+
 /* grad_params [6785] += d/dparams of sum_i grad_sigma[i] * sigma_i
  * (accumulates; zero it first). */
 int nerfgb_proposal_backward(const float *params, const float *xyz,
@@ -209,8 +215,9 @@ int nerfgb_proposal_weights_backward(const float *sigma, const float *t_vals,
  * its density at the Sc stratified samples, composited as the coarse pass
  * is, gives the PDF of the fine sampler; the fine MLP then runs on the
  * Sc + Sf sorted samples. The proposal's weights are those of
- * nerfgb_proposal_weights. Outputs the fine rgb/depth/acc maps. Same
- * workspace size as nerfgb_render_rays. */
+ * nerfgb_proposal_weights; the proposal runs in FP32 with an FP32 MLP and
+ * in BF16 (nerfgb_proposal_forward_bf16) otherwise. Outputs the fine
+ * rgb/depth/acc maps. Same workspace size as nerfgb_render_rays. */
 int nerfgb_render_rays_proposal(const float *proposal_params,
                                 const void *packed_fine, int precision,
                                 const float *rays_o, const float *rays_d,
@@ -244,7 +251,8 @@ long long nerfgb_render_gated_workspace_bytes(int n_rays, int n_coarse,
                                               int n_fine);
 
 /* The proposal-gated render: the coarse -> fine chain of nerfgb_render_rays,
- * with the proposal deciding which samples the NeRF MLP evaluates. Coarse
+ * with the proposal (FP32 with an FP32 MLP, BF16 otherwise) deciding which
+ * samples the NeRF MLP evaluates. Coarse
  * samples whose proposal weight (nerfgb_proposal_weights of the proposal
  * density at the stratified samples) is at most gate_tau get sigma = 0 and
  * are not evaluated, in the coarse pass and again in the fine pass's sorted

@@ -49,6 +49,7 @@ SIGNATURES = {
                                P, P, P, P, P, P, P, P, P]),
     "nerfgb_proposal_param_count": (LL, []),
     "nerfgb_proposal_forward": (I, [P, P, LL, P, P]),
+    "nerfgb_proposal_forward_bf16": (I, [P, P, LL, P, P]),
     "nerfgb_proposal_backward": (I, [P, P, P, LL, P, P]),
     "nerfgb_proposal_weights": (I, [P, P, I, I, I, P, P]),
     "nerfgb_proposal_weights_backward": (I, [P, P, P, I, I, P, P]),

@@ -60,6 +60,9 @@ int launch_gate_fine(const int *perm, const unsigned char *mask_c, int R, int Sc
 
 // Proposal network forward (proposal.cu).
 int launch_proposal_forward(const float *params, const float *xyz, long long n, float *sigma, cudaStream_t stream);
+// The same network on tensor cores: BF16 operands, FP32 accumulation (proposal.cu).
+int launch_proposal_forward_bf16(const float *params, const float *xyz, long long n, float *sigma,
+                                 cudaStream_t stream);
 
 // Compositing with a chosen last interval (ray_ops.cu): last_delta >= 0 is
 // used as is (the reference uses 1e10), < 0 means the previous spacing.

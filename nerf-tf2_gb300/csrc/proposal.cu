@@ -18,6 +18,7 @@
 // memory (odd row strides, conflict-free), then each thread reduces its own
 // slice of dW over the tile in registers and adds it to the CTA's gradient
 // in shared memory; one atomicAdd per parameter per CTA at the end.
+#include <cuda_bf16.h>
 #include <math.h>
 
 #include "common.cuh"
@@ -102,6 +103,141 @@ __global__ void __launch_bounds__(kThreads)
 #pragma unroll
     for (int j = 0; j < kH; ++j) z3 = fmaf(fmaxf(z2[j], 0.0f), sw[kW3 + j], z3);
     sigma[i] = softplus(z3);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Inference forward on tensor cores: BF16 operands, FP32 accumulation
+// (mma.sync m16n8k16; at 6,656 MAC per sample the kernel is bound by the
+// encoding and its memory traffic, not by the tensor pipe). One warp per 16
+// samples: layer 1's accumulator fragments are layer 2's A fragments (the
+// m16n8 C layout of two n-tiles is the m16k16 A layout), so h1 never leaves
+// registers. Weights sit in shared memory transposed ([n][k], k contiguous),
+// rows padded by 8 BF16 so that a B-fragment load is conflict-free.
+// ---------------------------------------------------------------------------
+constexpr int kK1 = 48;              // 39 inputs padded to 3 k-steps of 16
+constexpr int kLd1 = kK1 + 8, kLd2 = kH + 8;
+constexpr int kFwdWarps = 4;
+
+__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
+  __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
+  return *reinterpret_cast<uint32_t *>(&p);
+}
+__device__ __forceinline__ uint32_t bf16x2_relu(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+__device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, "
+      "{%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+// Encoding feature k (the layout of encode6) of point x.
+__device__ __forceinline__ float enc_feature(const float (&x)[3], int k) {
+  if (k < 3) return x[k];
+  if (k >= kIn) return 0.0f;
+  const int q = k - 3, c = q / 12, l = (q % 12) >> 1;
+  float sn, cs;
+  sincosf(fmul(x[c], enc_multiplier(l)), &sn, &cs);
+  return (q & 1) ? cs : sn;
+}
+
+__global__ void __launch_bounds__(32 * kFwdWarps)
+    prop_fwd_bf16_kernel(const float *__restrict__ params, const float *__restrict__ xyz, long long n,
+                         float *__restrict__ sigma) {
+  __shared__ __align__(16) __nv_bfloat16 sW1[kH * kLd1];
+  __shared__ __align__(16) __nv_bfloat16 sW2[kH * kLd2];
+  __shared__ float sB1[kH], sB2[kH], sW3[kH], sB3;
+  for (int e = threadIdx.x; e < kH * kLd1; e += blockDim.x) {
+    const int nn = e / kLd1, k = e % kLd1;
+    sW1[e] = __float2bfloat16_rn(k < kIn ? params[kW1 + k * kH + nn] : 0.0f);
+  }
+  for (int e = threadIdx.x; e < kH * kLd2; e += blockDim.x) {
+    const int nn = e / kLd2, k = e % kLd2;
+    sW2[e] = __float2bfloat16_rn(k < kH ? params[kW2 + k * kH + nn] : 0.0f);
+  }
+  for (int j = threadIdx.x; j < kH; j += blockDim.x) {
+    sB1[j] = params[kB1 + j];
+    sB2[j] = params[kB2 + j];
+    sW3[j] = params[kW3 + j];
+  }
+  if (threadIdx.x == 0) sB3 = params[kB3];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+  const long long ntiles = (n + 15) / 16;
+  const long long wstride = (long long)gridDim.x * kFwdWarps;
+  for (long long tile = (long long)blockIdx.x * kFwdWarps + (threadIdx.x >> 5); tile < ntiles; tile += wstride) {
+    const long long r0 = tile * 16 + g, r1 = r0 + 8;
+    float x0[3] = {0.f, 0.f, 0.f}, x1[3] = {0.f, 0.f, 0.f};
+    if (r0 < n) {
+      x0[0] = xyz[3 * r0];
+      x0[1] = xyz[3 * r0 + 1];
+      x0[2] = xyz[3 * r0 + 2];
+    }
+    if (r1 < n) {
+      x1[0] = xyz[3 * r1];
+      x1[1] = xyz[3 * r1 + 1];
+      x1[2] = xyz[3 * r1 + 2];
+    }
+    // layer 1: [16 x 48] enc x [48 x 64] W1, accumulators start at b1
+    float d1[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      d1[j][0] = d1[j][2] = sB1[8 * j + 2 * t];
+      d1[j][1] = d1[j][3] = sB1[8 * j + 2 * t + 1];
+    }
+#pragma unroll
+    for (int ks = 0; ks < kK1 / 16; ++ks) {
+      const int k0 = 16 * ks + 2 * t;
+      uint32_t a[4];
+      a[0] = bf16x2(enc_feature(x0, k0), enc_feature(x0, k0 + 1));
+      a[1] = bf16x2(enc_feature(x1, k0), enc_feature(x1, k0 + 1));
+      a[2] = bf16x2(enc_feature(x0, k0 + 8), enc_feature(x0, k0 + 9));
+      a[3] = bf16x2(enc_feature(x1, k0 + 8), enc_feature(x1, k0 + 9));
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const __nv_bfloat16 *b = sW1 + (8 * j + g) * kLd1 + k0;
+        mma_bf16(d1[j], a, *reinterpret_cast<const uint32_t *>(b), *reinterpret_cast<const uint32_t *>(b + 8));
+      }
+    }
+    // layer 2: relu(h1) as BF16 A fragments straight from the layer-1 accumulators
+    float d2[8][4];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      d2[j][0] = d2[j][2] = sB2[8 * j + 2 * t];
+      d2[j][1] = d2[j][3] = sB2[8 * j + 2 * t + 1];
+    }
+#pragma unroll
+    for (int ks = 0; ks < kH / 16; ++ks) {
+      const uint32_t a[4] = {bf16x2_relu(d1[2 * ks][0], d1[2 * ks][1]), bf16x2_relu(d1[2 * ks][2], d1[2 * ks][3]),
+                             bf16x2_relu(d1[2 * ks + 1][0], d1[2 * ks + 1][1]),
+                             bf16x2_relu(d1[2 * ks + 1][2], d1[2 * ks + 1][3])};
+      const int k0 = 16 * ks + 2 * t;
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        const __nv_bfloat16 *b = sW2 + (8 * j + g) * kLd2 + k0;
+        mma_bf16(d2[j], a, *reinterpret_cast<const uint32_t *>(b), *reinterpret_cast<const uint32_t *>(b + 8));
+      }
+    }
+    // layer 3 (FP32): relu(z2) . w3 over this thread's 16 columns, then the quad
+    float p0 = 0.0f, p1 = 0.0f;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const float w0 = sW3[8 * j + 2 * t], w1 = sW3[8 * j + 2 * t + 1];
+      p0 = fmaf(fmaxf(d2[j][0], 0.0f), w0, fmaf(fmaxf(d2[j][1], 0.0f), w1, p0));
+      p1 = fmaf(fmaxf(d2[j][2], 0.0f), w0, fmaf(fmaxf(d2[j][3], 0.0f), w1, p1));
+    }
+    p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
+    p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
+    p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
+    p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
+    if (t == 0) {
+      if (r0 < n) sigma[r0] = softplus(sB3 + p0);
+      if (r1 < n) sigma[r1] = softplus(sB3 + p1);
+    }
   }
 }
 
@@ -218,6 +354,13 @@ int launch_proposal_forward(const float *params, const float *xyz, long long n, 
   return launch_status();
 }
 
+int launch_proposal_forward_bf16(const float *params, const float *xyz, long long n, float *sigma,
+                                 cudaStream_t stream) {
+  prop::prop_fwd_bf16_kernel<<<prop::grid_for(n, 16 * prop::kFwdWarps), 32 * prop::kFwdWarps, 0, stream>>>(
+      params, xyz, n, sigma);
+  return launch_status();
+}
+
 }  // namespace nerfgb
 
 using namespace nerfgb;
@@ -243,6 +386,14 @@ extern "C" int nerfgb_proposal_weights_backward(const float *sigma, const float 
   if (!sigma || !t_vals || !grad_weights || !grad_sigma) return NERFGB_E_INVALID_ARG;
   return launch_composite_bwd(sigma, t_vals, nullptr, nullptr, grad_weights, n_rays, n_bins, 0, -1.0f, grad_sigma,
                               nullptr, as_stream(stream));
+}
+
+extern "C" int nerfgb_proposal_forward_bf16(const float *params, const float *xyz, long long n, float *sigma,
+                                            void *stream) {
+  if (n < 0) return NERFGB_E_INVALID_ARG;
+  if (n == 0) return NERFGB_OK;
+  if (!params || !xyz || !sigma) return NERFGB_E_INVALID_ARG;
+  return launch_proposal_forward_bf16(params, xyz, n, sigma, as_stream(stream));
 }
 
 extern "C" int nerfgb_proposal_forward(const float *params, const float *xyz, long long n, float *sigma,

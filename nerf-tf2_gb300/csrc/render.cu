@@ -33,6 +33,14 @@ static RenderWs carve(void *base, int R, int Sc, int Sf) {
   return w;
 }
 
+// The proposal runs at the render's precision class: FP32 with an FP32 MLP,
+// BF16 operands (tensor cores, FP32 accumulation) with a BF16 or FP8 MLP.
+static int launch_proposal(int precision, const float *params, const float *xyz, long long n, float *sigma,
+                           cudaStream_t stream) {
+  return precision == NERFGB_PREC_FP32 ? launch_proposal_forward(params, xyz, n, sigma, stream)
+                                       : launch_proposal_forward_bf16(params, xyz, n, sigma, stream);
+}
+
 int launch_mlp(const void *packed, int precision, const float *xyz, const float *dirs, long long n, int rpd,
                float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm) {
   if (precision == NERFGB_PREC_FP32) return launch_mlp_fp32(packed, xyz, dirs, n, rpd, rgb, sigma, stream, rm);
@@ -135,7 +143,7 @@ extern "C" int nerfgb_render_rays_proposal(const float *proposal_params, const v
                                  w.t_c, w.edges, w.widths, stream)) != NERFGB_OK)
     return rc;
   // The proposal density at the stratified samples replaces the coarse MLP.
-  if ((rc = launch_proposal_forward(proposal_params, w.xyz_c, (long long)R * Sc, w.sig_c, st)) != NERFGB_OK)
+  if ((rc = launch_proposal(precision, proposal_params, w.xyz_c, (long long)R * Sc, w.sig_c, st)) != NERFGB_OK)
     return rc;
   if ((rc = nerfgb_proposal_weights(w.sig_c, w.t_c, R, Sc, trans_mode, w.w_c, stream)) != NERFGB_OK) return rc;
   if ((rc = nerfgb_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, uf, R, Sc, Sf, w.xyz_f,
@@ -230,7 +238,7 @@ extern "C" int nerfgb_render_rays_gated(const float *proposal_params, const void
                                  w.t_c, w.edges, w.widths, stream)) != NERFGB_OK)
     return rc;
   // Proposal weights over the coarse bins, then the coarse gate.
-  if ((rc = launch_proposal_forward(proposal_params, w.xyz_c, (long long)R * Sc, g.sig_p, st)) != NERFGB_OK)
+  if ((rc = launch_proposal(precision, proposal_params, w.xyz_c, (long long)R * Sc, g.sig_p, st)) != NERFGB_OK)
     return rc;
   if ((rc = nerfgb_proposal_weights(g.sig_p, w.t_c, R, Sc, trans_mode, g.w_p, stream)) != NERFGB_OK) return rc;
   if (cudaMemsetAsync(g.counts, 0, 2 * sizeof(int), st) != cudaSuccess ||

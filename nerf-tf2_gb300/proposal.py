@@ -38,12 +38,16 @@ class ProposalNetwork:
         blob = glorot_blob(seed) if params is None else params
         self.params = as_cuda(blob, shape=(PARAM_COUNT,), name="proposal params").clone()
 
-    def __call__(self, xyz):
-        """sigma [n,1] at xyz [n,3]."""
+    def __call__(self, xyz, precision="fp32"):
+        """sigma [n,1] at xyz [n,3]. "fp32": the SIMT kernel (training uses
+        it); "bf16": tensor cores, BF16 operands and FP32 accumulation."""
+        if precision not in ("fp32", "bf16"):
+            raise ValueError(f"proposal precision must be fp32 or bf16, not {precision!r}")
         xyz = as_cuda(xyz, name="xyz")
         n = xyz.shape[0]
         sigma = empty(n, 1)
-        _lib.call("nerfgb_proposal_forward", ptr(self.params), ptr(xyz), n, ptr(sigma), stream())
+        _lib.call("nerfgb_proposal_forward" if precision == "fp32" else "nerfgb_proposal_forward_bf16",
+                  ptr(self.params), ptr(xyz), n, ptr(sigma), stream())
         return sigma
 
     def backward(self, xyz, grad_sigma, grad_params=None):

@@ -110,6 +110,38 @@ def test_proposal_forward_backward_vs_oracle(ng, oracle, cuda):
     np.testing.assert_allclose(g, wg, atol=1e-3 * np.abs(wg).max(), rtol=1e-3)
 
 
+def _bf16(a):
+    """Round-to-nearest-even to BF16, returned as float32."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    u = (u + 0x7FFF + ((u >> 16) & 1)) & 0xFFFF0000
+    return u.astype(np.uint32).view(np.float32)
+
+
+@pytest.mark.parametrize("n", [1000, 13])
+def test_proposal_forward_bf16_vs_oracle(ng, oracle, cuda, n):
+    """The tensor-core proposal forward (BF16 operands, FP32 accumulation)
+    against (1) a float64 evaluation with the same BF16 roundings of the
+    encoding, W1, h1 and W2 (checks the fragment layout: tight) and (2) the
+    float64 oracle (BF16-sized tolerance)."""
+    rng = np.random.default_rng(n)
+    blob = ng.proposal.glorot_blob(4)
+    blob[2496:2560] = rng.uniform(-0.1, 0.1, 64)
+    blob[6656:6720] = rng.uniform(-0.1, 0.1, 64)
+    x = rng.uniform(-4, 4, (n, 3)).astype(F32)
+    prop = ng.ProposalNetwork(blob)
+    sig = host(prop(dev(x), precision="bf16"))[:, 0]
+    p = oracle.prop_unpack(blob, F32)
+    enc = oracle.positional_encoding(x, 6, F32)
+    h1 = np.maximum(_bf16(enc).astype(F64) @ _bf16(p["W1"]).astype(F64) + p["b1"], 0)
+    z2 = _bf16(h1.astype(F32)).astype(F64) @ _bf16(p["W2"]).astype(F64) + p["b2"]
+    z3 = np.maximum(z2, 0) @ p["W3"].astype(F64) + p["b3"][0]
+    emul = oracle.softplus(z3)
+    np.testing.assert_allclose(sig, emul, rtol=2e-4, atol=2e-5)
+    want = oracle.prop_forward(blob, x, F64)
+    assert np.abs(sig - want).max() < 3e-2 * max(1.0, np.abs(want).max())
+    assert np.abs(sig - host(prop(dev(x)))[:, 0]).max() > 0  # not the FP32 kernel
+
+
 @pytest.fixture(scope="module")
 def proposal_case(ng):
     """A band-limited sparse scene (one random-init network as coarse and
