@@ -118,11 +118,8 @@ __global__ void __launch_bounds__(kThreads)
 constexpr int kK1 = 48;              // 39 inputs padded to 3 k-steps of 16
 constexpr int kLd1 = kK1 + 8, kLd2 = kH + 8;
 constexpr int kFwdWarps = 4;
+constexpr int kEncLdB = kK1 + 8;     // per-warp encoding rows (BF16), padded
 
-__device__ __forceinline__ uint32_t bf16x2(float lo, float hi) {
-  __nv_bfloat162 p = __floats2bfloat162_rn(lo, hi);
-  return *reinterpret_cast<uint32_t *>(&p);
-}
 __device__ __forceinline__ uint32_t bf16x2_relu(float lo, float hi) {
   uint32_t d;
   asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
@@ -135,22 +132,13 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
-// Encoding feature k (the layout of encode6) of point x.
-__device__ __forceinline__ float enc_feature(const float (&x)[3], int k) {
-  if (k < 3) return x[k];
-  if (k >= kIn) return 0.0f;
-  const int q = k - 3, c = q / 12, l = (q % 12) >> 1;
-  float sn, cs;
-  sincosf(fmul(x[c], enc_multiplier(l)), &sn, &cs);
-  return (q & 1) ? cs : sn;
-}
-
 __global__ void __launch_bounds__(32 * kFwdWarps)
     prop_fwd_bf16_kernel(const float *__restrict__ params, const float *__restrict__ xyz, long long n,
                          float *__restrict__ sigma) {
   __shared__ __align__(16) __nv_bfloat16 sW1[kH * kLd1];
   __shared__ __align__(16) __nv_bfloat16 sW2[kH * kLd2];
   __shared__ float sB1[kH], sB2[kH], sW3[kH], sB3;
+  __shared__ __align__(16) __nv_bfloat16 sEnc[kFwdWarps][16 * kEncLdB];
   for (int e = threadIdx.x; e < kH * kLd1; e += blockDim.x) {
     const int nn = e / kLd1, k = e % kLd1;
     sW1[e] = __float2bfloat16_rn(k < kIn ? params[kW1 + k * kH + nn] : 0.0f);
@@ -171,17 +159,39 @@ __global__ void __launch_bounds__(32 * kFwdWarps)
   const long long wstride = (long long)gridDim.x * kFwdWarps;
   for (long long tile = (long long)blockIdx.x * kFwdWarps + (threadIdx.x >> 5); tile < ntiles; tile += wstride) {
     const long long r0 = tile * 16 + g, r1 = r0 + 8;
-    float x0[3] = {0.f, 0.f, 0.f}, x1[3] = {0.f, 0.f, 0.f};
-    if (r0 < n) {
-      x0[0] = xyz[3 * r0];
-      x0[1] = xyz[3 * r0 + 1];
-      x0[2] = xyz[3 * r0 + 2];
+    // The tile's encodings (BF16) into the warp's buffer: two lanes per row,
+    // each computing nine of the row's eighteen sin/cos pairs (angles a = h,
+    // h + 2, ..., a = 6c + l) plus the three coordinates (h = 0) or the zero
+    // padding (h = 1).
+    __nv_bfloat16 *enc = sEnc[threadIdx.x >> 5];
+    {
+      const int row = lane >> 1, h = lane & 1;
+      const long long gr = tile * 16 + row;
+      float x[3] = {0.f, 0.f, 0.f};
+      if (gr < n) {
+        x[0] = xyz[3 * gr];
+        x[1] = xyz[3 * gr + 1];
+        x[2] = xyz[3 * gr + 2];
+      }
+      __nv_bfloat16 *er = enc + row * kEncLdB;
+      if (h == 0) {
+        er[0] = __float2bfloat16_rn(x[0]);
+        er[1] = __float2bfloat16_rn(x[1]);
+        er[2] = __float2bfloat16_rn(x[2]);
+      } else {
+#pragma unroll
+        for (int k = kIn; k < kK1; ++k) er[k] = __float2bfloat16_rn(0.0f);
+      }
+#pragma unroll
+      for (int a = h; a < 18; a += 2) {
+        const int c = a / 6, l = a % 6;
+        float sn, cs;
+        sincosf(fmul(x[c], enc_multiplier(l)), &sn, &cs);
+        er[3 + c * 12 + 2 * l] = __float2bfloat16_rn(sn);
+        er[3 + c * 12 + 2 * l + 1] = __float2bfloat16_rn(cs);
+      }
     }
-    if (r1 < n) {
-      x1[0] = xyz[3 * r1];
-      x1[1] = xyz[3 * r1 + 1];
-      x1[2] = xyz[3 * r1 + 2];
-    }
+    __syncwarp();
     // layer 1: [16 x 48] enc x [48 x 64] W1, accumulators start at b1
     float d1[8][4];
 #pragma unroll
@@ -192,11 +202,9 @@ __global__ void __launch_bounds__(32 * kFwdWarps)
 #pragma unroll
     for (int ks = 0; ks < kK1 / 16; ++ks) {
       const int k0 = 16 * ks + 2 * t;
-      uint32_t a[4];
-      a[0] = bf16x2(enc_feature(x0, k0), enc_feature(x0, k0 + 1));
-      a[1] = bf16x2(enc_feature(x1, k0), enc_feature(x1, k0 + 1));
-      a[2] = bf16x2(enc_feature(x0, k0 + 8), enc_feature(x0, k0 + 9));
-      a[3] = bf16x2(enc_feature(x1, k0 + 8), enc_feature(x1, k0 + 9));
+      const uint32_t *e0 = reinterpret_cast<const uint32_t *>(enc + g * kEncLdB + k0);
+      const uint32_t *e1 = reinterpret_cast<const uint32_t *>(enc + (g + 8) * kEncLdB + k0);
+      const uint32_t a[4] = {e0[0], e1[0], e0[4], e1[4]};
 #pragma unroll
       for (int j = 0; j < 8; ++j) {
         const __nv_bfloat16 *b = sW1 + (8 * j + g) * kLd1 + k0;
@@ -238,6 +246,7 @@ __global__ void __launch_bounds__(32 * kFwdWarps)
       if (r0 < n) sigma[r0] = softplus(sB3 + p0);
       if (r1 < n) sigma[r1] = softplus(sB3 + p1);
     }
+    __syncwarp();  // the buffer is rewritten by the next tile
   }
 }
 
