@@ -139,13 +139,14 @@ __global__ void __launch_bounds__(32 * kFwdWarps)
   __shared__ __align__(16) __nv_bfloat16 sW2[kH * kLd2];
   __shared__ float sB1[kH], sB2[kH], sW3[kH], sB3;
   __shared__ __align__(16) __nv_bfloat16 sEnc[kFwdWarps][16 * kEncLdB];
-  for (int e = threadIdx.x; e < kH * kLd1; e += blockDim.x) {
-    const int nn = e / kLd1, k = e % kLd1;
-    sW1[e] = __float2bfloat16_rn(k < kIn ? params[kW1 + k * kH + nn] : 0.0f);
+  // weights transposed into [n][k] (reads follow the [k][n] source, coalesced)
+  for (int e = threadIdx.x; e < kLd1 * kH; e += blockDim.x) {
+    const int k = e / kH, nn = e % kH;
+    sW1[nn * kLd1 + k] = __float2bfloat16_rn(k < kIn ? params[kW1 + k * kH + nn] : 0.0f);
   }
-  for (int e = threadIdx.x; e < kH * kLd2; e += blockDim.x) {
-    const int nn = e / kLd2, k = e % kLd2;
-    sW2[e] = __float2bfloat16_rn(k < kH ? params[kW2 + k * kH + nn] : 0.0f);
+  for (int e = threadIdx.x; e < kLd2 * kH; e += blockDim.x) {
+    const int k = e / kH, nn = e % kH;
+    sW2[nn * kLd2 + k] = __float2bfloat16_rn(k < kH ? params[kW2 + k * kH + nn] : 0.0f);
   }
   for (int j = threadIdx.x; j < kH; j += blockDim.x) {
     sB1[j] = params[kB1 + j];
@@ -365,7 +366,12 @@ int launch_proposal_forward(const float *params, const float *xyz, long long n, 
 
 int launch_proposal_forward_bf16(const float *params, const float *xyz, long long n, float *sigma,
                                  cudaStream_t stream) {
-  prop::prop_fwd_bf16_kernel<<<prop::grid_for(n, 16 * prop::kFwdWarps), 32 * prop::kFwdWarps, 0, stream>>>(
+  // persistent: two CTAs per SM, so that each converts the weights once for
+  // many 16-sample tiles
+  const long long tiles = (n + 16 * prop::kFwdWarps - 1) / (16 * prop::kFwdWarps);
+  const int sms = num_sms();
+  const long long cap = (long long)(sms > 0 ? sms : 148) * 2;
+  prop::prop_fwd_bf16_kernel<<<(unsigned)(tiles < cap ? tiles : cap), 32 * prop::kFwdWarps, 0, stream>>>(
       params, xyz, n, sigma);
   return launch_status();
 }
