@@ -142,6 +142,16 @@ int nerfgb_mlp_forward_mapped(const void *packed, int precision,
                               float *rgb, float *sigma, int *err_word,
                               void *stream);
 
+/* ---- ray generation ------------------------------------------------- */
+
+/* Replaces get_rays_tf (nerf/utils/ray_utils.py:53-106): rays_o, rays_d
+ * [H*W, 3] for pixel p = v*W + u of a pinhole camera, intrinsic [3,3] and
+ * c2w [4,4] row-major float32 device arrays. d = R (x, y, 1) with
+ * x = (u - cx)/fx, y = (v - cy)/fy, normalised by sqrt(d.d) + 1e-8; the
+ * rotation and the norm are sequential float32 sums. */
+int nerfgb_get_rays(int H, int W, const float *intrinsic, const float *c2w,
+                    float *rays_o, float *rays_d, void *stream);
+
 /* ---- uniforms -------------------------------------------------------- */
 
 /* Fills out[0..n) with uniforms in [0,1) from Philox4x32-10 keyed by seed;

@@ -401,6 +401,30 @@ __global__ void __launch_bounds__(32 * kFineWarps)
   }
 }
 
+// get_rays_tf (ray_utils.py:53-106): one thread per pixel p = v * W + u.
+// x = (u - cx) / fx, y = (v - cy) / fy, z = 1; d = R (x, y, z) as a
+// sequential three-term sum per component (TF leaves the matmul's order
+// open); d /= sqrt(d.d) + 1e-8 with d.d summed in order; o = c2w[:3, 3].
+// Plain IEEE float32 operations without contraction, as the oracle does.
+__global__ void get_rays_kernel(int H, int W, const float *__restrict__ K, const float *__restrict__ c2w,
+                                float *__restrict__ rays_o, float *__restrict__ rays_d) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (long long)H * W) return;
+  const float u = (float)(p % W), v = (float)(p / W);
+  const float x = fdiv(fsub(u, K[2]), K[0]);
+  const float y = fdiv(fsub(v, K[5]), K[4]);
+  float d[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) d[i] = fadd(fadd(fmul(x, c2w[4 * i]), fmul(y, c2w[4 * i + 1])), c2w[4 * i + 2]);
+  const float m = fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2]));
+  const float den = fadd(__fsqrt_rn(m), 1e-8f);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    rays_d[3 * p + i] = fdiv(d[i], den);
+    rays_o[3 * p + i] = c2w[4 * i + 3];
+  }
+}
+
 __global__ void uniform_kernel(unsigned long long seed, unsigned long long offset, long long n,
                                float *__restrict__ out) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -539,5 +563,15 @@ extern "C" int nerfgb_uniform(unsigned long long seed, unsigned long long offset
   if (n == 0) return NERFGB_OK;
   if (!out) return NERFGB_E_INVALID_ARG;
   uniform_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(seed, offset, n, out);
+  return launch_status();
+}
+
+extern "C" int nerfgb_get_rays(int H, int W, const float *intrinsic, const float *c2w, float *rays_o,
+                               float *rays_d, void *stream) {
+  if (H < 0 || W < 0) return NERFGB_E_INVALID_ARG;
+  const long long n = (long long)H * W;
+  if (n == 0) return NERFGB_OK;
+  if (!intrinsic || !c2w || !rays_o || !rays_d) return NERFGB_E_INVALID_ARG;
+  get_rays_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(H, W, intrinsic, c2w, rays_o, rays_d);
   return launch_status();
 }

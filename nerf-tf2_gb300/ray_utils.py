@@ -57,6 +57,19 @@ def uniform(shape):
     return _rng.draw(shape)
 
 
+def get_rays_tf(H, W, intrinsic, c2w):
+    """ray_utils.py:53-106 on the device: (rays_o, rays_d), each [H*W, 3]
+    float32, for the pinhole camera `intrinsic` [3,3] at pose `c2w` [4,4]
+    (numpy arrays or tensors). The 3x3 rotation and the norm are sequential
+    float32 sums."""
+    K = as_cuda(torch.as_tensor(intrinsic, dtype=torch.float32), shape=(3, 3), name="intrinsic")
+    T = as_cuda(torch.as_tensor(c2w, dtype=torch.float32), shape=(4, 4), name="c2w")
+    n = int(H) * int(W)
+    rays_o, rays_d = empty(n, 3), empty(n, 3)
+    _lib.call("nerfgb_get_rays", int(H), int(W), ptr(K), ptr(T), ptr(rays_o), ptr(rays_d), stream())
+    return rays_o, rays_d
+
+
 def create_input_batch_coarse_model(params, rays_o, rays_d, near, far, *, u_vals=None):
     """ray_utils.py:137-274. Returns {"xyz_inputs", "dir_inputs", "bin_data",
     "t_vals"}; bin_data holds "bin_edges", "left_edges", "right_edges",

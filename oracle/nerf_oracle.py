@@ -342,6 +342,22 @@ def get_rays(H, W, intrinsic, c2w):
     return o, d
 
 
+def get_rays_tf(H, W, intrinsic, c2w):
+    """ray_utils.py:53-106 in float32. The matmul (:96) and the reduce_sum
+    (:99) are sequential left-to-right sums without FMA (TF leaves their
+    order open); z = 1 makes the third product exact."""
+    K = np.asarray(intrinsic, F32)
+    T = np.asarray(c2w, F32)
+    u, v = np.meshgrid(np.arange(W, dtype=F32), np.arange(H, dtype=F32), indexing="xy")
+    x = ((u - K[0, 2]) / K[0, 0]).reshape(-1)                              # :86
+    y = ((v - K[1, 2]) / K[1, 1]).reshape(-1)                              # :87
+    d = np.stack([(x * T[i, 0] + y * T[i, 1]) + T[i, 2] for i in range(3)], -1)  # :94-96
+    m = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]       # :99
+    d = d / (np.sqrt(m) + F32(1e-8))[:, None]                              # :100
+    o = np.broadcast_to(T[:3, 3], d.shape)                                 # :103
+    return o, d
+
+
 # ---------------------------------------------------------------------------
 # Philox4x32-10 in numpy (Salmon et al., SC 2011), to check the library's
 # device uniforms: element e of the stream keyed by seed is output (e mod 4)

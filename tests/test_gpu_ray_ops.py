@@ -211,3 +211,16 @@ def test_uniforms_match_philox(ng, oracle, cuda):
     b = host(ng.ray_utils.uniform((5,)))
     assert np.array_equal(a.reshape(-1), oracle.philox_uniform(1234, 0, 37 * 64))
     assert np.array_equal(b, oracle.philox_uniform(1234, 37 * 64, 5))
+
+
+@pytest.mark.parametrize("H,W", [(800, 800), (7, 13), (1, 1)])
+def test_get_rays_bit_exact(ng, oracle, cuda, H, W):
+    """get_rays_tf (ray_utils.py:53-106) on the device, bit-exact against the
+    float32 restatement."""
+    K = ng.synthetic.intrinsic(H, W, 1111.111 * W / 800)
+    pose = ng.synthetic.random_pose(H * 31 + W)
+    o, d = ng.ray_utils.get_rays_tf(H, W, K, pose)
+    wo, wd = oracle.get_rays_tf(H, W, K, pose)
+    assert o.shape == (H * W, 3) and d.shape == (H * W, 3)
+    assert np.array_equal(host(d), wd)
+    assert np.array_equal(host(o), wo)

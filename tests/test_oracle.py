@@ -322,3 +322,17 @@ def test_gated_render_skips_gated_samples(oracle, ng):
     got, m_c, m_f, _ = oracle.nerf_render_gated(p, blob, pc, pf, o, d, n, f, uc, uf, 10.0, F64)
     assert not m_c.any() and m_f.sum() == 4 * 128
     assert np.all(got["weights"][~m_f] == 0)
+
+
+# --- ray generation ----------------------------------------------------------
+def test_get_rays_tf_matches_float64(oracle, ng):
+    """get_rays_tf (float32, ray_utils.py:53-106) against get_rays (float64,
+    :6-51): the same rays to float32 rounding."""
+    K = ng.synthetic.intrinsic(12, 17, 21.5)
+    pose = ng.synthetic.random_pose(4)
+    o32, d32 = oracle.get_rays_tf(12, 17, K, pose)
+    o64, d64 = oracle.get_rays(12, 17, K, pose)
+    assert o32.dtype == np.float32 and d32.shape == (12 * 17, 3)
+    np.testing.assert_allclose(d32, d64, atol=2e-6)
+    np.testing.assert_allclose(o32, o64, atol=1e-6)
+    np.testing.assert_allclose(np.linalg.norm(d32, axis=1), 1.0, atol=1e-6)
