@@ -152,6 +152,27 @@ int nerfgb_mlp_forward_mapped(const void *packed, int precision,
 int nerfgb_get_rays(int H, int W, const float *intrinsic, const float *c2w,
                     float *rays_o, float *rays_d, void *stream);
 
+/* Replaces the sample-mode map function (nerf/core/base_dataset.py:555-621)
+ * for one image: ray b of the batch is get_rays_tf's ray of pixel idxs[b]
+ * (device int32 [batch], drawn by the caller, e.g. nerfgb_uniform_int; the
+ * reference draws them with tf.random.uniform), with near/far and
+ * rgb = image / 255 (image: uint8 [H, W, 3] on the device). Outputs rays_o,
+ * rays_d, rgb [batch, 3], near_out, far_out [batch]. An index outside
+ * [0, H*W) yields zeros. */
+int nerfgb_sample_rays(const unsigned char *image, int H, int W,
+                       const float *intrinsic, const float *c2w, float near,
+                       float far, const int *idxs, int batch, float *rays_o,
+                       float *rays_d, float *near_out, float *far_out,
+                       float *rgb, void *stream);
+
+/* Replaces create_depth_map (nerf/utils/ray_utils.py:108-135): out [n] =
+ * pred_depth / scale_factor (map_type 1) or the camera-frame z of
+ * rays_o + rays_d * pred_depth / scale_factor under w2c [4,4] (map_type 2;
+ * the rays of the frame, e.g. from nerfgb_get_rays). */
+int nerfgb_depth_map(const float *pred_depth, long long n, float scale_factor,
+                     int map_type, const float *rays_o, const float *rays_d,
+                     const float *w2c, float *out, void *stream);
+
 /* ---- uniforms -------------------------------------------------------- */
 
 /* Fills out[0..n) with uniforms in [0,1) from Philox4x32-10 keyed by seed;
@@ -159,6 +180,11 @@ int nerfgb_get_rays(int H, int W, const float *intrinsic, const float *c2w,
  * jitter uniforms (the reference draws them with tf.random.uniform). */
 int nerfgb_uniform(unsigned long long seed, unsigned long long offset,
                    long long n, float *out, void *stream);
+
+/* Integers in [0, maxval): out[i] = (w * maxval) >> 32 for the 32-bit word
+ * w = offset + i of the same Philox4x32-10 stream. */
+int nerfgb_uniform_int(unsigned long long seed, unsigned long long offset,
+                       long long n, int maxval, int *out, void *stream);
 
 /* ---- fused render --------------------------------------------------- */
 

@@ -45,6 +45,9 @@ SIGNATURES = {
     "nerfgb_mlp_forward_mapped": (I, [P, I, P, P, LL, I, P, P, P, P, P, P]),
     "nerfgb_uniform": (I, [ULL, ULL, LL, P, P]),
     "nerfgb_get_rays": (I, [I, I, P, P, P, P, P]),
+    "nerfgb_sample_rays": (I, [P, I, I, P, P, F, F, P, I, P, P, P, P, P, P]),
+    "nerfgb_uniform_int": (I, [ULL, ULL, LL, I, P, P]),
+    "nerfgb_depth_map": (I, [P, LL, F, I, P, P, P, P, P]),
     "nerfgb_render_workspace_bytes": (LL, [I, I, I]),
     "nerfgb_render_rays": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
                                P, P, P, P, P, P, P, P, P]),

@@ -125,12 +125,16 @@ __device__ __forceinline__ uint4 philox4x32_10(uint4 ctr, uint2 key) {
 __device__ __forceinline__ float u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
 
 // Uniform for flat element index e of the stream keyed by seed.
-__device__ __forceinline__ float philox_uniform(unsigned long long seed, unsigned long long e) {
+// Word e of the stream keyed by seed: output (e mod 4) of counter (e div 4).
+__device__ __forceinline__ uint32_t philox_word(unsigned long long seed, unsigned long long e) {
   unsigned long long c = e >> 2;
   uint4 r = philox4x32_10(make_uint4((uint32_t)c, (uint32_t)(c >> 32), 0u, 0u),
                           make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)));
-  uint32_t w = (e & 3) == 0 ? r.x : (e & 3) == 1 ? r.y : (e & 3) == 2 ? r.z : r.w;
-  return u01(w);
+  return (e & 3) == 0 ? r.x : (e & 3) == 1 ? r.y : (e & 3) == 2 ? r.z : r.w;
+}
+
+__device__ __forceinline__ float philox_uniform(unsigned long long seed, unsigned long long e) {
+  return u01(philox_word(seed, e));
 }
 
 inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }

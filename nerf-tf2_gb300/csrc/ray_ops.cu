@@ -401,28 +401,92 @@ __global__ void __launch_bounds__(32 * kFineWarps)
   }
 }
 
-// get_rays_tf (ray_utils.py:53-106): one thread per pixel p = v * W + u.
-// x = (u - cx) / fx, y = (v - cy) / fy, z = 1; d = R (x, y, z) as a
-// sequential three-term sum per component (TF leaves the matmul's order
-// open); d /= sqrt(d.d) + 1e-8 with d.d summed in order; o = c2w[:3, 3].
-// Plain IEEE float32 operations without contraction, as the oracle does.
-__global__ void get_rays_kernel(int H, int W, const float *__restrict__ K, const float *__restrict__ c2w,
-                                float *__restrict__ rays_o, float *__restrict__ rays_d) {
-  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= (long long)H * W) return;
-  const float u = (float)(p % W), v = (float)(p / W);
+// get_rays_tf (ray_utils.py:53-106) for pixel (u, v): x = (u - cx) / fx,
+// y = (v - cy) / fy, z = 1; d = R (x, y, z) as a sequential three-term sum
+// per component (TF leaves the matmul's order open); d /= sqrt(d.d) + 1e-8
+// with d.d summed in order; o = c2w[:3, 3]. Plain IEEE float32 operations
+// without contraction, as the oracle does.
+__device__ __forceinline__ void pixel_ray(float u, float v, const float *__restrict__ K,
+                                          const float *__restrict__ c2w, float (&o)[3], float (&d)[3]) {
   const float x = fdiv(fsub(u, K[2]), K[0]);
   const float y = fdiv(fsub(v, K[5]), K[4]);
-  float d[3];
 #pragma unroll
   for (int i = 0; i < 3; ++i) d[i] = fadd(fadd(fmul(x, c2w[4 * i]), fmul(y, c2w[4 * i + 1])), c2w[4 * i + 2]);
   const float m = fadd(fadd(fmul(d[0], d[0]), fmul(d[1], d[1])), fmul(d[2], d[2]));
   const float den = fadd(__fsqrt_rn(m), 1e-8f);
 #pragma unroll
   for (int i = 0; i < 3; ++i) {
-    rays_d[3 * p + i] = fdiv(d[i], den);
-    rays_o[3 * p + i] = c2w[4 * i + 3];
+    d[i] = fdiv(d[i], den);
+    o[i] = c2w[4 * i + 3];
   }
+}
+
+// One thread per pixel p = v * W + u.
+__global__ void get_rays_kernel(int H, int W, const float *__restrict__ K, const float *__restrict__ c2w,
+                                float *__restrict__ rays_o, float *__restrict__ rays_d) {
+  const long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= (long long)H * W) return;
+  float o[3], d[3];
+  pixel_ray((float)(p % W), (float)(p / W), K, c2w, o, d);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    rays_d[3 * p + i] = d[i];
+    rays_o[3 * p + i] = o[i];
+  }
+}
+
+// Sample-mode batch (base_dataset.py:555-621): ray idxs[b] of the image's
+// get_rays_tf rays with near/far = bounds and rgb = image / 255 (uint8 HWC).
+// Indices outside [0, H*W) give a zero ray, zero rgb and bounds.
+__global__ void sample_rays_kernel(const unsigned char *__restrict__ img, int H, int W,
+                                   const float *__restrict__ K, const float *__restrict__ c2w, float near,
+                                   float far, const int *__restrict__ idxs, int B, float *__restrict__ rays_o,
+                                   float *__restrict__ rays_d, float *__restrict__ near_out,
+                                   float *__restrict__ far_out, float *__restrict__ rgb) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const long long p = idxs[b];
+  float o[3] = {0.f, 0.f, 0.f}, d[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
+  const bool in = p >= 0 && p < (long long)H * W;
+  if (in) {
+    pixel_ray((float)(p % W), (float)(p / W), K, c2w, o, d);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) c[i] = fdiv((float)img[3 * p + i], 255.0f);
+  }
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    rays_o[3 * b + i] = o[i];
+    rays_d[3 * b + i] = d[i];
+    rgb[3 * b + i] = c[i];
+  }
+  near_out[b] = in ? near : 0.0f;
+  far_out[b] = in ? far : 0.0f;
+}
+
+// Uniform integers in [0, maxval): (word * maxval) >> 32 of the Philox
+// stream's words offset .. offset + n - 1.
+__global__ void uniform_int_kernel(unsigned long long seed, unsigned long long offset, long long n, int maxval,
+                                   int *__restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = (int)(((unsigned long long)philox_word(seed, offset + (unsigned long long)i) * (unsigned)maxval) >> 32);
+}
+
+// create_depth_map (ray_utils.py:108-135): type 1 = depth * (1 / scale);
+// type 2 = the camera-frame z of o + d * depth * (1 / scale) under w2c.
+__global__ void depth_map_kernel(const float *__restrict__ depth, long long n, float inv_scale, int type,
+                                 const float *__restrict__ rays_o, const float *__restrict__ rays_d,
+                                 const float *__restrict__ w2c, float *__restrict__ out) {
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float ds = fmul(depth[i], inv_scale);
+  if (type == 1) {
+    out[i] = ds;
+    return;
+  }
+  float z = w2c[11];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) z = fadd(z, fmul(w2c[8 + k], fadd(rays_o[3 * i + k], fmul(rays_d[3 * i + k], ds))));
+  out[i] = z;
 }
 
 __global__ void uniform_kernel(unsigned long long seed, unsigned long long offset, long long n,
@@ -573,5 +637,39 @@ extern "C" int nerfgb_get_rays(int H, int W, const float *intrinsic, const float
   if (n == 0) return NERFGB_OK;
   if (!intrinsic || !c2w || !rays_o || !rays_d) return NERFGB_E_INVALID_ARG;
   get_rays_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(H, W, intrinsic, c2w, rays_o, rays_d);
+  return launch_status();
+}
+
+extern "C" int nerfgb_sample_rays(const unsigned char *image, int H, int W, const float *intrinsic,
+                                  const float *c2w, float near, float far, const int *idxs, int batch,
+                                  float *rays_o, float *rays_d, float *near_out, float *far_out, float *rgb,
+                                  void *stream) {
+  if (H < 0 || W < 0 || batch < 0) return NERFGB_E_INVALID_ARG;
+  if (batch == 0) return NERFGB_OK;
+  if (!image || !intrinsic || !c2w || !idxs || !rays_o || !rays_d || !near_out || !far_out || !rgb)
+    return NERFGB_E_INVALID_ARG;
+  sample_rays_kernel<<<(batch + 255) / 256, 256, 0, as_stream(stream)>>>(image, H, W, intrinsic, c2w, near, far,
+                                                                          idxs, batch, rays_o, rays_d, near_out,
+                                                                          far_out, rgb);
+  return launch_status();
+}
+
+extern "C" int nerfgb_uniform_int(unsigned long long seed, unsigned long long offset, long long n, int maxval,
+                                  int *out, void *stream) {
+  if (n < 0 || maxval < 1) return NERFGB_E_INVALID_ARG;
+  if (n == 0) return NERFGB_OK;
+  if (!out) return NERFGB_E_INVALID_ARG;
+  uniform_int_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(seed, offset, n, maxval, out);
+  return launch_status();
+}
+
+extern "C" int nerfgb_depth_map(const float *pred_depth, long long n, float scale_factor, int map_type,
+                                const float *rays_o, const float *rays_d, const float *w2c, float *out,
+                                void *stream) {
+  if (n < 0 || (map_type != 1 && map_type != 2) || !(scale_factor != 0.0f)) return NERFGB_E_INVALID_ARG;
+  if (n == 0) return NERFGB_OK;
+  if (!pred_depth || !out || (map_type == 2 && (!rays_o || !rays_d || !w2c))) return NERFGB_E_INVALID_ARG;
+  depth_map_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(pred_depth, n, 1.0f / scale_factor, map_type,
+                                                                    rays_o, rays_d, w2c, out);
   return launch_status();
 }

@@ -345,6 +345,23 @@ class NeRF:
                       ptr(self.coarse_model.err_word), stream())
         return out
 
+    def render_frame(self, H, W, intrinsic, c2w, bounds=(2.0, 6.0), **render_kw):
+        """One image of the render loop (nerf/main/render.py:79-97): the
+        frame's rays from the pinhole camera on the device
+        (ray_utils.get_rays_tf), near/far = `bounds`, NeRF.render in chunks
+        (keyword arguments pass through), and the maps as images: "rgb"
+        [H,W,3], "depth" and "acc" [H,W], and "image_u8" [H,W,3] =
+        clip(rgb * 255, 0, 255) truncated to uint8 (render.py:96-97)."""
+        rays_o, rays_d = ray_utils.get_rays_tf(H, W, intrinsic, c2w)
+        n = rays_o.shape[0]
+        near = torch.full((n, 1), float(bounds[0]), device=rays_o.device)
+        far = torch.full((n, 1), float(bounds[1]), device=rays_o.device)
+        out = self.render(rays_o, rays_d, near, far, **render_kw)
+        frame = {"rgb": out["rgb"].reshape(H, W, 3), "depth": out["depth"].reshape(H, W),
+                 "acc": out["acc"].reshape(H, W)}
+        frame["image_u8"] = (frame["rgb"] * 255.0).clamp(0.0, 255.0).to(torch.uint8)
+        return frame
+
 
 def psnr(y_true, y_pred):
     """nerf/core/ops.py:249-257: per-element PSNR in dB (float64)."""

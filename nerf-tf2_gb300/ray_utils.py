@@ -70,6 +70,62 @@ def get_rays_tf(H, W, intrinsic, c2w):
     return rays_o, rays_d
 
 
+def sample_mode_batch(img, pose, bounds, intrinsic, batch_size, *, idxs=None, seed=0):
+    """base_dataset.py:555-621 (the sample-mode map function) for one image
+    on the device: ((rays_o, rays_d, near, far), (rgb,)) for batch_size rays
+    drawn uniformly with replacement among the image's H*W. ``img`` is uint8
+    [H, W, 3]; ``idxs`` (int32 [batch_size]) replaces the reference's
+    tf.random.uniform draw, else it comes from the Philox stream keyed by
+    ``seed``."""
+    img = torch.as_tensor(img)
+    if img.dtype != torch.uint8 or img.dim() != 3 or img.shape[2] != 3:
+        raise ValueError("img must be a uint8 [H, W, 3] array")
+    img = img.to(device="cuda").contiguous()
+    H, W = int(img.shape[0]), int(img.shape[1])
+    K = as_cuda(torch.as_tensor(intrinsic, dtype=torch.float32), shape=(3, 3), name="intrinsic")
+    T = as_cuda(torch.as_tensor(pose, dtype=torch.float32), shape=(4, 4), name="pose")
+    B = int(batch_size)
+    if idxs is None:
+        idxs = torch.empty(B, dtype=torch.int32, device="cuda")
+        _lib.call("nerfgb_uniform_int", ctypes.c_ulonglong(int(seed)), ctypes.c_ulonglong(0), B, H * W,
+                  ptr(idxs), stream())
+    else:
+        idxs = as_cuda(idxs, dtype=torch.int32, shape=(B,), name="idxs")
+    rays_o, rays_d, rgb = empty(B, 3), empty(B, 3), empty(B, 3)
+    near, far = empty(B, 1), empty(B, 1)
+    _lib.call("nerfgb_sample_rays", ptr(img), H, W, ptr(K), ptr(T), ctypes.c_float(float(bounds[0])),
+              ctypes.c_float(float(bounds[1])), ptr(idxs), B, ptr(rays_o), ptr(rays_d), ptr(near), ptr(far),
+              ptr(rgb), stream())
+    return (rays_o, rays_d, near, far), (rgb,)
+
+
+def create_depth_map(pred_depth, H, W, scale_factor, map_type, intrinsic=None, C_to_W2=None):
+    """ray_utils.py:108-135 on the device: "type_1" = pred_depth /
+    scale_factor as [H, W]; "type_2" = the camera-frame z of the depth
+    points along get_rays_tf's rays (float32; the reference computes it in
+    float64 with NumPy)."""
+    d = as_cuda(pred_depth, name="pred_depth").reshape(-1)
+    n = int(H) * int(W)
+    if d.numel() != n:
+        raise ValueError(f"pred_depth has {d.numel()} values, H*W = {n}")
+    out = empty(n)
+    if map_type == "type_1":
+        _lib.call("nerfgb_depth_map", ptr(d), n, ctypes.c_float(float(scale_factor)), 1, None, None, None,
+                  ptr(out), stream())
+    elif map_type == "type_2":
+        if intrinsic is None or C_to_W2 is None:
+            raise ValueError("type_2 needs intrinsic and C_to_W2")
+        rays_o, rays_d = get_rays_tf(H, W, intrinsic, C_to_W2)
+        import numpy as np
+        w2c = as_cuda(torch.as_tensor(np.linalg.inv(np.asarray(C_to_W2, np.float64)), dtype=torch.float32),
+                      shape=(4, 4), name="w2c")
+        _lib.call("nerfgb_depth_map", ptr(d), n, ctypes.c_float(float(scale_factor)), 2, ptr(rays_o),
+                  ptr(rays_d), ptr(w2c), ptr(out), stream())
+    else:
+        raise ValueError(f"Invalid map_type: {map_type}")
+    return out.reshape(int(H), int(W))
+
+
 def create_input_batch_coarse_model(params, rays_o, rays_d, near, far, *, u_vals=None):
     """ray_utils.py:137-274. Returns {"xyz_inputs", "dir_inputs", "bin_data",
     "t_vals"}; bin_data holds "bin_edges", "left_edges", "right_edges",

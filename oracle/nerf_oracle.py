@@ -358,6 +358,31 @@ def get_rays_tf(H, W, intrinsic, c2w):
     return o, d
 
 
+def sample_mode_batch(img, pose, bounds, intrinsic, idxs):
+    """base_dataset.py:555-621 with the indices supplied (the reference
+    draws them with tf.random.uniform at :605-608)."""
+    H, W = img.shape[:2]
+    o, d = get_rays_tf(H, W, intrinsic, pose)                               # :589-591
+    rgb = img.reshape(-1, 3).astype(F32) / F32(255.0)                      # :595-597
+    n = o.shape[0]
+    near = np.full((n, 1), bounds[0], F32)
+    far = np.full((n, 1), bounds[1], F32)                                  # :599-602
+    i = np.asarray(idxs)
+    return (o[i], d[i], near[i], far[i]), (rgb[i],)                        # :610-614
+
+
+def create_depth_map(pred_depth, H, W, scale_factor, map_type, intrinsic=None, C_to_W2=None):
+    """ray_utils.py:108-135 (float64, NumPy get_rays)."""
+    ds = np.asarray(pred_depth, F64) * (1 / scale_factor)                 # :117
+    if map_type == "type_1":
+        return ds.reshape(H, W)                                            # :120
+    o, d = get_rays(H, W, np.asarray(intrinsic, F64), np.asarray(C_to_W2, F64))  # :123
+    pts = o + d * ds[:, None]                                              # :124
+    w2c = np.linalg.inv(np.asarray(C_to_W2, F64))                          # :126
+    cam = pts @ w2c[:3, :3].T + w2c[:3, 3]                                 # :127
+    return cam[:, 2].reshape(H, W)                                         # :129-130
+
+
 # ---------------------------------------------------------------------------
 # Philox4x32-10 in numpy (Salmon et al., SC 2011), to check the library's
 # device uniforms: element e of the stream keyed by seed is output (e mod 4)
@@ -381,15 +406,26 @@ def philox4x32_10(x0, x1, x2, x3, k0, k1):
     return x0, x1, x2, x3
 
 
-def philox_uniform(seed, offset, n):
+def philox_words(seed, offset, n):
+    """Words offset .. offset + n - 1 of the stream keyed by seed (uint32)."""
     e = np.arange(offset, offset + n, dtype=np.uint64)
     c = e >> np.uint64(2)
     lo = (c & np.uint64(0xFFFFFFFF)).astype(np.uint32)
     hi = (c >> np.uint64(32)).astype(np.uint32)
     z = np.zeros_like(lo)
     words = np.stack(philox4x32_10(lo, hi, z, z, seed & 0xFFFFFFFF, (seed >> 32) & 0xFFFFFFFF), axis=1)
-    w = words[np.arange(n), (e & np.uint64(3)).astype(np.int64)]
+    return words[np.arange(n), (e & np.uint64(3)).astype(np.int64)]
+
+
+def philox_uniform(seed, offset, n):
+    w = philox_words(seed, offset, n)
     return (w >> np.uint32(8)).astype(np.float32) * np.float32(1.0 / 16777216.0)
+
+
+def philox_uniform_int(seed, offset, n, maxval):
+    """Integers in [0, maxval): (word * maxval) >> 32."""
+    w = philox_words(seed, offset, n).astype(np.uint64)
+    return ((w * np.uint64(maxval)) >> np.uint64(32)).astype(np.int32)
 
 
 # ---------------------------------------------------------------------------

@@ -6,6 +6,8 @@ IEEE arithmetic only (sampling, CDF, inverse transform, sort), are compared
 bit-exactly. Transcendental results (exp, sin, cos) are compared within the
 tolerances written in each test.
 """
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -224,3 +226,57 @@ def test_get_rays_bit_exact(ng, oracle, cuda, H, W):
     assert o.shape == (H * W, 3) and d.shape == (H * W, 3)
     assert np.array_equal(host(d), wd)
     assert np.array_equal(host(o), wo)
+
+
+def test_sample_mode_batch_bit_exact(ng, oracle, cuda):
+    """The sample-mode map function (base_dataset.py:555-621) on the device
+    with supplied indices, bit-exact: rays, bounds, rgb = img / 255; an
+    out-of-range index gives zeros."""
+    H, W, B = 30, 50, 777
+    rng = np.random.default_rng(2)
+    img = rng.integers(0, 256, (H, W, 3), dtype=np.uint8)
+    K = ng.synthetic.intrinsic(H, W, 41.0)
+    pose = ng.synthetic.random_pose(8)
+    idxs = rng.integers(0, H * W, B).astype(np.int32)
+    idxs[:3] = [0, H * W - 1, W]
+    (o, d, n, f), (rgb,) = ng.ray_utils.sample_mode_batch(img, pose, (2.0, 6.0), K, B, idxs=idxs)
+    (wo, wd, wn, wf), (wrgb,) = oracle.sample_mode_batch(img, pose, (2.0, 6.0), K, idxs)
+    for got, want in ((o, wo), (d, wd), (n, wn), (f, wf), (rgb, wrgb)):
+        assert np.array_equal(host(got), want)
+    bad = idxs.copy()
+    bad[5] = -1
+    bad[6] = H * W
+    (o2, d2, n2, f2), (rgb2,) = ng.ray_utils.sample_mode_batch(img, pose, (2.0, 6.0), K, B, idxs=bad)
+    assert not host(d2)[5:7].any() and not host(rgb2)[5:7].any() and not host(n2)[5:7].any()
+
+
+def test_uniform_int_matches_philox(ng, oracle, cuda):
+    """Indices drawn from the library's Philox stream: (word * maxval) >> 32
+    of the same words as the float uniforms, in [0, maxval)."""
+    n, maxval, seed, off = 10001, 640000, 1234, 8
+    out = torch.empty(n, dtype=torch.int32, device="cuda")
+    ng._lib.call("nerfgb_uniform_int", ctypes.c_ulonglong(seed), ctypes.c_ulonglong(off), n, maxval,
+                 out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    want = oracle.philox_uniform_int(seed, off, n, maxval)
+    got = host(out)
+    assert np.array_equal(got, want)
+    assert got.min() >= 0 and got.max() < maxval
+    (o, d, _, _), _ = ng.ray_utils.sample_mode_batch(np.zeros((800, 800, 3), np.uint8), ng.synthetic.random_pose(1),
+                                                       (2.0, 6.0), ng.synthetic.intrinsic(), 4096, seed=7)
+    assert torch.isfinite(d).all() and o.shape == (4096, 3)
+
+
+@pytest.mark.parametrize("map_type", ["type_1", "type_2"])
+def test_create_depth_map(ng, oracle, cuda, map_type):
+    """create_depth_map (ray_utils.py:108-135): type_1 to float32 rounding,
+    type_2 (float32 rays and points against the reference's float64) within
+    2e-5 relative."""
+    H, W = 20, 31
+    rng = np.random.default_rng(4)
+    depth = rng.uniform(2.0, 6.0, H * W).astype(F32)
+    K = ng.synthetic.intrinsic(H, W, 27.0)
+    pose = ng.synthetic.random_pose(9)
+    got = host(ng.ray_utils.create_depth_map(dev(depth), H, W, 0.5, map_type, intrinsic=K, C_to_W2=pose))
+    want = oracle.create_depth_map(depth, H, W, 0.5, map_type, intrinsic=K, C_to_W2=pose)
+    assert got.shape == (H, W)
+    np.testing.assert_allclose(got, want, rtol=2e-5, atol=2e-5)

@@ -78,3 +78,24 @@ def test_render_default_uniforms_deterministic(ng, cuda, case):
     c = nerf.render(dev(o), dev(d), dev(n), dev(f), seed=8)
     assert torch.equal(a["rgb"], b["rgb"])
     assert not torch.equal(a["rgb"], c["rgb"])
+
+
+def test_render_frame_is_render_of_device_rays(ng, cuda):
+    """NeRF.render_frame (the render loop, nerf/main/render.py:79-97) equals
+    NeRF.render on get_rays_tf's rays, and its uint8 image is the clipped,
+    truncated rgb."""
+    H, W = 24, 40
+    K = ng.synthetic.intrinsic(H, W, 33.3)
+    pose = ng.synthetic.random_pose(5)
+    nerf = ng.NeRF(ng.make_params(), precision="bf16", coarse_params=ng.weights.glorot_blob(1),
+                   fine_params=ng.weights.glorot_blob(2))
+    fr = nerf.render_frame(H, W, K, pose, bounds=(2.0, 6.0), seed=3, chunk=256)
+    o, d = ng.ray_utils.get_rays_tf(H, W, K, pose)
+    n = o.shape[0]
+    ref = nerf.render(o, d, torch.full((n, 1), 2.0, device="cuda"), torch.full((n, 1), 6.0, device="cuda"),
+                      seed=3, chunk=256)
+    assert fr["rgb"].shape == (H, W, 3) and fr["depth"].shape == (H, W)
+    assert torch.equal(fr["rgb"].reshape(-1, 3), ref["rgb"])
+    assert torch.equal(fr["depth"].reshape(-1), ref["depth"])
+    img = np.clip(host(ref["rgb"]) * 255.0, 0.0, 255.0).astype(np.uint8).reshape(H, W, 3)
+    assert np.array_equal(host(fr["image_u8"]), img)
