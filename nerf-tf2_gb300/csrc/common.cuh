@@ -65,10 +65,25 @@ constexpr long long kFp32PackBytes = (kGemmWElems + kTableElems) * 4;
 
 // BF16 pack: per GEMM layer, K chunks of 32; chunk (n, k) byte offset
 // (k/8)*(N*16) + n*16 + (k%8)*2 (K-major core matrices, no swizzle). Then
-// the fp32 table at a 1 KB aligned offset.
+// the fp32 table at a 1 KB aligned offset, then the same weights in the
+// CTA-pair layout (pair_w_byte).
 constexpr long long kBf16WBytes = kGemmWElems * 2;
 constexpr long long kBf16TableOff = (kBf16WBytes + 1023) / 1024 * 1024;  // bytes
-constexpr long long kBf16PackBytes = kBf16TableOff + (long long)kTableElems * 4;
+
+// CTA-pair layout, for the 2-SM MMA in which each CTA of a pair holds one
+// N-half of every weight chunk: per GEMM layer, chunks of kPairKch K-rows
+// (the last may be shorter, kc rows); per chunk N-half 0 then N-half 1, each
+// (k/8)*(N/2*16) + n'*16 + (k%8)*2 with n' = n mod N/2, so that a CTA's half
+// of a chunk is one contiguous copy.
+constexpr int kPairKch = 64;
+constexpr long long kBf16PairOff = (kBf16TableOff + (long long)kTableElems * 4 + 1023) / 1024 * 1024;
+constexpr long long kBf16PackBytes = kBf16PairOff + kBf16WBytes;
+NG_HD long long pair_w_byte(int g, int k, int n) {
+  const int N = gemm_n(g), H = N / 2, c = k / kPairKch, kk = k % kPairKch;
+  const int kc = gemm_kp(g) - c * kPairKch < kPairKch ? gemm_kp(g) - c * kPairKch : kPairKch;
+  return kBf16PairOff + gemm_w_offset(g) * 2 + (long long)c * (kPairKch * N * 2) + (long long)(n / H) * (kc * H * 2) +
+         (kk / 8) * (H * 16) + (n % H) * 16 + (kk % 8) * 2;
+}
 
 // Stored activations of one row for training (floats): enc_xyz [64] | h0..h7
 // [8 x 256] | bottleneck [256] | enc_dir [32] | h9 [128].

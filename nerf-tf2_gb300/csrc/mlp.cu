@@ -41,6 +41,7 @@ __global__ void pack_kernel(const float *__restrict__ flat, int precision, unsig
       long long byte = gemm_w_offset(g) * 2 + (long long)c * (32 * N * 2) + (kk >> 3) * (N * 16) + n * 16 +
                        (kk & 7) * 2;
       *reinterpret_cast<__nv_bfloat16 *>(out + byte) = __float2bfloat16_rn(v);
+      *reinterpret_cast<__nv_bfloat16 *>(out + pair_w_byte(g, k, n)) = __float2bfloat16_rn(v);
     }
     return;
   }
