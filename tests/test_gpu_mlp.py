@@ -86,6 +86,27 @@ def test_mlp_bf16_vs_fp64(ng, oracle, cuda, n):
     assert np.abs(host(rgb) - r64).mean() < 3e-3
 
 
+def test_mlp_bf16_many_tiles(ng, oracle, cuda):
+    """200,003 rows: several 512-row tiles per CTA pair of the persistent
+    kernel (and a ragged last tile). Every row is computed the same way
+    wherever it lands (tile, pair CTA, sub-tile): a row permutation permutes
+    the outputs bit for bit; sampled rows match the fp64 oracle."""
+    n = 200003
+    blob = biased_blob(ng, 21)
+    x, d = samples(n, 23)
+    mlp = ng.get_coarse_or_fine_model("fine", params=blob, precision="bf16")
+    rgb, sigma = mlp((dev(x), dev(d)))
+    perm = np.random.default_rng(5).permutation(n)
+    rgb_p, sigma_p = mlp((dev(x[perm]), dev(d[perm])))
+    mlp.check_device_errors()
+    pt = torch.from_numpy(perm).cuda()
+    assert torch.equal(rgb_p, rgb[pt]) and torch.equal(sigma_p, sigma[pt])
+    rows = np.concatenate([np.random.default_rng(6).choice(n, 250, replace=False), [0, n - 1]])
+    r64, s64 = oracle.mlp_forward(oracle.unpack_params(blob, F64), x[rows], d[rows], F64)
+    assert np.abs(host(rgb)[rows] - r64).max() < 2e-2
+    assert np.abs(host(sigma)[rows] - s64).max() / max(1.0, np.abs(s64).max()) < 5e-2
+
+
 @pytest.mark.parametrize("n", [4097, 300])
 def test_mlp_fp8_vs_fp64(ng, oracle, cuda, n):
     """FP8-e4m3 operands (3 mantissa bits) with per-output-channel weight
