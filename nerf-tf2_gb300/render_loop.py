@@ -13,6 +13,7 @@ import zlib
 import numpy as np
 
 from . import ray_utils
+from .synthetic import _normalize
 
 # render.py:28-31
 SUBDIRS = ("rgb", "acc_map", "depth_type_1", "depth_type_2")
@@ -44,6 +45,39 @@ def write_png(path, image):
            _png_chunk(b"IDAT", zlib.compress(raw, 6)) + _png_chunk(b"IEND", b""))
     with open(path, "wb") as f:
         f.write(png)
+
+
+def create_spherical_path(radius, inclination, num_cameras, manual_rotation=None):
+    """The render loop's cameras (pose_utils.py:770-840): num_cameras
+    camera-to-world poses [N, 4, 4] (float64) on a sphere of `radius` about
+    the origin, at `inclination` degrees from +z and azimuths evenly spaced
+    over [0, 360) degrees. Each camera's z axis points at the origin, its x
+    axis along the azimuthal direction, y = z x x. `manual_rotation`: None,
+    or the path of a .npy 3x3 rotation applied to every pose (rotation @
+    pose)."""
+    az = np.radians(np.linspace(0, 360, num_cameras, endpoint=False, dtype=np.float64))
+    inc = np.radians(np.full_like(az, inclination))
+    r = np.full_like(az, radius)
+    origins = np.stack([r * np.sin(inc) * np.cos(az), r * np.sin(inc) * np.sin(az), r * np.cos(inc)], axis=1)
+    z = _normalize(-1 * origins)
+    x = _normalize(np.stack([-1 * r * np.sin(inc) * np.sin(az), r * np.sin(inc) * np.cos(az), np.zeros_like(az)],
+                            axis=1))
+    y = _normalize(np.cross(z, x))
+    poses = np.zeros((num_cameras, 4, 4), dtype=np.float64)
+    poses[:, :3, 0], poses[:, :3, 1], poses[:, :3, 2], poses[:, :3, 3] = x, y, z, origins
+    poses[:, 3, 3] = 1.0
+    if manual_rotation is not None:
+        transform = np.eye(4, dtype=np.float64)
+        transform[:3, :3] = np.load(manual_rotation)
+        poses = transform @ poses
+    return poses
+
+
+def default_bounds(radius):
+    """render.py:64-71: without configured bounds, near and far are 25 % and
+    75 % of the sphere's diameter."""
+    diameter = 2 * radius
+    return (0.25 * diameter, 0.75 * diameter)
 
 
 def render_name(i, num_cameras):

@@ -126,3 +126,34 @@ def test_render_cameras_files(ng, tmp_path, monkeypatch):
         np.testing.assert_array_equal(d1, (fr["depth"] / 0.25).numpy())
         np.testing.assert_array_equal(d2, (fr["depth"] * 0.5).numpy())
         np.testing.assert_array_equal(acc, fr["acc"].numpy())
+
+
+@pytest.mark.parametrize("n,inc", [(1, 60.0), (7, 45.0), (40, 80.0)])
+def test_create_spherical_path(ng, tmp_path, n, inc):
+    """pose_utils.py:770-840: the same pose as synthetic.look_at_pose per
+    camera; cameras on the sphere, looking at the origin, right-handed
+    orthonormal frames (to the 1e-8 of the reference's normalisation),
+    azimuths 360/n degrees apart; the manual rotation left-multiplies every
+    pose."""
+    rl = importlib.import_module("nerf-tf2_gb300.render_loop")
+    poses = rl.create_spherical_path(4.0, inc, n)
+    assert poses.shape == (n, 4, 4) and poses.dtype == np.float64
+    for i in range(n):
+        want = ng.synthetic.look_at_pose(np.radians(360.0 * i / n), np.radians(inc), 4.0)
+        np.testing.assert_allclose(poses[i], want, rtol=0, atol=1e-14)
+        R, t = poses[i, :3, :3], poses[i, :3, 3]
+        # unit to within the reference's normalisation epsilon (|v| + 1e-8)
+        np.testing.assert_allclose(R.T @ R, np.eye(3), rtol=0, atol=1e-7)
+        assert abs(np.linalg.det(R) - 1.0) < 1e-7
+        np.testing.assert_allclose(np.linalg.norm(t), 4.0, rtol=1e-15)
+        np.testing.assert_allclose(R[:, 2], -t / np.linalg.norm(t), atol=1e-8)
+        np.testing.assert_allclose(np.degrees(np.arccos(t[2] / 4.0)), inc, atol=1e-9)
+    assert np.array_equal(poses[:, 3], np.tile([0.0, 0.0, 0.0, 1.0], (n, 1)))
+    c, s_ = np.cos(0.3), np.sin(0.3)
+    rot = np.array([[c, -s_, 0.0], [s_, c, 0.0], [0.0, 0.0, 1.0]])
+    np.save(tmp_path / "rot.npy", rot)
+    turned = rl.create_spherical_path(4.0, inc, n, manual_rotation=str(tmp_path / "rot.npy"))
+    T = np.eye(4)
+    T[:3, :3] = rot
+    np.testing.assert_array_equal(turned, T @ poses)
+    assert rl.default_bounds(4.0) == (2.0, 6.0)
