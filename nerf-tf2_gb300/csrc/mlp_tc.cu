@@ -721,9 +721,13 @@ __global__ void __launch_bounds__(kThreads, 1)
   volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + kAbort);
   // Tiles: this CTA (or pair) takes first, first + step, ...; rank = the
   // CTA's place in its pair (its rows follow the even CTA's 256).
+  // (Single CTA: blockIdx.x and gridDim.x, read at each use rather than
+  // kept live across the roles' code.)
   const uint32_t crank = PAIR ? cluster_rank() : 0u;
-  const long long t_first = PAIR ? (long long)cluster_id() : (long long)blockIdx.x;
-  const long long t_step = PAIR ? (long long)cluster_count() : (long long)gridDim.x;
+  const long long pair_first = PAIR ? (long long)cluster_id() : 0ll;
+  const long long pair_step = PAIR ? (long long)cluster_count() : 0ll;
+#define t_first (PAIR ? pair_first : (long long)blockIdx.x)
+#define t_step (PAIR ? pair_step : (long long)gridDim.x)
   constexpr long long kTabOff = F8 ? kFp8TableOff : kBf16TableOff;
   const float *table = TSMEM ? reinterpret_cast<const float *>(smem + L::kTableOff)
                              : reinterpret_cast<const float *>(packed + kTabOff);
@@ -840,10 +844,12 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ok = false;
                 break;
               }
-              uint32_t bytes;
-              const uint8_t *src = chunk_src(g, c, bytes);
+              const int N = gemm_n(g), Kp = gemm_kp(g);
+              const int kc = Kp - c * KCH < KCH ? Kp - c * KCH : KCH;
+              const uint32_t bytes = (uint32_t)N * kc * kE;
               mbar_expect_tx(full, bytes);
-              bulk_g2s(sbase + kRingOff + st * kStageBytes, src, bytes, full);
+              bulk_g2s(sbase + kRingOff + st * kStageBytes, packed + gemm_w_offset(g) * kE + (long long)c * KCH * N * kE,
+                       bytes, full);
               issued = true;
               phase ^= 1;
             }
@@ -1328,6 +1334,8 @@ __global__ void __launch_bounds__(kThreads, 1)
     else
       asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
   }
+#undef t_first
+#undef t_step
 }
 
 }  // namespace tc
