@@ -16,9 +16,10 @@ import ctypes
 
 import torch
 
-from . import _lib, ray_utils
+from . import _lib, h5, ray_utils
 from ._tensors import as_cuda, device, empty, ptr, stream
 from .weights import PARAM_COUNT, from_dict, glorot_blob, to_dict
+from .weights import from_keras_layers as weights_from_keras
 
 PRECISIONS = {"fp32": _lib.PREC_FP32, "bf16": _lib.PREC_BF16, "fp8": _lib.PREC_FP8}
 
@@ -80,6 +81,12 @@ class NerfMLP:
         blob = from_dict(d, self.name)
         self.params.copy_(torch.from_numpy(blob))
         self.mark_updated()
+
+    def load_weights(self, path):
+        """Keras's Model.load_weights for an HDF5 weight file written by the
+        reference (nerf/core/ops.py:142-143): layers matched in order, kernel
+        and bias per layer (h5.py reads the file without h5py)."""
+        self.set_weights(weights_from_keras(h5.keras_layer_weights(path), self.name))
 
     # -- forward -------------------------------------------------------------
     def __call__(self, inputs, *, precision=None, rows_per_dir=1):
@@ -344,6 +351,16 @@ class NeRF:
                       ptr(out["rgb"][sl]), ptr(out["depth"][sl]), ptr(out["acc"][sl]), ptr(ws),
                       ptr(self.coarse_model.err_word), stream())
         return out
+
+    def load_model(self, load_dir, load_tag):
+        """nerf/core/model.py:278-287: the coarse and fine networks' weights
+        from <load_dir>/<load_tag>_coarse.h5 and <load_tag>_fine.h5 (the
+        files the reference's checkpoint callback writes, ops.py:131-143).
+        The optimizer state (<load_tag>_optimizer.npz, model.py:246-276) is
+        not read: its Keras slot-variable names cannot be checked here."""
+        import os
+        self.coarse_model.load_weights(os.path.join(load_dir, f"{load_tag}_coarse.h5"))
+        self.fine_model.load_weights(os.path.join(load_dir, f"{load_tag}_fine.h5"))
 
     def render_frame(self, H, W, intrinsic, c2w, bounds=(2.0, 6.0), **render_kw):
         """One image of the render loop (nerf/main/render.py:79-97): the

@@ -55,3 +55,24 @@ def from_dict(d, model_name="coarse"):
         parts.append(np.asarray(d[f"{model_name}/{name}/kernel:0"], np.float32).reshape(-1))
         parts.append(np.asarray(d[f"{model_name}/{name}/bias:0"], np.float32).reshape(-1))
     return np.concatenate(parts)
+
+
+def from_keras_layers(layers, model_name="coarse"):
+    """Weights read from a Keras weight file (h5.keras_layer_weights:
+    [(layer name, [(weight name, array), ...]), ...]) ->
+    {"<model>/<layer>/kernel:0": ..., ...}. As Keras's load_weights does for
+    an HDF5 file (by topology, not by name), the file's layers that hold
+    weights are matched in order to the network's (dense_0..7, sigma,
+    dense_8, dense_9, rgb), each as [kernel, bias]; shapes must agree."""
+    if len(layers) != len(LAYERS):
+        raise ValueError(f"the file has {len(layers)} layers with weights, the network has {len(LAYERS)}")
+    d = {}
+    for (lname, ws), (name, i, o) in zip(layers, LAYERS):
+        if len(ws) != 2:
+            raise ValueError(f"layer {lname}: {len(ws)} weights, expected kernel and bias")
+        (_, k), (_, b) = ws
+        if tuple(k.shape) != (i, o) or tuple(b.shape) != (o,):
+            raise ValueError(f"layer {lname}: shapes {tuple(k.shape)}, {tuple(b.shape)}; expected ({i}, {o}), ({o},)")
+        d[f"{model_name}/{name}/kernel:0"] = np.asarray(k, np.float32)
+        d[f"{model_name}/{name}/bias:0"] = np.asarray(b, np.float32)
+    return d
