@@ -8,8 +8,12 @@
  *    Tensors are dense, row-major, float32 (int32 for indices).
  *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
  *    stream). Every call is enqueued on it and returns without a host sync.
- *  - The caller allocates every output and workspace. The library itself
- *    allocates no device memory.
+ *  - The caller allocates every output and workspace; no entry point
+ *    allocates device memory per call. Two exceptions hold memory for the
+ *    life of the process: the 16 MiB scratch array of
+ *    nerfgb_render_rays_noalloc (a static device array, reserved when the
+ *    library's module loads on a device) and the cuBLASLt handle that the
+ *    BF16 training backward creates on its first call.
  *  - Every entry point returns NERFGB_OK (0) or a negative NERFGB_E_* code.
  *    None aborts, throws or exits.
  *  - Kernels with bounded device-side waits report a timeout through
@@ -403,9 +407,11 @@ int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tape,
  * library-owned device array of NERFGB_NOALLOC_SCRATCH_BYTES that every GPU
  * loading this code holds until the process exits; the call allocates
  * nothing. Requests needing more return NERFGB_E_SCRATCH_LIMIT (render in
- * smaller chunks). The first call on a device looks up the array's address;
- * make it before any stream capture. All calls share the array: calls that
- * overlap on the GPU race and must be serialised. */
+ * smaller chunks). The first call in each CUDA context (once per device for
+ * the runtime's primary context, and again after cudaDeviceReset, which
+ * reloads the module) looks up the array's address; make it before any
+ * stream capture. All calls share the array: calls that overlap on the GPU
+ * race and must be serialised. */
 int nerfgb_render_rays_noalloc(const void *packed_coarse,
                                const void *packed_fine, int precision,
                                const float *rays_o, const float *rays_d,

@@ -48,6 +48,9 @@
 #include <cuda_fp8.h>
 #include <stdint.h>
 
+#include <mutex>
+#include <unordered_map>
+
 #include "common.cuh"
 #include "mlp_internal.cuh"
 
@@ -1367,12 +1370,23 @@ static int launch_variant(const void *packed, const float *xyz, const float *dir
     cfg.stream = stream;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    static int max_pairs = -1;
-    if (max_pairs < 0) {
-      cfg.gridDim = dim3((unsigned)(sms / 2 * 2));
-      int m = 0;
-      if (cudaOccupancyMaxActiveClusters(&m, kern, &cfg) != cudaSuccess) return NERFGB_E_CUDA;
-      max_pairs = m;
+    // Co-resident pairs of this kernel, per device (asked once per device;
+    // concurrent first calls are serialised).
+    static std::mutex mu;
+    static std::unordered_map<int, int> pairs_of_device;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return NERFGB_E_DEVICE;
+    int max_pairs;
+    {
+      std::lock_guard<std::mutex> lock(mu);
+      auto hit = pairs_of_device.find(dev);
+      if (hit == pairs_of_device.end()) {
+        cfg.gridDim = dim3((unsigned)(sms / 2 * 2));
+        int m = 0;
+        if (cudaOccupancyMaxActiveClusters(&m, kern, &cfg) != cudaSuccess) return NERFGB_E_CUDA;
+        hit = pairs_of_device.emplace(dev, m).first;
+      }
+      max_pairs = hit->second;
     }
     if (max_pairs < 1) return NERFGB_E_UNSUPPORTED;
     const long long pairs = ntiles < max_pairs ? (ntiles > 0 ? ntiles : 1) : max_pairs;

@@ -18,7 +18,7 @@ import torch
 
 from . import _lib, h5, ray_utils
 from ._tensors import as_cuda, device, empty, ptr, stream
-from .weights import PARAM_COUNT, from_dict, glorot_blob, to_dict
+from .weights import PARAM_COUNT, from_dict, glorot_blob, optimizer_state_from_npz, to_dict
 from .weights import from_keras_layers as weights_from_keras
 
 PRECISIONS = {"fp32": _lib.PREC_FP32, "bf16": _lib.PREC_BF16, "fp8": _lib.PREC_FP8}
@@ -84,8 +84,9 @@ class NerfMLP:
 
     def load_weights(self, path):
         """Keras's Model.load_weights for an HDF5 weight file written by the
-        reference (nerf/core/ops.py:142-143): layers matched in order, kernel
-        and bias per layer (h5.py reads the file without h5py)."""
+        reference (nerf/core/ops.py:142-143): the file's layers matched to the
+        network's by their Keras names, kernel and bias per layer (h5.py
+        reads the file without h5py)."""
         self.set_weights(weights_from_keras(h5.keras_layer_weights(path), self.name))
 
     # -- forward -------------------------------------------------------------
@@ -352,15 +353,30 @@ class NeRF:
                       ptr(self.coarse_model.err_word), stream())
         return out
 
-    def load_model(self, load_dir, load_tag):
-        """nerf/core/model.py:278-287: the coarse and fine networks' weights
-        from <load_dir>/<load_tag>_coarse.h5 and <load_tag>_fine.h5 (the
-        files the reference's checkpoint callback writes, ops.py:131-143).
-        The optimizer state (<load_tag>_optimizer.npz, model.py:246-276) is
-        not read: its Keras slot-variable names cannot be checked here."""
+    def load_model(self, load_dir, load_tag, skip_optimizer=False):
+        """NeRF.set_everything (nerf/core/model.py:238-287): unless
+        `skip_optimizer` (the reference's params.model.load.skip_optimizer),
+        the Adam state from <load_dir>/<load_tag>_optimizer.npz
+        (weights.optimizer_state_from_npz: step count and the m/v slots of
+        both networks), then the coarse and fine networks' weights from
+        <load_tag>_coarse.h5 and <load_tag>_fine.h5 (the files the
+        reference's checkpoint callback writes, ops.py:131-149). The next
+        train_step continues from the loaded step, as Keras's Adam does."""
         import os
+        if not skip_optimizer:
+            st = optimizer_state_from_npz(os.path.join(load_dir, f"{load_tag}_optimizer.npz"))
+            self.load_optimizer_state(st)
         self.coarse_model.load_weights(os.path.join(load_dir, f"{load_tag}_coarse.h5"))
         self.fine_model.load_weights(os.path.join(load_dir, f"{load_tag}_fine.h5"))
+
+    def load_optimizer_state(self, state):
+        """Sets the Adam step and the m/v slots of both networks from
+        weights.optimizer_state_from_npz's result."""
+        opt = self._train_state()
+        opt["step"] = int(state["step"])
+        for k, name in enumerate(("coarse", "fine")):
+            for slot in ("m", "v"):
+                opt[slot][k].copy_(torch.from_numpy(state[slot][name]))
 
     def render_frame(self, H, W, intrinsic, c2w, bounds=(2.0, 6.0), **render_kw):
         """One image of the render loop (nerf/main/render.py:79-97): the

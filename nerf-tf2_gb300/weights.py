@@ -60,14 +60,31 @@ def from_dict(d, model_name="coarse"):
 def from_keras_layers(layers, model_name="coarse"):
     """Weights read from a Keras weight file (h5.keras_layer_weights:
     [(layer name, [(weight name, array), ...]), ...]) ->
-    {"<model>/<layer>/kernel:0": ..., ...}. As Keras's load_weights does for
-    an HDF5 file (by topology, not by name), the file's layers that hold
-    weights are matched in order to the network's (dense_0..7, sigma,
-    dense_8, dense_9, rgb), each as [kernel, bias]; shapes must agree."""
+    {"<model>/<layer>/kernel:0": ..., ...}.
+
+    Keras's load_weights pairs an HDF5 file's layers with the network's by
+    position in model.layers, which for a functional model is the graph-depth
+    order of the network that wrote the file (dense_0..7, dense_8, dense_9,
+    rgb, sigma for get_coarse_or_fine_model, not the order of its source).
+    The reference names every layer (model.py:366-387: "<model>/dense_i",
+    "<model>/sigma", "<model>/rgb"), so the file's layers are matched here by
+    that name, which gives the same pairing for a file the reference wrote
+    and does not depend on the order of layer_names. Each layer holds
+    [kernel, bias] with the network's shapes; the file must hold every layer
+    of the network and no other layer with weights."""
     if len(layers) != len(LAYERS):
         raise ValueError(f"the file has {len(layers)} layers with weights, the network has {len(LAYERS)}")
+    by_name = {}
+    for lname, ws in layers:
+        short = lname.rsplit("/", 1)[-1]
+        if short in by_name:
+            raise ValueError(f"layer {lname}: the file names layer {short!r} twice")
+        by_name[short] = (lname, ws)
     d = {}
-    for (lname, ws), (name, i, o) in zip(layers, LAYERS):
+    for name, i, o in LAYERS:
+        if name not in by_name:
+            raise ValueError(f"the file has no layer {model_name}/{name} (its layers: {sorted(by_name)})")
+        lname, ws = by_name[name]
         if len(ws) != 2:
             raise ValueError(f"layer {lname}: {len(ws)} weights, expected kernel and bias")
         (_, k), (_, b) = ws
@@ -76,3 +93,62 @@ def from_keras_layers(layers, model_name="coarse"):
         d[f"{model_name}/{name}/kernel:0"] = np.asarray(k, np.float32)
         d[f"{model_name}/{name}/bias:0"] = np.asarray(b, np.float32)
     return d
+
+
+def optimizer_state_from_npz(path, model_names=("coarse", "fine")):
+    """The Adam state the reference saves as <tag>_optimizer.npz
+    (nerf/core/ops.py:110-120 writes optimizer.variables() with np.savez,
+    plus "names" for their order; nerf/core/model.py:246-276 reads it back).
+
+    Keras names Adam's variables "<optimizer>/iter:0" (the step count),
+    "<optimizer>/beta_1:0" etc. (hyperparameters) and, per trainable
+    variable "<model>/<layer>/kernel:0", the slots
+    "<optimizer>/<model>/<layer>/kernel/m:0" and ".../v:0". The reference
+    checks that the saved names equal those of the optimizer it rebuilt, in
+    order; here the slots are matched by name instead, onto this package's
+    flat parameter layout, and every slot of every layer must be present
+    with its variable's shape. Saved beta_1/beta_2 must be Keras's defaults
+    (0.9, 0.999), the values the reference's Adam uses (model.py:413-418).
+
+    Returns {"step": int, "m": {model: blob}, "v": {model: blob}} with
+    float32 blobs of PARAM_COUNT values."""
+    data = np.load(path, allow_pickle=False)
+    names = [str(x) for x in data["names"]]
+    step = None
+    slots = {}
+    for full in names:
+        base = full[:-2] if full.endswith(":0") else full
+        if base.endswith("/iter") or base == "iter":
+            step = int(np.asarray(data[full]).reshape(()))
+            continue
+        leaf = base.rsplit("/", 1)[-1]
+        if leaf in ("beta_1", "beta_2"):
+            want = 0.9 if leaf == "beta_1" else 0.999
+            if not np.isclose(float(np.asarray(data[full]).reshape(())), want, rtol=0, atol=1e-7):
+                raise ValueError(f"{full}: saved Adam {leaf} differs from the reference's {want}")
+            continue
+        if leaf not in ("m", "v"):
+            continue  # decay, learning_rate: the schedule is recomputed from the step
+        parts = base.split("/")
+        if len(parts) < 4 or parts[-2] not in ("kernel", "bias"):
+            raise ValueError(f"{full}: not a slot of a kernel or bias variable")
+        key = (parts[-4], parts[-3], parts[-2], leaf)  # model, layer, kernel|bias, m|v
+        if key in slots:
+            raise ValueError(f"{full}: slot saved twice")
+        slots[key] = np.asarray(data[full], np.float32)
+    if step is None:
+        raise ValueError(f"{path}: no iteration count (…/iter:0) among the saved names")
+    out = {"step": step, "m": {}, "v": {}}
+    for model in model_names:
+        for slot in ("m", "v"):
+            parts = []
+            for name, i, o in LAYERS:
+                for kind, shape in (("kernel", (i, o)), ("bias", (o,))):
+                    a = slots.get((model, name, kind, slot))
+                    if a is None:
+                        raise ValueError(f"{path}: no Adam slot {slot} for {model}/{name}/{kind}")
+                    if tuple(a.shape) != shape:
+                        raise ValueError(f"{model}/{name}/{kind}/{slot}: shape {tuple(a.shape)}, expected {shape}")
+                    parts.append(a.reshape(-1))
+            out[slot][model] = np.concatenate(parts)
+    return out

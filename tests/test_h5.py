@@ -39,15 +39,20 @@ def test_reads_a_real_hdf5_file(ng):
     assert ds.attrs["MATLAB_class"] == b"double"
 
 
-def keras_layers(ng, model_name, blob):
-    """The reference network's layers in Keras order, with weights for the
-    Dense layers (weight names as Keras gives them)."""
+# model.layers of get_coarse_or_fine_model (model.py:334-394) as a Keras
+# functional model lists them: by graph depth from the inputs, so the sigma
+# head (an output) comes last and rays_d joins just before dense_8.
+KERAS_ORDER = ["xyz", "enc_xyz"] + [f"dense_{i}" for i in range(5)] + ["concat_1"] + \
+    [f"dense_{i}" for i in (5, 6, 7)] + ["rays_d", "dense_8", "enc_rays_d", "concat_2", "dense_9", "rgb", "sigma"]
+
+
+def keras_layers(ng, model_name, blob, order=None):
+    """The reference network's layers in the order Keras saves them (or
+    `order`, short names), with weights for the Dense layers (weight names
+    as Keras gives them)."""
     d = ng.weights.to_dict(blob, model_name)
     m = model_name
-    order = [f"{m}/xyz", f"{m}/rays_d", f"{m}/enc_xyz", f"{m}/enc_rays_d"] + \
-            [f"{m}/dense_{i}" for i in range(5)] + [f"{m}/concat_1"] + \
-            [f"{m}/dense_{i}" for i in (5, 6, 7)] + [f"{m}/sigma", f"{m}/dense_8", f"{m}/concat_2",
-                                                       f"{m}/dense_9", f"{m}/rgb"]
+    order = [f"{m}/{s}" for s in (order or KERAS_ORDER)]
     out = []
     for lname in order:
         short = lname.split("/", 1)[1]
@@ -77,17 +82,44 @@ def test_keras_weight_file_roundtrip(ng, tmp_path, model_name, split, userblock)
     assert root.attrs["backend"] == b"tensorflow"
 
 
+def test_load_order_does_not_depend_on_file_order(ng, tmp_path):
+    """The file's layers are matched to the network's by name: the order of
+    layer_names (Keras's depth order, the source order, or any other) gives
+    the same blob."""
+    blob = ng.weights.glorot_blob(23)
+    source_order = ["xyz", "rays_d", "enc_xyz", "enc_rays_d"] + [f"dense_{i}" for i in range(5)] + \
+        ["concat_1", "dense_5", "dense_6", "dense_7", "sigma", "dense_8", "concat_2", "dense_9", "rgb"]
+    shuffled = list(KERAS_ORDER)
+    np.random.default_rng(4).shuffle(shuffled)
+    for k, order in enumerate((KERAS_ORDER, source_order, shuffled)):
+        p = str(tmp_path / f"o{k}.h5")
+        h5_writer.write_keras_weights(p, keras_layers(ng, "fine", blob, order))
+        got = h5(ng).keras_layer_weights(p)
+        assert [ln.split("/", 1)[1] for ln, _ in got] == [s for s in order if s.startswith(("dense", "sigma", "rgb"))]
+        assert np.array_equal(ng.weights.from_dict(ng.weights.from_keras_layers(got, "fine"), "fine"), blob)
+
+
 def test_keras_weights_checked(ng, tmp_path):
     blob = ng.weights.glorot_blob(3)
     layers = keras_layers(ng, "coarse", blob)
-    lname, ws = layers[5]  # coarse/dense_1
-    layers[5] = (lname, [(ws[0][0], ws[0][1][:, :128]), ws[1]])
+    k = [ln for ln, _ in layers].index("coarse/dense_1")
+    lname, ws = layers[k]
+    layers[k] = (lname, [(ws[0][0], ws[0][1][:, :128]), ws[1]])
     p = str(tmp_path / "bad.h5")
     h5_writer.write_keras_weights(p, layers)
     with pytest.raises(ValueError, match="shapes"):
         ng.weights.from_keras_layers(h5(ng).keras_layer_weights(p), "coarse")
     with pytest.raises(ValueError, match="layers with weights"):
         ng.weights.from_keras_layers(h5(ng).keras_layer_weights(p)[:-1], "coarse")
+    q = str(tmp_path / "good.h5")
+    h5_writer.write_keras_weights(q, keras_layers(ng, "coarse", blob))
+    good = h5(ng).keras_layer_weights(q)
+    renamed = [(ln.replace("dense_3", "dense_33"), ws) for ln, ws in good]
+    with pytest.raises(ValueError, match="no layer coarse/dense_3"):
+        ng.weights.from_keras_layers(renamed, "coarse")
+    twice = [(ln.replace("dense_3", "dense_2"), ws) for ln, ws in good]
+    with pytest.raises(ValueError, match="twice"):
+        ng.weights.from_keras_layers(twice, "coarse")
 
 
 def test_refuses_what_it_does_not_read(ng, tmp_path):
@@ -151,8 +183,70 @@ def test_model_entry_points(ng, tmp_path):
 
     class FakeNeRF:
         coarse_model, fine_model = FakeMLP("coarse"), FakeMLP("fine")
+        opt = None
+
+        def load_optimizer_state(self, st):
+            self.opt = st
 
     fake = FakeNeRF()
-    ng.model.NeRF.load_model(fake, str(tmp_path), "000100_31.20")
+    ng.model.NeRF.load_model(fake, str(tmp_path), "000100_31.20", skip_optimizer=True)
     assert np.array_equal(fake.coarse_model.got, blob)
     assert np.array_equal(fake.fine_model.got, blob[::-1])
+    assert fake.opt is None
+    with pytest.raises(FileNotFoundError):  # as np.load in the reference's set_everything
+        ng.model.NeRF.load_model(fake, str(tmp_path), "000100_31.20")
+    m = {"coarse": blob * 0.5, "fine": blob * 0.25}
+    v = {"coarse": blob * blob, "fine": blob * blob * 2}
+    save_optimizer_npz(ng, str(tmp_path / "000100_31.20_optimizer.npz"), 1234, m, v)
+    ng.model.NeRF.load_model(fake, str(tmp_path), "000100_31.20")
+    assert fake.opt["step"] == 1234
+    for name in ("coarse", "fine"):
+        assert np.array_equal(fake.opt["m"][name], m[name].astype(np.float32))
+        assert np.array_equal(fake.opt["v"][name], v[name].astype(np.float32))
+
+
+def keras_adam_names(ng):
+    """optimizer.variables() names of the reference's Keras Adam over the
+    NeRF's trainable variables (coarse model's, then fine model's): the step
+    count, the float hyperparameters, then every m slot and every v slot."""
+    var = [f"{m}/{name}/{kind}" for m in ("coarse", "fine") for name, _, _ in ng.weights.LAYERS
+           for kind in ("kernel", "bias")]
+    return (["Adam/iter:0", "Adam/beta_1:0", "Adam/beta_2:0", "Adam/decay:0"] +
+            [f"Adam/{x}/m:0" for x in var] + [f"Adam/{x}/v:0" for x in var])
+
+
+def save_optimizer_npz(ng, path, step, m, v):
+    """Writes the file as the reference's checkpoint callback does
+    (nerf/core/ops.py:110-120): np.savez of {name: value} plus "names"."""
+    off = ng.weights.offsets()
+    items = {}
+    for n in keras_adam_names(ng):
+        if n == "Adam/iter:0":
+            items[n] = np.int64(step)
+        elif n.endswith(("beta_1:0", "beta_2:0", "decay:0")):
+            items[n] = np.float32({"beta_1": 0.9, "beta_2": 0.999, "decay": 0.0}[n[5:-2]])
+        else:
+            _, model, layer, kind, slot = n[:-2].split("/")
+            ko, bo, i, o = off[layer]
+            src = (m if slot == "m" else v)[model]
+            items[n] = src[ko:ko + i * o].reshape(i, o) if kind == "kernel" else src[bo:bo + o]
+    items["names"] = np.array(keras_adam_names(ng))
+    np.savez(path, **items)
+
+
+def test_optimizer_npz_checked(ng, tmp_path):
+    blob = ng.weights.glorot_blob(8)
+    p = str(tmp_path / "x_optimizer.npz")
+    save_optimizer_npz(ng, p, 7, {"coarse": blob, "fine": blob}, {"coarse": blob ** 2, "fine": blob ** 2})
+    st = ng.weights.optimizer_state_from_npz(p)
+    assert st["step"] == 7 and st["m"]["fine"].shape == (ng.weights.PARAM_COUNT,)
+    d = dict(np.load(p))
+    d["Adam/beta_1:0"] = np.float32(0.8)
+    np.savez(p, **d)
+    with pytest.raises(ValueError, match="beta_1"):
+        ng.weights.optimizer_state_from_npz(p)
+    d["Adam/beta_1:0"] = np.float32(0.9)
+    d["names"] = np.array([n for n in d["names"] if n != "Adam/fine/rgb/bias/v:0"])
+    np.savez(p, **d)
+    with pytest.raises(ValueError, match="no Adam slot v for fine/rgb/bias"):
+        ng.weights.optimizer_state_from_npz(p)

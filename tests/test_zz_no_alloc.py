@@ -63,12 +63,24 @@ def test_noalloc_matches_workspace_render_twice(ng):
 
 
 def test_noalloc_rejects_requests_beyond_scratch(ng):
+    """A request whose intermediates exceed the 16 MiB array is refused with
+    NERFGB_E_SCRATCH_LIMIT, and its outputs are left untouched."""
     lib = ng._lib.lib()
-    need = lib.nerfgb_render_workspace_bytes(4096, 64, 128)
+    R = 4096
+    need = lib.nerfgb_render_workspace_bytes(R, 64, 128)
     assert need > (16 << 20)
-    fake = ctypes.c_void_p(256)
-    rc = lib.nerfgb_render_rays_noalloc(fake, fake, 1, fake, fake, fake, fake, None, None, 0,
-                                        4096, 64, 128, 1, 1, 0, 1, None, None, None, fake, fake,
-                                        fake, fake, None)
+    nerf = ng.NeRF(ng.make_params(), precision="bf16", seed=5)
+    o, d, n, f = ng.synthetic.sphere_rays(R, 3)
+    rays = [torch.from_numpy(x).cuda() for x in (o, d, n, f)]
+    outs = [torch.full((R, 3), -1.0, device="cuda"), torch.full((R,), -1.0, device="cuda"),
+            torch.full((R,), -1.0, device="cuda")]
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    pc, pf = nerf.coarse_model.packed(), nerf.fine_model.packed()
+    rc = lib.nerfgb_render_rays_noalloc(_ptr(pc), _ptr(pf), ng._lib.PREC_BF16, *map(_ptr, rays), None, None,
+                                        ctypes.c_ulonglong(0), R, 64, 128, 1, 1, 0, ng._lib.TRANS_LOGSUM,
+                                        None, None, None, *map(_ptr, outs), _ptr(err),
+                                        torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
     assert rc == ng._lib.E_SCRATCH_LIMIT
     assert ng._lib.status_name(rc) == "NERFGB_E_SCRATCH_LIMIT"
+    assert all(bool((t == -1.0).all()) for t in outs) and int(err.item()) == 0
