@@ -197,6 +197,68 @@ def reference_arm(args):
 
 
 # ---------------------------------------------------------------------------
+# Errors against the FP64 oracle (untimed): a fixed subset of rays rendered
+# on the GPU with explicit uniforms, and the same rays through the oracle's
+# FP64 chain with the same uniforms.
+# ---------------------------------------------------------------------------
+def fp64_subset(rays, n=256, seed=123, n_fine=SF):
+    """n rays spread over the frame (every R//n-th) and their uniforms."""
+    import torch
+    R = rays[0].shape[0]
+    idx = torch.arange(0, R, max(1, R // n), device=rays[0].device)[:n]
+    sub = [x[idx].contiguous() for x in rays]
+    rng = np.random.default_rng(seed)
+    uc = rng.random((len(idx), SC), dtype=np.float32)
+    uf = rng.random((len(idx), n_fine), dtype=np.float32)
+    return sub, uc, uf
+
+
+def fp64_errors(got_rgb, want_rgb):
+    g = np.asarray(got_rgb, np.float64)
+    w = np.asarray(want_rgb, np.float64)
+    mse = float(np.mean((g - w) ** 2))
+    return {"max_abs_rgb": float(np.abs(g - w).max()), "mean_abs_rgb": float(np.abs(g - w).mean()),
+            "psnr_db": float(-10.0 * np.log10(max(mse, 1e-30)))}
+
+
+def config1(ng, dev, blob_seed=(1, 2), steps=20, warmup=3):
+    """The coarse pass alone on 1,024 sphere rays (64 stratified samples,
+    Glorot-initialised network): rays/s per precision (CUDA events over
+    `steps` passes, inputs resident) and errors against the FP64 oracle's
+    coarse pass on all 1,024 rays."""
+    import torch
+    oracle = importlib.import_module("oracle")
+    R = 1024
+    o, d, n, f = ng.synthetic.sphere_rays(R, 0)
+    rays = [torch.from_numpy(x).to(dev) for x in (o, d, n, f)]
+    uc = np.random.default_rng(1).random((R, SC), dtype=np.float32)
+    ucd = torch.from_numpy(uc).to(dev)
+    p = ng.make_params(N_coarse=SC, N_fine=SF)
+    bc, bf = ng.weights.glorot_blob(blob_seed[0]), ng.weights.glorot_blob(blob_seed[1])
+    want, _ = oracle.nerf_forward(p, oracle.unpack_params(bc, np.float64), oracle.unpack_params(bf, np.float64),
+                                  o, d, n, f, uc.astype(np.float64),
+                                  np.random.default_rng(2).random((R, SF)), np.float64)
+    out = {"workload": "1024 sphere rays (radius 4, direction noise N(0,0.05)), near 2, far 6, 64 stratified "
+                       "samples, coarse network only (Glorot init), rgb/depth/acc maps"}
+    for prec in ("fp32", "bf16", "fp8"):
+        nerf = ng.NeRF(p, precision=prec, coarse_params=bc, fine_params=bf)
+        for _ in range(warmup):
+            nerf.render_coarse(*rays, u_coarse=ucd)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            got = nerf.render_coarse(*rays, u_coarse=ucd)
+        e1.record()
+        torch.cuda.synchronize()
+        nerf.coarse_model.check_device_errors()
+        ms = e0.elapsed_time(e1) / steps
+        out[prec] = {"rays_per_s": R / (ms / 1000.0), "ms_per_pass": ms,
+                     "vs_fp64_oracle": fp64_errors(got["pred_rgb"].cpu().numpy(), want["pred_rgb"])}
+    return out
+
+
+# ---------------------------------------------------------------------------
 # GPU side
 # ---------------------------------------------------------------------------
 class ClockSampler:
@@ -389,6 +451,31 @@ def main():
                                  "psnr_gap_db": psnr_plain - ng.psnr(gt, img_other["rgb"]),
                                  "gate_met": bool(psnr_plain - ng.psnr(gt, img_other["rgb"]) <= 0.1)}
 
+    # errors against the FP64 oracle on 256 rays of the frame (explicit
+    # uniforms): every path of this line, the gated one against the oracle's
+    # gated chain (the proposal in FP64 too) and all against the plain chain
+    oracle = importlib.import_module("oracle")
+    sub, uc_s, uf_s = fp64_subset(rays)
+    hsub = [x.cpu().numpy() for x in sub]
+    p64 = oracle.unpack_params(blob, np.float64)
+    _, w_plain = oracle.nerf_forward(params, p64, p64, *hsub, uc_s.astype(np.float64), uf_s.astype(np.float64),
+                                     np.float64)
+    ucd, ufd = torch.from_numpy(uc_s).to(dev), torch.from_numpy(uf_s).to(dev)
+    fp64 = {"rays": int(sub[0].shape[0]), "uniforms": "explicit, numpy PCG64 seed 123",
+            "plain_fp32": fp64_errors(plain.render(*sub, u_coarse=ucd, u_fine=ufd)["rgb"].cpu().numpy(),
+                                      w_plain["pred_rgb"]),
+            f"{args.path}_plain": fp64_errors(fast.render(*sub, u_coarse=ucd, u_fine=ufd)["rgb"].cpu().numpy(),
+                                              w_plain["pred_rgb"])}
+    if proposal is not None:
+        got = fast.render(*sub, u_coarse=ucd, u_fine=ufd, **prop_kw)["rgb"].cpu().numpy()
+        fp64["headline_vs_plain_chain"] = fp64_errors(got, w_plain["pred_rgb"])
+        if args.proposal_mode == "gate":
+            w_gate, _, _, _ = oracle.nerf_render_gated(params, proposal.params.cpu().numpy(), p64, p64, *hsub,
+                                                       uc_s.astype(np.float64), uf_s.astype(np.float64),
+                                                       args.gate_tau, np.float64)
+            fp64["headline_vs_gated_chain"] = fp64_errors(got, w_gate["pred_rgb"])
+    cfg1 = config1(ng, dev)
+
     # roofline of the dominant kernel (the MLP) at the fine-pass launch shape
     nrows = CHUNK * (SC + SF)
     xyz = (torch.rand(nrows, 3, device=dev) * 4 - 2)
@@ -424,28 +511,42 @@ def main():
         peak = sms * 128 * 2 * clk_max * 1e6 / 1e12
         src = f"FP32 FMA issue peak: {sms} SMs x 128 FMA/clk x {clk_max:.0f} MHz"
         bound = "fp32-simt"
-    traffic = None
+    # DRAM bytes of one such launch are not measured in this run (that needs
+    # ncu): they come from the committed capture named in traffic_source
+    traffic, traffic_src = None, None
     tr_path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tr_path):
-        traffic = json.load(open(tr_path)).get(f"mlp_{args.path}_fine_chunk_bytes")
+        tr = json.load(open(tr_path))
+        traffic = tr.get(f"mlp_{args.path}_fine_chunk_bytes")
+        if traffic is not None:
+            traffic_src = "not measured in this run: " + tr.get("note", "profiles/traffic.json")
 
     # precision sweep: 65,536 rays x (64 coarse + 192 fine) samples, every MLP
     # precision, compensated log-sum transmittance; error against the FP32
-    # path on the same uniforms (the FP64 oracle comparison is in the tests)
+    # path on the same uniforms, and against the FP64 oracle on 256 of the
+    # rays with explicit uniforms
     sweep = None
     if args.sweep:
         p5 = ng.make_params(N_coarse=SC, N_fine=192)
-        o5, d5, n5, f5 = [x[:65536] for x in rays]
-        out5, rate5 = {}, {}
+        five = [x[:65536] for x in rays]
+        o5, d5, n5, f5 = five
+        sub5, uc5, uf5 = fp64_subset(five, n_fine=192, seed=321)
+        _, w5 = oracle.nerf_forward(p5, p64, p64, *[x.cpu().numpy() for x in sub5], uc5.astype(np.float64),
+                                    uf5.astype(np.float64), np.float64)
+        uc5d, uf5d = torch.from_numpy(uc5).to(dev), torch.from_numpy(uf5).to(dev)
+        out5, rate5, err5 = {}, {}, {}
         for prec in ("fp32", "bf16", "fp8"):
             m5 = ng.NeRF(p5, precision=prec, coarse_params=blob, fine_params=blob)
             sms = timed_steps(lambda i: m5.render(o5, d5, n5, f5, chunk=16384, seed=50 + i), 2 if prec != "fp32" else 1, 1)
             rate5[prec] = 65536 / (sms / 1000.0)
             out5[prec] = m5.render(o5, d5, n5, f5, chunk=16384, seed=77)["rgb"]
+            err5[prec] = fp64_errors(m5.render(*sub5, u_coarse=uc5d, u_fine=uf5d)["rgb"].cpu().numpy(),
+                                     w5["pred_rgb"])
         sweep = {"workload": "65536 rays x (64 coarse + 192 fine) samples, one frame's first 65536 rays",
                  **{prec: {"rays_per_s": rate5[prec],
                            "max_abs_rgb_vs_fp32": float((out5[prec] - out5["fp32"]).abs().max()),
-                           "psnr_vs_fp32_db": ng.psnr(out5["fp32"], out5[prec])} for prec in rate5}}
+                           "psnr_vs_fp32_db": ng.psnr(out5["fp32"], out5[prec]),
+                           "vs_fp64_oracle_256_rays": err5[prec]} for prec in rate5}}
 
     # training step (model.py:127-180): 4096 rays of the scene's renders
     train = None
@@ -483,13 +584,15 @@ def main():
                            "speedup": plain_ms / ms},
             "bf16_plain": {"value": world * R / (bf16_ms / 1000.0), "unit": "rays/s"},
             "quality": quality,
+            "fp64_oracle": fp64,
+            "config1_coarse_pass": cfg1,
             "proposal": prop_info,
             "train_step": train,
             "precision_sweep": sweep,
             "roofline": {"kernel": f"mlp_{args.path} fine-pass launch ({nrows} rows)", "bound": bound,
                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None, "peak_source": src,
-                         "traffic": traffic, "launch_ms": k_ms},
+                         "traffic": traffic, "traffic_source": traffic_src, "launch_ms": k_ms},
             "cpu_baseline": cpu,
             "e2e": {"value": world * R / (e2e_ms / 1000.0), "unit": "rays/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},

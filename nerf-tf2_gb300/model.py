@@ -276,6 +276,30 @@ class NeRF:
     predict_step = __call__
 
     # -- fused inference ----------------------------------------------------
+    def render_coarse(self, rays_o, rays_d, near, far, *, u_coarse=None, precision=None):
+        """The coarse pass alone (model.py:88-100): stratified samples, the
+        coarse network and compositing, three launches. Directions are read
+        per ray by the MLP (no [R*S,3] dir_inputs tensor). Returns
+        post_process_model_output's dict."""
+        p = self.params
+        rays_o = as_cuda(rays_o, name="rays_o")
+        R = rays_o.shape[0]
+        rays_d = as_cuda(rays_d, shape=(R, 3), name="rays_d")
+        near = as_cuda(near, shape=(R, 1), name="near")
+        far = as_cuda(far, shape=(R, 1), name="far")
+        S = int(p.sampling.N_coarse)
+        perturb = bool(p.sampling.perturb)
+        if perturb:
+            u = ray_utils.uniform((R, S)) if u_coarse is None else as_cuda(u_coarse, shape=(R, S), name="u_coarse")
+        else:
+            u = None
+        xyz, t, edges, widths = empty(R * S, 3), empty(R, S), empty(R, S + 1), empty(R, S)
+        _lib.call("nerfgb_coarse_sample", ptr(rays_o), ptr(rays_d), ptr(near), ptr(far), ptr(u), R, S,
+                  int(perturb), int(bool(p.sampling.lin_inv_depth)), ptr(xyz), None, ptr(t), ptr(edges),
+                  ptr(widths), stream())
+        rgb_s, sig_s = self.coarse_model((xyz, rays_d), precision=precision, rows_per_dir=S)
+        return ray_utils.post_process_model_output(rgb_s, sig_s, t, self.white_bg, trans_mode=self.trans_mode)
+
     def render(self, rays_o, rays_d, near, far, *, chunk=4096, u_coarse=None, u_fine=None, seed=0,
                precision=None, return_coarse=False, proposal=None, proposal_mode="replace",
                gate_tau=1e-5):

@@ -305,17 +305,20 @@ def mlp_forward(p, xyz, dirs, dtype=F32, cache=False):
 
 
 def nerf_forward(params, p_coarse, p_fine, rays_o, rays_d, near, far,
-                 u_coarse, u_fine, dtype=F32):
-    """NeRF.forward (model.py:57-125) with supplied uniforms."""
+                 u_coarse, u_fine, dtype=F32, mlp=None):
+    """NeRF.forward (model.py:57-125) with supplied uniforms. ``mlp(p, xyz,
+    dirs)`` replaces mlp_forward when given (e.g. mlp_forward_lowp)."""
+    if mlp is None:
+        mlp = lambda p, x, d: mlp_forward(p, x, d, dtype)  # noqa: E731
     d_cm = create_input_batch_coarse_model(params, rays_o, rays_d, near, far,
                                            u_coarse, dtype)
-    rgb_c, sig_c = mlp_forward(p_coarse, d_cm["xyz_inputs"], d_cm["dir_inputs"], dtype)
+    rgb_c, sig_c = mlp(p_coarse, d_cm["xyz_inputs"], d_cm["dir_inputs"])
     pp_cm = post_process_model_output(rgb_c, sig_c, d_cm["t_vals"],
                                       params.system.white_bg)
     d_fm = create_input_batch_fine_model(params, rays_o, rays_d, pp_cm["weights"],
                                          d_cm["bin_data"], d_cm["t_vals"], u_fine,
                                          dtype)
-    rgb_f, sig_f = mlp_forward(p_fine, d_fm["xyz_inputs"], d_fm["dir_inputs"], dtype)
+    rgb_f, sig_f = mlp(p_fine, d_fm["xyz_inputs"], d_fm["dir_inputs"])
     pp_fm = post_process_model_output(rgb_f, sig_f, d_fm["t_vals"],
                                       params.system.white_bg)
     return pp_cm, pp_fm
@@ -581,20 +584,27 @@ def gate_fine(sort_perm, mask_c):
 
 
 def nerf_render_gated(params, prop_blob, p_coarse, p_fine, rays_o, rays_d, near, far,
-                      u_coarse, u_fine, tau, dtype=F32):
+                      u_coarse, u_fine, tau, dtype=F32, mlp=None, prop=None, mask_c=None):
     """Returns (fine post_process_model_output, coarse mask [R,Sc], union
-    mask [R,S], proposal weights [R,Sc])."""
+    mask [R,S], proposal weights [R,Sc]). ``mlp(p, xyz, dirs)`` and
+    ``prop(blob, xyz)`` replace mlp_forward and prop_forward when given;
+    ``mask_c`` [R,Sc] replaces the coarse gate's decisions (e.g. the ones a
+    device run made)."""
+    if mlp is None:
+        mlp = lambda p, x, d: mlp_forward(p, x, d, dtype)  # noqa: E731
+    if prop is None:
+        prop = lambda b, x: prop_forward(b, x, dtype)  # noqa: E731
     d_cm = create_input_batch_coarse_model(params, rays_o, rays_d, near, far, u_coarse, dtype)
     t_c = d_cm["t_vals"]
     Sc = t_c.shape[1]
-    w_p = proposal_weights(prop_forward(prop_blob, d_cm["xyz_inputs"], dtype), t_c)
-    m_c = gate_coarse(w_p, tau)
-    _, sig_c = mlp_forward(p_coarse, d_cm["xyz_inputs"], d_cm["dir_inputs"], dtype)
+    w_p = proposal_weights(prop(prop_blob, d_cm["xyz_inputs"]), t_c)
+    m_c = gate_coarse(w_p, tau) if mask_c is None else np.asarray(mask_c, bool).reshape(t_c.shape)
+    _, sig_c = mlp(p_coarse, d_cm["xyz_inputs"], d_cm["dir_inputs"])
     sig_c = np.where(m_c.reshape(-1), sig_c.reshape(-1), dtype(0))
     w_c = compute_weights(sig_c, t_c, Sc)
     d_fm = create_input_batch_fine_model(params, rays_o, rays_d, w_c, d_cm["bin_data"], t_c,
                                          u_fine, dtype, return_indices=True)
-    rgb_f, sig_f = mlp_forward(p_fine, d_fm["xyz_inputs"], d_fm["dir_inputs"], dtype)
+    rgb_f, sig_f = mlp(p_fine, d_fm["xyz_inputs"], d_fm["dir_inputs"])
     m_f = gate_fine(d_fm["sort_perm"], m_c)
     on = m_f.reshape(-1)
     sig_f = np.where(on, sig_f.reshape(-1), dtype(0))
@@ -660,3 +670,101 @@ def mse(y_true, y_pred):
     """keras.losses.MeanSquaredError: mean over every element (model.py:32)."""
     d = np.asarray(y_pred) - np.asarray(y_true)
     return float(np.mean(d * d)), 2 * d / d.size
+
+
+# ---------------------------------------------------------------------------
+# Low-precision emulation (not in the reference): the arithmetic that the
+# build's tensor-core MLPs are specified to do, evaluated in float64 so that
+# only the specified roundings differ from the FP64 oracle. BF16: every GEMM
+# operand (encodings, activations, weights) rounded to BF16, products summed
+# exactly, the sum rounded to FP32, the FP32 bias added in FP32. FP8: E4M3
+# operands, each weight column n divided by s_n = max_k |W[k,n]| / 448 before
+# rounding, the sum rounded to FP32 and mapped back as fma(sum, s_n, b_n).
+# The sigma and rgb heads run in FP32 on the unrounded activations, as in
+# the FP32 path (model.py:374-387).
+# ---------------------------------------------------------------------------
+E4M3_MAX = 448.0
+
+
+def round_bf16(a):
+    """Round-to-nearest-even of float32 values to BF16 (8 significand bits),
+    returned as float32."""
+    u = np.array(a, F32, copy=True).view(np.uint32)   # finite values: no overflow below
+    r = (u >> 16) & np.uint32(1)
+    u += np.uint32(0x7FFF)
+    u += r
+    u &= np.uint32(0xFFFF0000)
+    return u.view(F32).reshape(np.shape(a))
+
+
+def round_e4m3(a):
+    """Round-to-nearest-even of float32 values to FP8 E4M3 (4 significand
+    bits, exponents -6..8, subnormal step 2^-9), saturated to +-448
+    (OCP FP8 formats, satfinite conversion), returned as float32."""
+    x = np.asarray(a, F32)
+    # normal range: keep 3 of float32's 23 fraction bits, ties to even (a
+    # carry into the exponent is the correct next binade)
+    u = np.array(x, F32, copy=True).view(np.uint32)
+    r = (u >> 20) & np.uint32(1)
+    u += np.uint32(0x7FFFF)
+    u += r
+    u &= np.uint32(0xFFF00000)
+    y = u.view(F32).reshape(x.shape)
+    # below 2^-6: multiples of the subnormal step 2^-9 (exact scaling, rint ties to even)
+    small = np.abs(x) < F32(2.0 ** -6)
+    y = np.where(small, np.rint(x * F32(512.0)) / F32(512.0), y)
+    return np.clip(y, F32(-E4M3_MAX), F32(E4M3_MAX)).astype(F32)
+
+
+def fp8_scales(W):
+    """Per-output-channel weight scales s_n = max_k |W[k, n]| / 448 (FP32)."""
+    return (np.abs(np.asarray(W, F32)).max(axis=0) / F32(E4M3_MAX)).astype(F32)
+
+
+def _gemm_lowp(a_q, W, b, fmt):
+    """One Dense layer of the tensor-core kernels: a_q [M, K] already in the
+    operand format. Returns the FP32 pre-activation."""
+    W = np.asarray(W, F32)
+    b = np.asarray(b, F32)
+    if fmt == "bf16":
+        acc = (a_q.astype(F64) @ round_bf16(W).astype(F64)).astype(F32)
+        return (acc + b).astype(F32)
+    s = fp8_scales(W)
+    wq = round_e4m3(np.where(s > 0, W / np.where(s > 0, s, F32(1)), F32(0)).astype(F32))
+    acc = (a_q.astype(F64) @ wq.astype(F64)).astype(F32)
+    return (acc.astype(F64) * s + b).astype(F32)   # fmaf(acc, s, b): one rounding
+
+
+def mlp_forward_lowp(p, xyz, dirs, fmt):
+    """get_coarse_or_fine_model's network (model.py:334-394) as the BF16
+    (fmt="bf16") or FP8-e4m3 (fmt="fp8") tensor-core kernels compute it.
+    p: unpack_params(blob, F32). Returns (rgb [M,3], sigma [M,1]) float32."""
+    q = round_bf16 if fmt == "bf16" else round_e4m3
+    enc_xyz = q(positional_encoding(xyz, 10, F32))
+    enc_dir = q(positional_encoding(dirs, 4, F32))
+    h = enc_xyz
+    for i in range(8):
+        v = _gemm_lowp(h, *p[f"dense_{i}"], fmt)
+        h = q(np.maximum(v, 0))
+        if i == 4:
+            h = np.concatenate([h, enc_xyz], axis=-1)
+    W, b = p["sigma"]
+    sigma = np.maximum(np.maximum(v, 0).astype(F64) @ np.asarray(W, F64) + np.asarray(b, F64), 0)
+    v8 = _gemm_lowp(h, *p["dense_8"], fmt)
+    h9in = np.concatenate([q(v8), enc_dir], axis=-1)
+    v9 = _gemm_lowp(h9in, *p["dense_9"], fmt)
+    W, b = p["rgb"]
+    z = np.maximum(v9, 0).astype(F64) @ np.asarray(W, F64) + np.asarray(b, F64)
+    rgb = 1.0 / (1.0 + np.exp(-z))
+    return rgb.astype(F32), sigma.astype(F32)
+
+
+def prop_forward_bf16(blob, xyz):
+    """The proposal network (prop_forward) as its tensor-core kernel computes
+    it: BF16 encoding, W1, h1 and W2, FP32 biases, the last layer in FP32."""
+    p = prop_unpack(blob, F32)
+    enc = positional_encoding(xyz, 6, F32)
+    h1 = np.maximum(round_bf16(enc).astype(F64) @ round_bf16(p["W1"]).astype(F64) + p["b1"], 0)
+    z2 = round_bf16(h1.astype(F32)).astype(F64) @ round_bf16(p["W2"]).astype(F64) + p["b2"]
+    z3 = np.maximum(z2, 0) @ p["W3"].astype(F64) + p["b3"][0]
+    return softplus(z3).astype(F32)

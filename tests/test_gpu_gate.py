@@ -121,14 +121,15 @@ def test_gated_all_on_equals_plain(ng, cuda, case, precision):
         assert torch.equal(gated[k], plain[k]), k
 
 
-def _margin_tau(w, q):
-    """A gate threshold near the q-quantile of w with no weight within
-    0.02% of it (FP32 rounding moves a weight by ~1e-6 relative), so that no
-    gate can flip between the GPU and the oracle."""
+def _margin_tau(w, q, gap=1.0005):
+    """A gate threshold near the q-quantile of w with no weight within a
+    factor sqrt(gap) of it (FP32 rounding moves a weight by ~1e-6 relative;
+    the BF16 proposal kernel against its emulation by ~1e-4), so that no gate
+    can flip between the GPU and the oracle."""
     v = np.sort(w.reshape(-1))
     for start in range(int(q * v.size), v.size - 1):
         lo, hi = v[start], v[start + 1]
-        if hi > lo * 1.0005 and lo > 0:
+        if hi > lo * gap and lo > 0:
             return float(np.sqrt(lo * hi))
     raise AssertionError("no threshold with margin")
 
@@ -168,6 +169,53 @@ def test_gated_render_vs_oracle(ng, oracle, cuda, case, white_bg):
     # and the gate changes the result (not the plain chain in disguise)
     plain = nerf.render(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc), u_fine=dev(uf))
     assert float((plain["rgb"] - got["rgb"]).abs().max()) > 1e-3
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp8"])
+def test_gated_render_lowp_vs_oracle(ng, oracle, cuda, case, precision):
+    """The headline path: the gated render with BF16 (or FP8) NeRF MLPs and
+    the BF16 proposal kernel, against the oracle's gated chain with both
+    networks emulated in the kernels' arithmetic (oracle.mlp_forward_lowp,
+    oracle.prop_forward_bf16), and against the FP64 oracle's gated chain
+    with the format's own error bound."""
+    R, o, d, n, f, uc, uf = case
+    p = ng.make_params()
+    bc, bf = ng.weights.glorot_blob(1), ng.weights.glorot_blob(2)
+    prop = ng.ProposalNetwork(seed=3)
+    blob = host(prop.params)
+    # The gate's decisions, as the render's own kernels make them (the BF16
+    # proposal kernel and the proposal compositor on the same samples), with
+    # a threshold at their median: the oracle is given these decisions, as
+    # its emulation of the BF16 proposal differs in the last bits and would
+    # flip gates that sit at the threshold.
+    d_cm = ng.ray_utils.create_input_batch_coarse_model(p, dev(o), dev(d), dev(n), dev(f), u_vals=dev(uc))
+    w_dev = host(ng.proposal.proposal_weights(prop(d_cm["xyz_inputs"], precision="bf16"), d_cm["t_vals"],
+                                              trans_mode=ng._lib.TRANS_CUMPROD))
+    tau = _margin_tau(w_dev, 0.5)
+    mask_c = w_dev > tau
+    assert 0.3 < mask_c.mean() < 0.7
+    nerf = ng.NeRF(p, precision=precision, coarse_params=bc, fine_params=bf,
+                   trans_mode=ng._lib.TRANS_CUMPROD)
+    got = nerf.render(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc), u_fine=dev(uf), proposal=prop,
+                      proposal_mode="gate", gate_tau=tau)
+    nerf.coarse_model.check_device_errors()
+    emul = lambda pp, x, dd: oracle.mlp_forward_lowp(pp, x, dd, precision)  # noqa: E731
+    want, m_c, _, w_emul = oracle.nerf_render_gated(p, blob, oracle.unpack_params(bc), oracle.unpack_params(bf),
+                                                    o, d, n, f, uc, uf, tau, F32, mlp=emul,
+                                                    prop=lambda b, x: oracle.prop_forward_bf16(b, x),
+                                                    mask_c=mask_c)
+    # the emulated proposal agrees with the kernel's on all but a handful of gates
+    assert ((w_emul > tau) != mask_c).mean() < 0.01
+    tight = {"bf16": 5e-4, "fp8": 5e-3}[precision]
+    worst = {"bf16": 3e-2, "fp8": 1.5e-1}[precision]
+    _close_most(host(got["rgb"]), want["pred_rgb"], tight, worst)
+    _close_most(host(got["acc"]), want["acc_map"], tight, worst)
+    _close_most(host(got["depth"]), want["pred_depth"], 10 * tight, 10 * worst)
+    w64, _, _, _ = oracle.nerf_render_gated(p, blob, oracle.unpack_params(bc, F64), oracle.unpack_params(bf, F64),
+                                            o, d, n, f, uc.astype(F64), uf.astype(F64), tau, F64, mask_c=mask_c)
+    e64 = np.abs(host(got["rgb"]).astype(F64) - w64["pred_rgb"]).max(axis=1)
+    print(f"gated {precision} vs FP64 gated oracle: rgb max {e64.max():.2e} mean {e64.mean():.2e}")
+    assert e64.mean() < {"bf16": 5e-3, "fp8": 3e-2}[precision]
 
 
 def test_gated_render_meets_quality_gate(ng, cuda):

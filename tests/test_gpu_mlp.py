@@ -124,3 +124,33 @@ def test_mlp_fp8_vs_fp64(ng, oracle, cuda, n):
     # and clearly coarser than BF16 on the same inputs (the FP8 path is taken)
     r16, _ = ng.get_coarse_or_fine_model("coarse", params=blob, precision="bf16")((dev(x), dev(d)))
     assert np.abs(host(r16) - r64).mean() < err_rgb.mean()
+
+
+def _err_stats(got, want, scale=1.0):
+    e = np.abs(np.asarray(got, F64) - np.asarray(want, F64)).reshape(len(got), -1).max(axis=1) / scale
+    return float(e.max()), float(np.quantile(e, 0.99)), float(e.mean())
+
+
+@pytest.mark.parametrize("precision,n", [("bf16", 4096), ("bf16", 301), ("fp8", 4097), ("fp8", 300)])
+def test_mlp_lowp_vs_emulation(ng, oracle, cuda, precision, n):
+    """The tensor-core kernels against the oracle's emulation of their
+    specified arithmetic (oracle.mlp_forward_lowp: operands rounded to BF16 or
+    to E4M3 with per-channel weight scales, exact products, FP32 sums, FP32
+    bias and heads). What remains is the tensor core's FP32 summation order,
+    and an activation that lands within that difference of a rounding
+    boundary rounding the other way (a BF16 step is 2^-8 relative, an E4M3
+    step 2^-3), so the bounds are far below the formats' own error against
+    FP64 (test_mlp_bf16_vs_fp64, test_mlp_fp8_vs_fp64)."""
+    blob = biased_blob(ng, 8)
+    x, d = samples(n, 11 + n)
+    mlp = ng.get_coarse_or_fine_model("coarse", params=blob, precision=precision)
+    rgb, sigma = mlp((dev(x), dev(d)))
+    mlp.check_device_errors()
+    er, es = oracle.mlp_forward_lowp(oracle.unpack_params(blob, F32), x, d, precision)
+    r_max, r_99, r_mean = _err_stats(host(rgb), er)
+    s_max, s_99, s_mean = _err_stats(host(sigma), es, max(1.0, float(np.abs(es).max())))
+    print(f"{precision} n={n}: rgb max {r_max:.2e} p99 {r_99:.2e} mean {r_mean:.2e}; "
+          f"sigma max {s_max:.2e} p99 {s_99:.2e} mean {s_mean:.2e}")
+    tol = {"bf16": dict(mx=2e-3, p99=2e-4, mean=2e-5), "fp8": dict(mx=3e-2, p99=3e-3, mean=3e-4)}[precision]
+    for mx, p99, mean in ((r_max, r_99, r_mean), (s_max, s_99, s_mean)):
+        assert mx < tol["mx"] and p99 < tol["p99"] and mean < tol["mean"], (mx, p99, mean)

@@ -99,3 +99,86 @@ def test_render_frame_is_render_of_device_rays(ng, cuda):
     assert torch.equal(fr["depth"].reshape(-1), ref["depth"])
     img = np.clip(host(ref["rgb"]) * 255.0, 0.0, 255.0).astype(np.uint8).reshape(H, W, 3)
     assert np.array_equal(host(fr["image_u8"]), img)
+
+
+@pytest.fixture(scope="module")
+def case1024(ng):
+    R = 1024
+    o, d, n, f = ng.synthetic.sphere_rays(R, 44)
+    rng = np.random.default_rng(45)
+    uc = rng.random((R, 64), dtype=F32)
+    uf = rng.random((R, 128), dtype=F32)
+    rng_b = np.random.default_rng(46)
+    bc, bf = ng.weights.glorot_blob(1), ng.weights.glorot_blob(2)
+    for blob in (bc, bf):  # non-zero biases, so that the bias paths are used
+        for name, (ko, bo, i, o_) in ng.weights.offsets().items():
+            blob[bo:bo + o_] = rng_b.uniform(-0.1, 0.1, o_)
+    return R, o, d, n, f, uc, uf, bc, bf
+
+
+def _row_err(got, want):
+    return np.abs(np.asarray(got, F64) - np.asarray(want, F64)).reshape(len(got), -1).max(axis=1)
+
+
+@pytest.mark.parametrize("precision", ["bf16", "fp8"])
+def test_fused_render_lowp_vs_oracle(ng, oracle, cuda, case1024, precision):
+    """The fused render (nerfgb_render_rays) in BF16 / FP8 on 1,024 rays
+    against (1) the FP64 oracle of NeRF.forward: the format's own error,
+    reported and bounded, and (2) the oracle's FP32 chain with the MLPs
+    emulated in the kernels' arithmetic (oracle.mlp_forward_lowp): tight on
+    all but a few rays. On those few the fine sampler's CDF, built from
+    coarse weights that differ in the last FP32 bits, puts a draw on the
+    other side of a bin edge; t is continuous across the edge, so such a ray
+    moves by little."""
+    R, o, d, n, f, uc, uf, bc, bf = case1024
+    p = ng.make_params()
+    nerf = ng.NeRF(p, precision=precision, coarse_params=bc, fine_params=bf,
+                   trans_mode=ng._lib.TRANS_CUMPROD)
+    out = nerf.render(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc), u_fine=dev(uf), chunk=512)
+    nerf.coarse_model.check_device_errors()
+    got = {k: host(out[k]) for k in ("rgb", "depth", "acc")}
+    _, w64 = oracle.nerf_forward(p, oracle.unpack_params(bc, F64), oracle.unpack_params(bf, F64),
+                                 o, d, n, f, uc.astype(F64), uf.astype(F64), F64)
+    e64 = _row_err(got["rgb"], w64["pred_rgb"])
+    psnr64 = oracle.psnr(w64["pred_rgb"], got["rgb"])
+    print(f"{precision} fused render vs FP64 oracle, 1024 rays: rgb max {e64.max():.2e} "
+          f"p90 {np.quantile(e64, 0.9):.2e} mean {e64.mean():.2e}; PSNR {psnr64:.1f} dB")
+    emul = lambda pp, x, dd: oracle.mlp_forward_lowp(pp, x, dd, precision)  # noqa: E731
+    _, we = oracle.nerf_forward(p, oracle.unpack_params(bc, F32), oracle.unpack_params(bf, F32),
+                                o, d, n, f, uc, uf, F32, mlp=emul)
+    stats = {}
+    for key, wkey in (("rgb", "pred_rgb"), ("acc", "acc_map"), ("depth", "pred_depth")):
+        e = _row_err(got[key], we[wkey])
+        stats[key] = e
+        print(f"  vs emulation {key}: max {e.max():.2e} p96 {np.quantile(e, 0.96):.2e} mean {e.mean():.2e}")
+    # The format's own error against FP64: this random-init network's density
+    # is rough, so a fine draw that the coarse pass's rounding moves samples
+    # a different value on a few rays; the mean and the PSNR bound the rest.
+    mean64, min_psnr = {"bf16": (5e-3, 30.0), "fp8": (3e-2, 20.0)}[precision]
+    assert e64.mean() < mean64 and psnr64 > min_psnr, (e64.mean(), psnr64)
+    tight = {"bf16": 5e-4, "fp8": 5e-3}[precision]
+    for key, scale in (("rgb", 1.0), ("acc", 1.0), ("depth", 10.0)):
+        e = stats[key]
+        assert np.quantile(e, 0.96) < tight * scale, (key, np.quantile(e, 0.96))
+        assert e.mean() < 0.2 * tight * scale, (key, e.mean())
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_render_coarse_vs_oracle(ng, oracle, cuda, case, precision):
+    """NeRF.render_coarse (the coarse pass, model.py:88-100) against the
+    oracle's coarse pass: FP32 at the chain's FP32 tolerance, BF16 against
+    the emulated-BF16 chain."""
+    R, o, d, n, f, uc, uf, bc, bf = case
+    p = ng.make_params()
+    nerf = ng.NeRF(p, precision=precision, coarse_params=bc, fine_params=bf,
+                   trans_mode=ng._lib.TRANS_CUMPROD)
+    got = nerf.render_coarse(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc))
+    nerf.coarse_model.check_device_errors()
+    mlp = None if precision == "fp32" else (lambda pp, x, dd: oracle.mlp_forward_lowp(pp, x, dd, "bf16"))
+    want, _ = oracle.nerf_forward(p, oracle.unpack_params(bc), oracle.unpack_params(bf), o, d, n, f, uc, uf,
+                                  F32, mlp=mlp)
+    tol = 1e-4 if precision == "fp32" else 5e-4
+    np.testing.assert_allclose(host(got["pred_rgb"]), want["pred_rgb"], atol=tol)
+    np.testing.assert_allclose(host(got["acc_map"]), want["acc_map"], atol=tol)
+    np.testing.assert_allclose(host(got["pred_depth"]), want["pred_depth"], atol=5 * tol)
+    np.testing.assert_allclose(host(got["weights"]), want["weights"], atol=tol)

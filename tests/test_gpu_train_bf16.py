@@ -90,3 +90,32 @@ def test_train_bf16_reduces_loss(ng, cuda):
     student.coarse_model.check_device_errors()
     assert all(np.isfinite(losses))
     assert losses[-1] < 0.8 * losses[0], losses
+
+
+def test_train_step_resumes_loaded_adam_state(ng, oracle, cuda):
+    """NeRF.load_optimizer_state (what load_model reads from the reference's
+    <tag>_optimizer.npz) sets the step and the m/v slots; the next train_step
+    is Adam step t+1 from them (model.py:246-276, then :171)."""
+    p = ng.make_params()
+    nerf = ng.NeRF(p, precision="fp32", seed=60)
+    rays = [dev(x) for x in ng.synthetic.sphere_rays(256, 9)]
+    target = torch.rand(256, 3, device="cuda", generator=torch.Generator(device="cuda").manual_seed(1))
+    rng = np.random.default_rng(2)
+    P = ng.weights.PARAM_COUNT
+    st = {"step": 41, "m": {k: (rng.normal(size=P) * 1e-3).astype(F32) for k in ("coarse", "fine")},
+          "v": {k: (rng.random(P) * 1e-6).astype(F32) for k in ("coarse", "fine")}}
+    nerf.load_optimizer_state(st)
+    before = [host(m.params).astype(F64) for m in (nerf.coarse_model, nerf.fine_model)]
+    uc = dev(rng.random((256, 64), dtype=F32))
+    uf = dev(rng.random((256, 128), dtype=F32))
+    nerf.train_step((tuple(rays), (target,)), u_coarse=uc, u_fine=uf, lr=1e-3)
+    grads = [host(g).astype(F64) for g in nerf.gradients()]
+    for k, (name, model) in enumerate((("coarse", nerf.coarse_model), ("fine", nerf.fine_model))):
+        want, _, _ = oracle.apply_adam(before[k], st["m"][name].astype(F64), st["v"][name].astype(F64), grads[k],
+                                       42, 1e-3)
+        # FP32 Adam against float64: where v is tiny, m / (sqrt(v) + eps) amplifies
+        # FP32 rounding; 2e-3 of the step size
+        np.testing.assert_allclose(host(model.params), want, rtol=1e-5, atol=2e-3 * 1e-3)
+        fresh, _, _ = oracle.apply_adam(before[k], 0.0, 0.0, grads[k], 1, 1e-3)
+        assert np.abs(fresh - want).max() > 1e-4  # the loaded state matters
+    assert nerf._train_state()["step"] == 42

@@ -336,3 +336,20 @@ def test_get_rays_tf_matches_float64(oracle, ng):
     np.testing.assert_allclose(d32, d64, atol=2e-6)
     np.testing.assert_allclose(o32, o64, atol=1e-6)
     np.testing.assert_allclose(np.linalg.norm(d32, axis=1), 1.0, atol=1e-6)
+
+
+def test_low_precision_roundings(oracle):
+    """The emulation's format roundings: round-to-nearest-even, E4M3 with
+    subnormals (step 2^-9) and saturation to 448 (OCP FP8 formats)."""
+    x = np.array([0, 1, 1.0625, 1.125, 1.1875, 448, 460, 1000, -1000, 2.0 ** -6, 2.0 ** -9, 3 * 2.0 ** -10,
+                  2.0 ** -10, 2.0 ** -11, -0.3, 240, 232], np.float32)
+    want = np.array([0, 1, 1, 1.125, 1.25, 448, 448, 448, -448, 2.0 ** -6, 2.0 ** -9, 2.0 ** -8, 0, 0,
+                     -0.3125, 240, 224], np.float32)
+    assert np.array_equal(oracle.round_e4m3(x), want)
+    b = np.array([1.00390625, 1.01171875, 3.14159, -2.0 ** -130, 65504.0], np.float32)
+    assert np.array_equal(oracle.round_bf16(b), np.array([1.0, 1.015625, 3.140625, -2.0 ** -130, 65536.0],
+                                                         np.float32))
+    # every E4M3 value is a fixed point
+    vals = np.array([s * m * 2.0 ** e for s in (1, -1) for e in range(-6, 9) for m in np.arange(8, 16) / 8
+                     if m * 2.0 ** e <= 448], np.float32)
+    assert np.array_equal(oracle.round_e4m3(vals), vals)
