@@ -559,7 +559,7 @@ def main():
             tms = timed_steps(lambda i: student.train_step((tuple(batch), (target,))), args.train_steps, 1)
             student.coarse_model.check_device_errors()
             train[tp] = {"rays_per_s": 4096 / (tms / 1000.0), "ms_per_step": tms,
-                         "gemms": "BF16 tensor cores (tcgen05 forward, cuBLASLt backward), FP32 accumulation"
+                         "gemms": "BF16 tcgen05 GEMMs forward and backward, FP32 accumulation"
                          if tp == "bf16" else "FP32 SIMT"}
 
     cpu = None

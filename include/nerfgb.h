@@ -9,11 +9,10 @@
  *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default
  *    stream). Every call is enqueued on it and returns without a host sync.
  *  - The caller allocates every output and workspace; no entry point
- *    allocates device memory per call. Two exceptions hold memory for the
- *    life of the process: the 16 MiB scratch array of
+ *    allocates device memory. One exception holds memory for the life of
+ *    the process: the 16 MiB scratch array of
  *    nerfgb_render_rays_noalloc (a static device array, reserved when the
- *    library's module loads on a device) and the cuBLASLt handle that the
- *    BF16 training backward creates on its first call.
+ *    library's module loads on a device).
  *  - Every entry point returns NERFGB_OK (0) or a negative NERFGB_E_* code.
  *    None aborts, throws or exits.
  *  - Kernels with bounded device-side waits report a timeout through
@@ -385,13 +384,14 @@ int nerfgb_mlp_forward_train_bf16(const void *packed_bf16, const float *xyz,
 long long nerfgb_mlp_backward_bf16_workspace_bytes(long long n_rows);
 
 /* nerfgb_mlp_backward from a BF16 tape: every dX and dW product is a BF16
- * GEMM with FP32 accumulation (cuBLASLt), against a BF16 copy of the FP32
- * master weights in packed_fp32 (the FP32 pack); bias and head gradients
- * in FP32. grad_params accumulates (zero it first). */
+ * tensor-core GEMM (tcgen05) with FP32 accumulation, against a BF16 copy of
+ * the FP32 master weights in packed_fp32 (the FP32 pack); bias and head
+ * gradients in FP32. grad_params accumulates (zero it first). err_word:
+ * caller-zeroed device int32 for the GEMMs' bounded waits. */
 int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tape,
                              long long n_rows, const float *d_rgb,
                              const float *d_sigma, float *grad_params,
-                             void *workspace, void *stream);
+                             void *workspace, int *err_word, void *stream);
 
 /* ---- fused render without allocation --------------------------------- */
 

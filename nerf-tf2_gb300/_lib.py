@@ -74,7 +74,7 @@ SIGNATURES = {
     "nerfgb_mlp_backward": (I, [P, P, LL, P, P, P, P, P]),
     "nerfgb_mlp_forward_train_bf16": (I, [P, P, P, LL, I, P, P, P, P, P]),
     "nerfgb_mlp_backward_bf16_workspace_bytes": (LL, [LL]),
-    "nerfgb_mlp_backward_bf16": (I, [P, P, LL, P, P, P, P, P]),
+    "nerfgb_mlp_backward_bf16": (I, [P, P, LL, P, P, P, P, P, P]),
     "nerfgb_render_rays_noalloc": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
                                        P, P, P, P, P, P, P, P]),
 }

@@ -17,8 +17,8 @@ CSRC = HERE / "csrc"
 INCLUDE = ROOT / "include"
 BUILD = HERE / "_build"
 LIB = HERE / "libnerfgb.so"
-SOURCES = ["ray_ops.cu", "mlp.cu", "mlp_tc.cu", "render.cu", "render_noalloc.cu", "train.cu", "proposal.cu",
-           "mlp_train.cu", "mlp_train_bf16.cu", "gate.cu"]
+SOURCES = ["ray_ops.cu", "mlp.cu", "mlp_tc.cu", "gemm_tc.cu", "render.cu", "render_noalloc.cu", "train.cu",
+           "proposal.cu", "mlp_train.cu", "mlp_train_bf16.cu", "gate.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -66,10 +66,7 @@ def build(force=False, verbose=False, extra_flags=()):
             if r.returncode != 0:
                 raise RuntimeError(f"nvcc failed on {cmd[-3]}")
     if force or jobs or _stale(LIB, objs):
-        # cuBLASLt: the BF16 training backward's plain GEMMs (mlp_train_bf16.cu)
-        libdir = str(pathlib.Path(nvcc()).resolve().parent.parent / "lib64")
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-L" + libdir, "-lcublasLt",
-               "-Xlinker", "-rpath," + libdir]
+        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stdout + r.stderr)

@@ -1,0 +1,393 @@
+// Tensor-core BF16 GEMMs of the MLP backward (the gradient tf.GradientTape
+// takes at nerf/core/model.py:148-170 through the Dense layers of
+// model.py:366-387), FP32 accumulation in TMEM:
+//
+//   C[M][N] = sum_k A[m][k] B[n][k]        (tcgen05.mma.cta_group::1.kind::f16)
+//
+// Operands are read from row-major global memory with 16-byte cp.async
+// copies into the no-swizzle core-matrix layout (8 rows x 16 bytes). The same
+// bytes serve both operand orientations: a row-major [rows][cols] tile copied
+// as "element (r, c) at (c/8)*S + r*16 + (c%8)*2" is
+//   K-major  when the reduction runs along cols (descriptor LBO = S, the
+//            stride between 8-column groups; SBO = 128, between 8-row groups),
+//   MN-major when the reduction runs along rows (LBO = 128, between 8-row
+//            groups of K; SBO = S, between 8-column groups of M or N; the
+//            instruction descriptor's transpose bit set).
+// The backward uses both:
+//   dX = dZ W^T   A = dZ [rows][n_out] (K-major), B = W [k_in][n_out]
+//                 (K-major), C = dX [rows][k_in] stored as BF16;
+//   dW = In^T dZ  A = In [rows][k_in] (MN-major: M = k_in), B = dZ
+//                 [rows][n_out] (MN-major: N = n_out), reduced over rows in
+//                 splits; each split's FP32 partial goes to a workspace and a
+//                 reduction kernel adds the splits into the gradient blob.
+//
+// Warp roles (9 warps): 0-3 epilogue (TMEM lane quadrant = warp), 4-7
+// loaders (cp.async into an NST-stage ring, full/empty mbarriers), 8 TMEM
+// allocation and the MMA issuer (one thread). Work items (an M tile, a split
+// of K) are taken persistently: item = blockIdx.x + i * gridDim.x. With one
+// 128-row M tile per item the accumulator is double-buffered in TMEM, so an
+// item's epilogue overlaps the next item's MMAs.
+//
+// Every mbarrier wait is bounded (tc::wait_bar): on a timeout the kernel
+// writes NERFGB_E_TIMEOUT to *err, every role stops, loaders drain their
+// copies, the issuer drains its MMAs, TMEM is freed and the kernel returns.
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "mlp_internal.cuh"
+#include "tcgen05.cuh"
+
+namespace nerfgb {
+namespace gemm {
+
+using namespace tc;
+
+constexpr int kKc = 64;                    // K per stage (4 MMAs of K = 16)
+constexpr int kEpiWarps = 4;
+constexpr int kLoadWarps = 4;
+constexpr int kLoadThreads = kLoadWarps * 32;
+constexpr int kIssuerWarp = kEpiWarps + kLoadWarps;
+constexpr int kThreads = (kIssuerWarp + 1) * 32;  // 288
+constexpr int kLag = 2;                    // loader stages in flight before it signals the oldest
+constexpr uint32_t kPad = 16;              // bytes added to a group stride (bank spread of the copies)
+
+enum Epi { kEpiBf16 = 0, kEpiF32 = 1 };
+
+struct Args {
+  const __nv_bfloat16 *A;  // K-major: [M][K] row stride lda; MN-major: [K][M] row stride lda
+  const __nv_bfloat16 *B;  // K-major: [N][K] row stride ldb; MN-major: [K][N] row stride ldb
+  long long lda, ldb;
+  long long M, N, K;       // N = the MMA's N (128 or 256); M and N rows past the operand bounds read 0
+  long long m_valid;       // rows of C written
+  long long k_split;       // K per work item (a multiple of kKc)
+  int m_tiles, k_splits;
+  void *C;                 // kEpiBf16: bf16 [M][ldc]; kEpiF32: float [k_splits][m_tiles * MT * 128][ldc]
+  long long ldc;
+  int *err;
+};
+
+// Stage geometry for MT 128-row M tiles per item.
+template <bool A_MN, bool B_MN, int MT>
+struct Geo {
+  // group strides (bytes) of the copied images
+  static constexpr uint32_t kSA = A_MN ? kKc * 16 + kPad : MT * 128 * 16 + kPad;  // A: per 8 M-cols / 8 K-cols
+  static constexpr uint32_t kSB = B_MN ? kKc * 16 + kPad : 256 * 16 + kPad;
+  static constexpr uint32_t kABytes = A_MN ? (MT * 128 / 8) * kSA : (kKc / 8) * kSA;
+  static constexpr uint32_t kBBytes = B_MN ? (256 / 8) * kSB : (kKc / 8) * kSB;
+  static constexpr uint32_t kStage = (kABytes + kBBytes + 127) / 128 * 128;
+  static constexpr int kNst = MT == 1 ? 4 : 3;
+  static constexpr uint32_t kRing = kNst * kStage;
+  static constexpr uint32_t kBarFull = kRing;            // [kNst]
+  static constexpr uint32_t kBarEmpty = kRing + 64;      // [kNst]
+  static constexpr uint32_t kBarAcc = kRing + 128;       // [2]
+  static constexpr uint32_t kBarTmem = kRing + 144;      // [2]
+  static constexpr uint32_t kBarDrain = kRing + 160;
+  static constexpr uint32_t kTmemSlot = kRing + 168;
+  static constexpr uint32_t kAbort = kRing + 172;
+  static constexpr uint32_t kSmem = kRing + 192;
+  static constexpr int kBufs = MT == 1 ? 2 : 1;          // TMEM accumulators (256 columns per 128-row tile)
+  static_assert(kNst <= 8 && kSmem <= 227 * 1024, "ring");
+};
+
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// Copies the [rows x 64] (K-major) or [64 x cols] (MN-major) piece of one
+// operand into a stage image. K-major: piece (r, kg) = X[r][k0 + 8kg ..]
+// -> kg*S + r*16. MN-major: piece (kr, g) = X[k0 + kr][c0 + 8g ..] -> g*S +
+// kr*16. Rows/columns past the bounds are zero-filled.
+template <bool MN, int ROWS>
+__device__ __forceinline__ void load_operand(uint32_t dst, const __nv_bfloat16 *X, long long ld, long long r0,
+                                             long long r_end, long long k0, long long k_end, uint32_t S, int t) {
+  constexpr int kPieces = ROWS * 8;  // 16-byte pieces per stage image
+#pragma unroll 4
+  for (int p = t; p < kPieces; p += kLoadThreads) {
+    if (!MN) {
+      const int r = p >> 3, kg = p & 7;
+      const long long gr = r0 + r, gk = k0 + 8 * kg;
+      const bool ok = gr < r_end && gk < k_end;
+      const __nv_bfloat16 *src = ok ? X + gr * ld + gk : X;
+      cp_async16(dst + (uint32_t)kg * S + (uint32_t)r * 16u, src, ok ? 16u : 0u);
+    } else {
+      constexpr int G = ROWS / 8;  // 8-element groups across the M (or N) extent
+      const int g = p % G, kr = p / G;
+      const long long gk = k0 + kr, gc = r0 + 8 * g;
+      const bool ok = gk < k_end && gc < r_end;
+      const __nv_bfloat16 *src = ok ? X + gk * ld + gc : X;
+      cp_async16(dst + (uint32_t)g * S + (uint32_t)kr * 16u, src, ok ? 16u : 0u);
+    }
+  }
+}
+
+template <bool A_MN, bool B_MN, int MT, int EPI>
+__global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
+  using G = Geo<A_MN, B_MN, MT>;
+  extern __shared__ __align__(1024) uint8_t smem[];
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(smem + G::kAbort);
+  const long long items = (long long)a.m_tiles * a.k_splits;
+  constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | ((A_MN ? 1u : 0u) << 15) |
+                              ((B_MN ? 1u : 0u) << 16) | ((128u >> 4) << 24);
+  const uint32_t idesc = kIdesc | ((uint32_t)(a.N >> 3) << 17);
+  // Chunks of item it: [k_begin, k_end) in steps of kKc.
+  auto item_range = [&](long long it, long long &mt, long long &kb, long long &ke) {
+    mt = it % a.m_tiles;
+    const long long ks = it / a.m_tiles;
+    kb = ks * a.k_split;
+    ke = kb + a.k_split < a.K ? kb + a.k_split : a.K;
+  };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < G::kNst; ++s) {
+      mbar_init(sbase + G::kBarFull + 8 * s, kLoadThreads);
+      mbar_init(sbase + G::kBarEmpty + 8 * s, 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(sbase + G::kBarAcc + 8 * b, 1);
+      mbar_init(sbase + G::kBarTmem + 8 * b, kEpiWarps);
+    }
+    mbar_init(sbase + G::kBarDrain, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == kIssuerWarp) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + G::kTmemSlot),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *reinterpret_cast<volatile uint32_t *>(smem + G::kTmemSlot);
+
+  if (warp >= kEpiWarps && warp < kIssuerWarp) {
+    // ---------------- loaders ----------------
+    const int t = threadIdx.x - kEpiWarps * 32;
+    long long q = 0, q_sig = 0;  // chunks issued, chunks signalled full
+    bool ok = true;
+    for (long long it = blockIdx.x; it < items && ok; it += gridDim.x) {
+      long long mt, kb, ke;
+      item_range(it, mt, kb, ke);
+      const long long m0 = mt * MT * 128;
+      for (long long k0 = kb; k0 < ke; k0 += kKc, ++q) {
+        const int st = (int)(q % G::kNst);
+        const uint32_t ph = (uint32_t)((q / G::kNst) & 1);
+        if (!wait_bar(sbase + G::kBarEmpty + 8 * st, ph ^ 1u, abort_flag, a.err)) {
+          ok = false;
+          break;
+        }
+        const uint32_t sa = sbase + st * G::kStage, sb = sa + G::kABytes;
+        load_operand<A_MN, MT * 128>(sa, a.A, a.lda, m0, a.M, k0, ke, G::kSA, t);
+        load_operand<B_MN, 256>(sb, a.B, a.ldb, 0, a.N, k0, ke, G::kSB, t);
+        cp_async_commit();
+        if (q - q_sig >= kLag) {
+          // the oldest pending stage has landed (this thread's copies): publish it
+          cp_async_wait<kLag>();
+          fence_proxy_async();
+          mbar_arrive(sbase + G::kBarFull + 8 * (int)(q_sig % G::kNst));
+          ++q_sig;
+        }
+      }
+    }
+    cp_async_wait<0>();
+    fence_proxy_async();
+    if (ok)
+      for (; q_sig < q; ++q_sig) mbar_arrive(sbase + G::kBarFull + 8 * (int)(q_sig % G::kNst));
+  } else if (warp == kIssuerWarp) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      long long q = 0, n_items = 0;
+      bool issued = false;
+      for (long long it = blockIdx.x; it < items; it += gridDim.x, ++n_items) {
+        if (*abort_flag) break;
+        long long mt, kb, ke;
+        item_range(it, mt, kb, ke);
+        const int b = G::kBufs == 2 ? (int)(n_items & 1) : 0;
+        if (n_items >= G::kBufs) {
+          // the epilogue has read this buffer's previous accumulator
+          const uint32_t ph = (uint32_t)(((n_items - G::kBufs) / G::kBufs) & 1);
+          if (!wait_bar(sbase + G::kBarTmem + 8 * b, ph, abort_flag, a.err)) break;
+          tc_fence_after();
+        }
+        const uint32_t d0 = tmem + (uint32_t)(b * MT) * 256u;
+        bool first = true;
+        for (long long k0 = kb; k0 < ke; k0 += kKc, ++q) {
+          const int st = (int)(q % G::kNst);
+          if (!wait_bar(sbase + G::kBarFull + 8 * st, (uint32_t)((q / G::kNst) & 1), abort_flag, a.err)) break;
+          tc_fence_after();
+          const uint32_t sa = (sbase + st * G::kStage) & 0x3FFFFu, sb = sa + G::kABytes;
+#pragma unroll
+          for (int s = 0; s < kKc / 16; ++s) {
+            // B: K-major k-step s = 2 column groups (2s * SB); MN-major = 2 row groups (2s * 128)
+            const uint64_t bdesc = B_MN ? smem_desc(sb + 256u * s, 128u, G::kSB) : smem_desc(sb + 2u * s * G::kSB, G::kSB, 128u);
+#pragma unroll
+            for (int h = 0; h < MT; ++h) {
+              const uint64_t adesc = A_MN ? smem_desc(sa + (uint32_t)h * 16u * G::kSA + 256u * s, 128u, G::kSA)
+                                          : smem_desc(sa + (uint32_t)h * 2048u + 2u * s * G::kSA, G::kSA, 128u);
+              tc_mma(d0 + (uint32_t)h * 256u, adesc, bdesc, idesc, (first && s == 0) ? 0u : 1u);
+            }
+          }
+          first = false;
+          issued = true;
+          tc_commit(sbase + G::kBarEmpty + 8 * st);
+        }
+        if (*abort_flag) break;
+        tc_commit(sbase + G::kBarAcc + 8 * b);
+      }
+      if (issued) {
+        tc_commit(sbase + G::kBarDrain);
+        const uint64_t t0 = globaltimer();
+        while (!mbar_try(sbase + G::kBarDrain, 0) && globaltimer() - t0 < 100000000ull) {
+        }
+      }
+    }
+  } else {
+    // ---------------- epilogue ----------------
+    long long n_items = 0;
+    for (long long it = blockIdx.x; it < items; it += gridDim.x, ++n_items) {
+      long long mt, kb, ke;
+      item_range(it, mt, kb, ke);
+      const int b = G::kBufs == 2 ? (int)(n_items & 1) : 0;
+      const uint32_t ph = (uint32_t)((n_items / G::kBufs) & 1);
+      if (!__all_sync(0xffffffffu, wait_bar(sbase + G::kBarAcc + 8 * b, ph, abort_flag, a.err))) break;
+      tc_fence_after();
+      const long long ks = it / a.m_tiles;
+#pragma unroll 1
+      for (int h = 0; h < MT; ++h) {
+        const long long r = mt * MT * 128 + h * 128 + 32 * warp + lane;  // row of C (= TMEM lane)
+        const uint32_t tl = tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)(b * MT + h) * 256u;
+#pragma unroll 1
+        for (int j = 0; j < (int)(a.N / 32); ++j) {
+          uint32_t raw[32];
+          tmem_ld32(tl + 32u * j, raw);
+          tmem_wait32(raw);
+          if (EPI == kEpiBf16) {
+            if (r < a.m_valid) {
+              uint4 *dst = reinterpret_cast<uint4 *>(reinterpret_cast<__nv_bfloat16 *>(a.C) + r * a.ldc + 32 * j);
+#pragma unroll
+              for (int q4 = 0; q4 < 4; ++q4)
+                dst[q4] = make_uint4(pack_bf16(__uint_as_float(raw[8 * q4]), __uint_as_float(raw[8 * q4 + 1])),
+                                     pack_bf16(__uint_as_float(raw[8 * q4 + 2]), __uint_as_float(raw[8 * q4 + 3])),
+                                     pack_bf16(__uint_as_float(raw[8 * q4 + 4]), __uint_as_float(raw[8 * q4 + 5])),
+                                     pack_bf16(__uint_as_float(raw[8 * q4 + 6]), __uint_as_float(raw[8 * q4 + 7])));
+            }
+          } else {
+            // this split's partial (every row of the tile; the reduction reads the valid ones)
+            float4 *dst = reinterpret_cast<float4 *>(reinterpret_cast<float *>(a.C) +
+                                                     (ks * a.m_tiles * MT * 128 + r) * a.ldc + 32 * j);
+#pragma unroll
+            for (int q4 = 0; q4 < 8; ++q4)
+              dst[q4] = make_float4(__uint_as_float(raw[4 * q4]), __uint_as_float(raw[4 * q4 + 1]),
+                                    __uint_as_float(raw[4 * q4 + 2]), __uint_as_float(raw[4 * q4 + 3]));
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(sbase + G::kBarTmem + 8 * b);
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == kIssuerWarp) {
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+  }
+}
+
+// grads[r][c] += sum_s part[s][r][c] for r < rows, c < cols (part row stride
+// ld, split stride split_rows * ld); grads row stride gld.
+__global__ void reduce_splits_kernel(const float *__restrict__ part, int splits, long long split_rows, int ld,
+                                     int rows, int cols, float *__restrict__ grads, int gld) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)rows * cols) return;
+  const int r = (int)(e / cols), c = (int)(e % cols);
+  float s = 0.0f;
+  for (int k = 0; k < splits; ++k) s += part[(k * split_rows + r) * ld + c];
+  grads[(long long)r * gld + c] += s;
+}
+
+template <bool A_MN, bool B_MN, int MT, int EPI>
+static int launch(const Args &a, cudaStream_t st) {
+  using G = Geo<A_MN, B_MN, MT>;
+  auto kern = gemm_kernel<A_MN, B_MN, MT, EPI>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kSmem) != cudaSuccess)
+    return NERFGB_E_CUDA;
+  const int sms = num_sms();
+  if (sms <= 0) return NERFGB_E_DEVICE;
+  const long long items = (long long)a.m_tiles * a.k_splits;
+  if (items == 0) return NERFGB_OK;
+  const int grid = (int)(items < sms ? items : sms);
+  kern<<<grid, kThreads, G::kSmem, st>>>(a);
+  return launch_status();
+}
+
+}  // namespace gemm
+
+// dX [M][256] (BF16, row stride 256) = dZ [M][n_out] (BF16, row stride 256)
+// times W^T, W = the layer's BF16 weights [k_in][n_out] (rows 0..255 used).
+int launch_gemm_dx(const __nv_bfloat16 *dz, long long M, int n_out, const __nv_bfloat16 *W, __nv_bfloat16 *dx,
+                   int *err, cudaStream_t st) {
+  gemm::Args a{};
+  a.A = dz;
+  a.lda = 256;
+  a.B = W;
+  a.ldb = n_out;
+  a.M = M;
+  a.N = 256;
+  a.K = n_out;
+  a.m_valid = M;
+  a.k_split = ((n_out + gemm::kKc - 1) / gemm::kKc) * gemm::kKc;
+  a.m_tiles = (int)((M + 127) / 128);
+  a.k_splits = 1;
+  a.C = dx;
+  a.ldc = 256;
+  a.err = err;
+  return gemm::launch<false, false, 1, gemm::kEpiBf16>(a, st);
+}
+
+// Rows of split partials the dW GEMM writes for M rows (workspace sizing).
+long long gemm_dw_partial_floats(int splits) { return (long long)splits * 256 * 256; }
+
+// grads (row stride n_out) [k][n] += sum_m In[m][k] dZ[m][n] for k < k_in
+// (In: BF16, row stride ld_in; k_in <= 256: 128 or 256-row M tiles), with
+// `splits` partial sums in `part` (gemm_dw_partial_floats(splits) floats).
+int launch_gemm_dw(const __nv_bfloat16 *in, long long ld_in, int k_in, const __nv_bfloat16 *dz, int n_out,
+                   long long M, float *grads, float *part, int splits, int *err, cudaStream_t st) {
+  if (k_in < 1 || k_in > 256 || (n_out != 128 && n_out != 256) || splits < 1) return NERFGB_E_UNSUPPORTED;
+  gemm::Args a{};
+  a.A = in;
+  a.lda = ld_in;
+  a.B = dz;
+  a.ldb = 256;
+  a.M = k_in <= 128 ? 128 : 256;
+  a.N = n_out;
+  a.K = M;
+  a.m_valid = k_in;
+  const long long chunks = (M + gemm::kKc - 1) / gemm::kKc;
+  const long long per = (chunks + splits - 1) / splits;
+  a.k_split = per * gemm::kKc;
+  a.k_splits = (int)((chunks + per - 1) / per);
+  a.m_tiles = 1;
+  a.C = part;
+  a.ldc = 256;
+  a.err = err;
+  const int rc = k_in <= 128 ? gemm::launch<true, true, 1, gemm::kEpiF32>(a, st)
+                             : gemm::launch<true, true, 2, gemm::kEpiF32>(a, st);
+  if (rc != NERFGB_OK) return rc;
+  const long long n = (long long)k_in * n_out;
+  gemm::reduce_splits_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, a.k_splits, a.M, 256, k_in, n_out,
+                                                                           grads, n_out);
+  return launch_status();
+}
+
+}  // namespace nerfgb

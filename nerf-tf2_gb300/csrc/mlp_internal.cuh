@@ -1,5 +1,6 @@
 // Launchers shared between the MLP translation units.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -39,6 +40,19 @@ int launch_head_bwd(const float *table, const float *tape, long long n, const fl
                     float *dz9, float *dsp, float *grads, cudaStream_t stream);
 int launch_head_bwd(const float *table, const uint16_t *tape, long long n, const float *d_rgb,
                     const float *d_sigma, float *dz9, float *dsp, float *grads, cudaStream_t stream);
+
+// Tensor-core GEMMs of the BF16 backward (gemm_tc.cu). dX [M][256] (BF16) =
+// dZ [M][n_out] (BF16, row stride 256) W^T with W the layer's BF16 weights
+// [k_in][n_out] (rows 0..255 used).
+int launch_gemm_dx(const __nv_bfloat16 *dz, long long M, int n_out, const __nv_bfloat16 *W, __nv_bfloat16 *dx,
+                   int *err, cudaStream_t stream);
+// grads [k][n] (row stride n_out) += sum_m In[m][k] dZ[m][n], k < k_in <= 256,
+// In BF16 with row stride ld_in, dZ BF16 with row stride 256; the rows are
+// reduced in `splits` parts whose partial sums go to `part`
+// (gemm_dw_partial_floats(splits) floats) before they are added.
+int launch_gemm_dw(const __nv_bfloat16 *in, long long ld_in, int k_in, const __nv_bfloat16 *dz, int n_out,
+                   long long M, float *grads, float *part, int splits, int *err, cudaStream_t stream);
+long long gemm_dw_partial_floats(int splits);
 
 // FP8-e4m3 tcgen05 forward (mlp_tc.cu).
 int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,

@@ -4,17 +4,13 @@
 // The forward is the tensor-core BF16 kernel with its tape (mlp_tc.cu,
 // STORE): each layer's BF16 activations are exactly the operands its
 // successor's MMAs read. The backward runs the layers of mlp_train.cu from
-// the heads down, with every product a BF16 GEMM accumulating in FP32:
+// the heads down, with every product a BF16 tensor-core GEMM accumulating in
+// FP32 (gemm_tc.cu):
 //   prep    z = dX (+ dpre_sigma * ws at dense_7) * [h > 0]  (dX in BF16
 //           from the GEMM, z in FP32), dz = bf16(z), db += column sums of z
 //   dW      grads[k][n] += sum_m In[m][k] dz[m][n]   (In = the tape's BF16 input columns)
 //   dX      dX[m][k] = sum_n dz[m][n] W[k][n], k < 256 (W = BF16 copy of the FP32 master weights)
-// The two products are plain GEMMs and go to cuBLASLt; everything around
-// them (heads, masks, bias sums, conversion) is in this library's kernels.
-#include <cublasLt.h>
 #include <cuda_bf16.h>
-
-#include <mutex>
 
 #include "common.cuh"
 #include "mlp_internal.cuh"
@@ -23,83 +19,8 @@ namespace nerfgb {
 namespace train16 {
 
 constexpr int kDzLd = 256;                    // row stride of the dZ buffers
-constexpr long long kLtWsBytes = 32ll << 20;  // cuBLASLt workspace
+constexpr int kMaxSplits = 160;               // row splits of a dW GEMM (partial sums in the workspace)
 constexpr int kPrepRows = 1024;               // rows per prep block
-
-static cublasLtHandle_t lt_handle() {
-  static std::mutex mu;
-  static cublasLtHandle_t handles[64] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return nullptr;
-  std::lock_guard<std::mutex> lock(mu);
-  if (!handles[dev] && cublasLtCreate(&handles[dev]) != CUBLAS_STATUS_SUCCESS) handles[dev] = nullptr;
-  return handles[dev];
-}
-
-// Largest power of two (<= 256) dividing the address.
-static uint32_t align_of(const void *p) {
-  const uintptr_t a = reinterpret_cast<uintptr_t>(p);
-  uint32_t al = 256;
-  while (al > 1 && (a % al) != 0) al >>= 1;
-  return al;
-}
-
-// C (column-major m x n, ldc; FP32 or BF16 per ctype) = op(A) op(B) + beta C;
-// A, B BF16 column-major with leading dimensions lda, ldb; FP32 accumulation.
-static int gemm(cublasOperation_t ta, cublasOperation_t tb, long long m, long long n, long long k, const void *A,
-                long long lda, const void *B, long long ldb, float beta, void *C, cudaDataType_t ctype, long long ldc,
-                void *ws, cudaStream_t st) {
-  if (m == 0 || n == 0) return NERFGB_OK;
-  cublasLtHandle_t h = lt_handle();
-  if (!h) return NERFGB_E_CUDA;
-  cublasLtMatmulDesc_t op = nullptr;
-  cublasLtMatrixLayout_t la = nullptr, lb = nullptr, lc = nullptr;
-  cublasLtMatmulPreference_t pref = nullptr;
-  int rc = NERFGB_E_CUDA;
-  const float alpha = 1.0f;
-  const uint64_t ws_bytes = (uint64_t)kLtWsBytes;
-  cublasLtMatmulHeuristicResult_t res{};
-  int nres = 0;
-  if (cublasLtMatmulDescCreate(&op, CUBLAS_COMPUTE_32F, CUDA_R_32F) != CUBLAS_STATUS_SUCCESS) goto done;
-  if (cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSA, &ta, sizeof(ta)) != CUBLAS_STATUS_SUCCESS ||
-      cublasLtMatmulDescSetAttribute(op, CUBLASLT_MATMUL_DESC_TRANSB, &tb, sizeof(tb)) != CUBLAS_STATUS_SUCCESS)
-    goto done;
-  if (cublasLtMatrixLayoutCreate(&la, CUDA_R_16BF, ta == CUBLAS_OP_N ? m : k, ta == CUBLAS_OP_N ? k : m, lda) !=
-          CUBLAS_STATUS_SUCCESS ||
-      cublasLtMatrixLayoutCreate(&lb, CUDA_R_16BF, tb == CUBLAS_OP_N ? k : n, tb == CUBLAS_OP_N ? n : k, ldb) !=
-          CUBLAS_STATUS_SUCCESS ||
-      cublasLtMatrixLayoutCreate(&lc, ctype, m, n, ldc) != CUBLAS_STATUS_SUCCESS)
-    goto done;
-  if (cublasLtMatmulPreferenceCreate(&pref) != CUBLAS_STATUS_SUCCESS ||
-      cublasLtMatmulPreferenceSetAttribute(pref, CUBLASLT_MATMUL_PREF_MAX_WORKSPACE_BYTES, &ws_bytes,
-                                           sizeof(ws_bytes)) != CUBLAS_STATUS_SUCCESS)
-    goto done;
-  {
-    // the heuristic assumes 256-byte aligned operands unless told otherwise
-    // (gradient blocks of the flat parameter blob are only 4-byte aligned)
-    const uint32_t al[3] = {align_of(A), align_of(B), align_of(C)};
-    const cublasLtMatmulPreferenceAttributes_t at[4] = {
-        CUBLASLT_MATMUL_PREF_MIN_ALIGNMENT_A_BYTES, CUBLASLT_MATMUL_PREF_MIN_ALIGNMENT_B_BYTES,
-        CUBLASLT_MATMUL_PREF_MIN_ALIGNMENT_C_BYTES, CUBLASLT_MATMUL_PREF_MIN_ALIGNMENT_D_BYTES};
-    for (int i = 0; i < 4; ++i)
-      if (cublasLtMatmulPreferenceSetAttribute(pref, at[i], &al[i < 3 ? i : 2], sizeof(uint32_t)) !=
-          CUBLAS_STATUS_SUCCESS)
-        goto done;
-  }
-  if (cublasLtMatmulAlgoGetHeuristic(h, op, la, lb, lc, lc, pref, 1, &res, &nres) != CUBLAS_STATUS_SUCCESS ||
-      nres < 1)
-    goto done;
-  if (cublasLtMatmul(h, op, &alpha, A, la, B, lb, &beta, C, lc, C, lc, &res.algo, ws, (size_t)ws_bytes, st) ==
-      CUBLAS_STATUS_SUCCESS)
-    rc = NERFGB_OK;
-done:
-  if (pref) cublasLtMatmulPreferenceDestroy(pref);
-  if (lc) cublasLtMatrixLayoutDestroy(lc);
-  if (lb) cublasLtMatrixLayoutDestroy(lb);
-  if (la) cublasLtMatrixLayoutDestroy(la);
-  if (op) cublasLtMatmulDescDestroy(op);
-  return rc;
-}
 
 __global__ void to_bf16_kernel(const float *__restrict__ src, __nv_bfloat16 *__restrict__ dst, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -185,7 +106,7 @@ __global__ void __launch_bounds__(256)
 struct Ws {
   float *f32, *dsp;                  // dZ9 from the heads (FP32), dpre_sigma
   __nv_bfloat16 *raw, *dz, *wb;      // dX output, masked dZ (GEMM operand), BF16 weights
-  void *lt;
+  float *part;                       // dW split partials
   long long bytes;
 };
 
@@ -204,7 +125,7 @@ static Ws carve(void *base, long long n) {
   w.raw = reinterpret_cast<__nv_bfloat16 *>(take(n * kDzLd * 2));
   w.dz = reinterpret_cast<__nv_bfloat16 *>(take(n * kDzLd * 2));
   w.wb = reinterpret_cast<__nv_bfloat16 *>(take(kGemmWElems * 2));
-  w.lt = take(kLtWsBytes);
+  w.part = reinterpret_cast<float *>(take(gemm_dw_partial_floats(kMaxSplits) * 4));
   w.bytes = off;
   return w;
 }
@@ -220,17 +141,20 @@ static int prep(const Tin *raw, long long M, int N, const uint16_t *tape, int ac
 // grads (flat layer fl, rows [k_dst0, k_dst0 + K)) += In^T dz, In = tape
 // columns [in_off, in_off + K).
 static int dW(const uint16_t *tape, int in_off, int K, const __nv_bfloat16 *dz, int N, long long M, float *grads,
-              int fl, int k_dst0, void *lt, cudaStream_t st) {
-  return gemm(CUBLAS_OP_N, CUBLAS_OP_T, N, K, M, dz, kDzLd, tape + in_off, kActsLd, 1.0f,
-              grads + flat_offset(fl) + (long long)k_dst0 * N, CUDA_R_32F, N, lt, st);
+              int fl, int k_dst0, float *part, int *err, cudaStream_t st) {
+  const int sms = num_sms();
+  if (sms <= 0) return NERFGB_E_DEVICE;
+  const long long chunks = (M + 63) / 64;
+  int splits = sms < kMaxSplits ? sms : kMaxSplits;
+  if (chunks < splits) splits = (int)chunks;
+  return launch_gemm_dw(reinterpret_cast<const __nv_bfloat16 *>(tape) + in_off, kActsLd, K, dz, N, M,
+                        grads + flat_offset(fl) + (long long)k_dst0 * N, part, splits, err, st);
 }
 
 // out [M][256] (BF16) = dz [M][N] W_g[0:256][N]^T.
-static int dX(const __nv_bfloat16 *wb, int g, const __nv_bfloat16 *dz, long long M, __nv_bfloat16 *out, void *lt,
+static int dX(const __nv_bfloat16 *wb, int g, const __nv_bfloat16 *dz, long long M, __nv_bfloat16 *out, int *err,
               cudaStream_t st) {
-  const int N = gemm_n(g);
-  return gemm(CUBLAS_OP_T, CUBLAS_OP_N, 256, M, N, wb + gemm_w_offset(g), N, dz, kDzLd, 0.0f, out, CUDA_R_16BF,
-              kDzLd, lt, st);
+  return launch_gemm_dx(dz, M, gemm_n(g), wb + gemm_w_offset(g), out, err, st);
 }
 
 static float *bias_grad(float *grads, int fl) { return grads + flat_offset(fl) + (long long)flat_in(fl) * flat_out(fl); }
@@ -259,13 +183,14 @@ extern "C" int nerfgb_mlp_forward_train_bf16(const void *packed_bf16, const floa
 
 extern "C" int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tape, long long n_rows,
                                         const float *d_rgb, const float *d_sigma, float *grad_params,
-                                        void *workspace, void *stream) {
+                                        void *workspace, int *err_word, void *stream) {
   using namespace train16;
   if (n_rows < 0) return NERFGB_E_INVALID_ARG;
   if (n_rows == 0) return NERFGB_OK;
-  if (!packed_fp32 || !tape || !d_rgb || !grad_params || !workspace || !aligned(packed_fp32, 256) ||
+  if (!packed_fp32 || !tape || !d_rgb || !grad_params || !workspace || !err_word || !aligned(packed_fp32, 256) ||
       !aligned(tape, 16) || !aligned(workspace, 256))
     return NERFGB_E_INVALID_ARG;
+  int *err = err_word;
   cudaStream_t st = as_stream(stream);
   const long long M = n_rows;
   const float *W = reinterpret_cast<const float *>(packed_fp32);  // FP32 pack: [Kp][N] blocks, then the table
@@ -281,15 +206,15 @@ extern "C" int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tap
   if ((rc = prep<false, false>(w.f32, M, 128, tp, 0, nullptr, nullptr, w.dz, bias_grad(grad_params, 10), st)) !=
       NERFGB_OK)
     return rc;
-  if ((rc = dW(tp, acts_offset(8), 256, w.dz, 128, M, grad_params, 10, 0, w.lt, st)) != NERFGB_OK) return rc;
-  if ((rc = dW(tp, kActsEncDir, 27, w.dz, 128, M, grad_params, 10, 256, w.lt, st)) != NERFGB_OK) return rc;
-  if ((rc = dX(w.wb, 9, w.dz, M, w.raw, w.lt, st)) != NERFGB_OK) return rc;
+  if ((rc = dW(tp, acts_offset(8), 256, w.dz, 128, M, grad_params, 10, 0, w.part, err, st)) != NERFGB_OK) return rc;
+  if ((rc = dW(tp, kActsEncDir, 27, w.dz, 128, M, grad_params, 10, 256, w.part, err, st)) != NERFGB_OK) return rc;
+  if ((rc = dX(w.wb, 9, w.dz, M, w.raw, err, st)) != NERFGB_OK) return rc;
   // dense_8 (flat 9): linear, input h7
   if ((rc = prep<false, false>(w.raw, M, 256, tp, 0, nullptr, nullptr, w.dz, bias_grad(grad_params, 9), st)) !=
       NERFGB_OK)
     return rc;
-  if ((rc = dW(tp, acts_offset(7), 256, w.dz, 256, M, grad_params, 9, 0, w.lt, st)) != NERFGB_OK) return rc;
-  if ((rc = dX(w.wb, 8, w.dz, M, w.raw, w.lt, st)) != NERFGB_OK) return rc;
+  if ((rc = dW(tp, acts_offset(7), 256, w.dz, 256, M, grad_params, 9, 0, w.part, err, st)) != NERFGB_OK) return rc;
+  if ((rc = dX(w.wb, 8, w.dz, M, w.raw, err, st)) != NERFGB_OK) return rc;
   // dense_7 .. dense_0
   for (int l = 7; l >= 0; --l) {
     float *db = bias_grad(grad_params, l);
@@ -297,16 +222,16 @@ extern "C" int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tap
                   : prep<true, false>(w.raw, M, 256, tp, acts_offset(l), nullptr, nullptr, w.dz, db, st);
     if (rc != NERFGB_OK) return rc;
     if (l == 0) {
-      if ((rc = dW(tp, kActsEncXyz, 63, w.dz, 256, M, grad_params, 0, 0, w.lt, st)) != NERFGB_OK) return rc;
+      if ((rc = dW(tp, kActsEncXyz, 63, w.dz, 256, M, grad_params, 0, 0, w.part, err, st)) != NERFGB_OK) return rc;
       break;
     }
     if (l == 5) {
-      if ((rc = dW(tp, acts_offset(4), 256, w.dz, 256, M, grad_params, 5, 0, w.lt, st)) != NERFGB_OK) return rc;
-      if ((rc = dW(tp, kActsEncXyz, 63, w.dz, 256, M, grad_params, 5, 256, w.lt, st)) != NERFGB_OK) return rc;
+      if ((rc = dW(tp, acts_offset(4), 256, w.dz, 256, M, grad_params, 5, 0, w.part, err, st)) != NERFGB_OK) return rc;
+      if ((rc = dW(tp, kActsEncXyz, 63, w.dz, 256, M, grad_params, 5, 256, w.part, err, st)) != NERFGB_OK) return rc;
     } else {
-      if ((rc = dW(tp, acts_offset(l - 1), 256, w.dz, 256, M, grad_params, l, 0, w.lt, st)) != NERFGB_OK) return rc;
+      if ((rc = dW(tp, acts_offset(l - 1), 256, w.dz, 256, M, grad_params, l, 0, w.part, err, st)) != NERFGB_OK) return rc;
     }
-    if ((rc = dX(w.wb, l, w.dz, M, w.raw, w.lt, st)) != NERFGB_OK) return rc;
+    if ((rc = dX(w.wb, l, w.dz, M, w.raw, err, st)) != NERFGB_OK) return rc;
   }
   return NERFGB_OK;
 }

@@ -132,7 +132,8 @@ class NerfMLP:
         """Accumulates the parameter gradient of sum(d_rgb*rgb + d_sigma*sigma)
         into grad_params (flat Keras layout). An FP32 tape takes the FP32
         backward; a BF16 tape (from ``forward_train(precision="bf16")``) the
-        BF16 one (BF16 GEMMs, FP32 accumulation, FP32 gradients)."""
+        BF16 one (BF16 tensor-core GEMMs, FP32 accumulation, FP32
+        gradients; a bounded-wait timeout lands in err_word)."""
         n = acts.shape[0]
         d_rgb = as_cuda(d_rgb, shape=(n, 3), name="d_rgb")
         d_sigma = as_cuda(d_sigma, shape=(n,), name="d_sigma")
@@ -140,8 +141,12 @@ class NerfMLP:
         bf16 = acts.dtype == torch.int16
         nbytes = (lib.nerfgb_mlp_backward_bf16_workspace_bytes if bf16 else lib.nerfgb_mlp_backward_workspace_bytes)(n)
         ws = torch.empty(int(nbytes), dtype=torch.uint8, device=acts.device)
-        _lib.call("nerfgb_mlp_backward_bf16" if bf16 else "nerfgb_mlp_backward", ptr(self.packed("fp32")),
-                  ptr(acts), n, ptr(d_rgb), ptr(d_sigma), ptr(grad_params), ptr(ws), stream())
+        if bf16:
+            _lib.call("nerfgb_mlp_backward_bf16", ptr(self.packed("fp32")), ptr(acts), n, ptr(d_rgb),
+                      ptr(d_sigma), ptr(grad_params), ptr(ws), ptr(self.err_word), stream())
+        else:
+            _lib.call("nerfgb_mlp_backward", ptr(self.packed("fp32")), ptr(acts), n, ptr(d_rgb), ptr(d_sigma),
+                      ptr(grad_params), ptr(ws), stream())
         return grad_params
 
     def check_device_errors(self):

