@@ -67,27 +67,33 @@ struct Args {
   int *err;
 };
 
-// Stage geometry for MT 128-row M tiles per item.
-template <bool A_MN, bool B_MN, int MT>
+// Stage geometry for MT 128-row M tiles per item. B_RES: B (K-major, all of
+// K <= 256) is loaded once per CTA into its own region after the ring and
+// the stages hold A alone.
+template <bool A_MN, bool B_MN, int MT, bool B_RES = false>
 struct Geo {
   // group strides (bytes) of the copied images
   static constexpr uint32_t kSA = A_MN ? kKc * 16 + kPad : MT * 128 * 16 + kPad;  // A: per 8 M-cols / 8 K-cols
   static constexpr uint32_t kSB = B_MN ? kKc * 16 + kPad : 256 * 16 + kPad;
   static constexpr uint32_t kABytes = A_MN ? (MT * 128 / 8) * kSA : (kKc / 8) * kSA;
-  static constexpr uint32_t kBBytes = B_MN ? (256 / 8) * kSB : (kKc / 8) * kSB;
+  static constexpr uint32_t kBBytes = B_RES ? 0 : B_MN ? (256 / 8) * kSB : (kKc / 8) * kSB;
   static constexpr uint32_t kStage = (kABytes + kBBytes + 127) / 128 * 128;
-  static constexpr int kNst = MT == 1 ? 4 : 3;
+  static constexpr int kNst = B_RES ? 4 : MT == 1 ? 4 : 3;
   static constexpr uint32_t kRing = kNst * kStage;
-  static constexpr uint32_t kBarFull = kRing;            // [kNst]
-  static constexpr uint32_t kBarEmpty = kRing + 64;      // [kNst]
-  static constexpr uint32_t kBarAcc = kRing + 128;       // [2]
-  static constexpr uint32_t kBarTmem = kRing + 144;      // [2]
-  static constexpr uint32_t kBarDrain = kRing + 160;
-  static constexpr uint32_t kTmemSlot = kRing + 168;
-  static constexpr uint32_t kAbort = kRing + 172;
-  static constexpr uint32_t kSmem = kRing + 192;
+  static constexpr uint32_t kBRes = kRing;                               // resident B: 32 column groups
+  static constexpr uint32_t kBar0 = kRing + (B_RES ? 32 * kSB : 0);
+  static constexpr uint32_t kBarFull = kBar0;            // [kNst]
+  static constexpr uint32_t kBarEmpty = kBar0 + 64;      // [kNst]
+  static constexpr uint32_t kBarAcc = kBar0 + 128;       // [2]
+  static constexpr uint32_t kBarTmem = kBar0 + 144;      // [2]
+  static constexpr uint32_t kBarDrain = kBar0 + 160;
+  static constexpr uint32_t kBarB = kBar0 + 168;
+  static constexpr uint32_t kTmemSlot = kBar0 + 176;
+  static constexpr uint32_t kAbort = kBar0 + 180;
+  static constexpr uint32_t kSmem = kBar0 + 192;
   static constexpr int kBufs = MT == 1 ? 2 : 1;          // TMEM accumulators (256 columns per 128-row tile)
   static_assert(kNst <= 8 && kSmem <= 227 * 1024, "ring");
+  static_assert(!B_RES || (!B_MN && MT == 1), "resident B: K-major, one M tile");
 };
 
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src, uint32_t src_bytes) {
@@ -126,9 +132,9 @@ __device__ __forceinline__ void load_operand(uint32_t dst, const __nv_bfloat16 *
   }
 }
 
-template <bool A_MN, bool B_MN, int MT, int EPI>
+template <bool A_MN, bool B_MN, int MT, int EPI, bool B_RES = false>
 __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
-  using G = Geo<A_MN, B_MN, MT>;
+  using G = Geo<A_MN, B_MN, MT, B_RES>;
   extern __shared__ __align__(1024) uint8_t smem[];
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -155,6 +161,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
       mbar_init(sbase + G::kBarTmem + 8 * b, kEpiWarps);
     }
     mbar_init(sbase + G::kBarDrain, 1);
+    mbar_init(sbase + G::kBarB, kLoadThreads);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -171,6 +178,20 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
   if (warp >= kEpiWarps && warp < kIssuerWarp) {
     // ---------------- loaders ----------------
     const int t = threadIdx.x - kEpiWarps * 32;
+    if (B_RES) {
+      // all of B (K <= 256 columns): piece (n, 8-column group g) -> g*SB + n*16
+      const int ng = (int)((a.K + 7) / 8);
+      for (int p = t; p < 256 * ng; p += kLoadThreads) {
+        const int g = p % ng, n = p / ng;
+        const bool ok = n < a.N;
+        cp_async16(sbase + G::kBRes + (uint32_t)g * G::kSB + (uint32_t)n * 16u,
+                   ok ? a.B + (long long)n * a.ldb + 8 * g : a.B, ok ? 16u : 0u);
+      }
+      cp_async_commit();
+      cp_async_wait<0>();
+      fence_proxy_async();
+      mbar_arrive(sbase + G::kBarB);
+    }
     long long q = 0, q_sig = 0;  // chunks issued, chunks signalled full
     bool ok = true;
     for (long long it = blockIdx.x; it < items && ok; it += gridDim.x) {
@@ -186,7 +207,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
         }
         const uint32_t sa = sbase + st * G::kStage, sb = sa + G::kABytes;
         load_operand<A_MN, MT * 128>(sa, a.A, a.lda, m0, a.M, k0, ke, G::kSA, t);
-        load_operand<B_MN, 256>(sb, a.B, a.ldb, 0, a.N, k0, ke, G::kSB, t);
+        if (!B_RES) load_operand<B_MN, 256>(sb, a.B, a.ldb, 0, a.N, k0, ke, G::kSB, t);
         cp_async_commit();
         if (q - q_sig >= kLag) {
           // the oldest pending stage has landed (this thread's copies): publish it
@@ -206,6 +227,9 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
     if (lane == 0) {
       long long q = 0, n_items = 0;
       bool issued = false;
+      if (B_RES) {
+        if (wait_bar(sbase + G::kBarB, 0, abort_flag, a.err)) tc_fence_after();
+      }
       for (long long it = blockIdx.x; it < items; it += gridDim.x, ++n_items) {
         if (*abort_flag) break;
         long long mt, kb, ke;
@@ -223,7 +247,10 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
           const int st = (int)(q % G::kNst);
           if (!wait_bar(sbase + G::kBarFull + 8 * st, (uint32_t)((q / G::kNst) & 1), abort_flag, a.err)) break;
           tc_fence_after();
-          const uint32_t sa = (sbase + st * G::kStage) & 0x3FFFFu, sb = sa + G::kABytes;
+          const uint32_t sa = (sbase + st * G::kStage) & 0x3FFFFu;
+          // resident B: this chunk's column groups start at k0 / 8
+          const uint32_t sb = B_RES ? ((sbase + G::kBRes) & 0x3FFFFu) + (uint32_t)(k0 / 8) * G::kSB
+                                    : sa + G::kABytes;
 #pragma unroll
           for (int s = 0; s < kKc / 16; ++s) {
             // B: K-major k-step s = 2 column groups (2s * SB); MN-major = 2 row groups (2s * 128)
@@ -316,10 +343,10 @@ __global__ void reduce_splits_kernel(const float *__restrict__ part, int splits,
   grads[(long long)r * gld + c] += s;
 }
 
-template <bool A_MN, bool B_MN, int MT, int EPI>
+template <bool A_MN, bool B_MN, int MT, int EPI, bool B_RES = false>
 static int launch(const Args &a, cudaStream_t st) {
-  using G = Geo<A_MN, B_MN, MT>;
-  auto kern = gemm_kernel<A_MN, B_MN, MT, EPI>;
+  using G = Geo<A_MN, B_MN, MT, B_RES>;
+  auto kern = gemm_kernel<A_MN, B_MN, MT, EPI, B_RES>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)G::kSmem) != cudaSuccess)
     return NERFGB_E_CUDA;
   const int sms = num_sms();
@@ -352,7 +379,8 @@ int launch_gemm_dx(const __nv_bfloat16 *dz, long long M, int n_out, const __nv_b
   a.C = dx;
   a.ldc = 256;
   a.err = err;
-  return gemm::launch<false, false, 1, gemm::kEpiBf16>(a, st);
+  // W^T (at most 256 x 256 BF16) stays in shared memory for the whole launch
+  return gemm::launch<false, false, 1, gemm::kEpiBf16, true>(a, st);
 }
 
 // Rows of split partials the dW GEMM writes for M rows (workspace sizing).

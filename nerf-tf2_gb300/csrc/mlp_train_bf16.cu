@@ -9,7 +9,8 @@
 //   prep    z = dX (+ dpre_sigma * ws at dense_7) * [h > 0]  (dX in BF16
 //           from the GEMM, z in FP32), dz = bf16(z), db += column sums of z
 //   dW      grads[k][n] += sum_m In[m][k] dz[m][n]   (In = the tape's BF16 input columns)
-//   dX      dX[m][k] = sum_n dz[m][n] W[k][n], k < 256 (W = BF16 copy of the FP32 master weights)
+//   dX      dX[m][k] = sum_n dz[m][n] W[k][n], k < 256 (W = BF16 copy of the FP32
+//           master weights, resident in shared memory for the launch)
 #include <cuda_bf16.h>
 
 #include "common.cuh"
@@ -229,7 +230,8 @@ extern "C" int nerfgb_mlp_backward_bf16(const void *packed_fp32, const void *tap
       if ((rc = dW(tp, acts_offset(4), 256, w.dz, 256, M, grad_params, 5, 0, w.part, err, st)) != NERFGB_OK) return rc;
       if ((rc = dW(tp, kActsEncXyz, 63, w.dz, 256, M, grad_params, 5, 256, w.part, err, st)) != NERFGB_OK) return rc;
     } else {
-      if ((rc = dW(tp, acts_offset(l - 1), 256, w.dz, 256, M, grad_params, l, 0, w.part, err, st)) != NERFGB_OK) return rc;
+      if ((rc = dW(tp, acts_offset(l - 1), 256, w.dz, 256, M, grad_params, l, 0, w.part, err, st)) != NERFGB_OK)
+        return rc;
     }
     if ((rc = dX(w.wb, l, w.dz, M, w.raw, err, st)) != NERFGB_OK) return rc;
   }
