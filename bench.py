@@ -64,6 +64,8 @@ def parse():
     ap.add_argument("--gate-tau", type=float, default=1e-5)
     ap.add_argument("--proposal-steps", type=int, default=2000)
     ap.add_argument("--train-steps", type=int, default=3)
+    ap.add_argument("--train-tile", type=int, default=4096,
+                    help="rays per recompute tile of the training backward (0: keep the forward's tape)")
     ap.add_argument("--sweep", type=int, default=1, help="1: FP32/BF16/FP8 sweep at 65536 rays x 256")
     return ap.parse_args()
 
@@ -106,19 +108,20 @@ def train_only(args):
     batch = [torch.from_numpy(x[:4096]).to(dev) for x in ng.synthetic.training_rays(500, 4, 1024)]
     target = teacher.render(*batch, seed=3)["rgb"]
     student = ng.NeRF(params, precision=args.path, seed=60)
+    tile = args.train_tile or None
     for _ in range(args.warmup):
-        student.train_step((tuple(batch), (target,)))
+        student.train_step((tuple(batch), (target,)), tile_rays=tile)
     ts = []
     for _ in range(args.steps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        student.train_step((tuple(batch), (target,)))
+        student.train_step((tuple(batch), (target,)), tile_rays=tile)
         e1.record()
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1))
     student.coarse_model.check_device_errors()
-    print(json.dumps({"kernel": f"train_{args.path}", "batch_rays": 4096, "step_ms": statistics.median(ts)}),
-          flush=True)
+    print(json.dumps({"kernel": f"train_{args.path}", "batch_rays": 4096, "tile_rays": tile,
+                      "step_ms": statistics.median(ts)}), flush=True)
 
 
 def dist_env():
@@ -553,14 +556,18 @@ def main():
     if args.train_steps > 0:
         batch = [torch.from_numpy(x[:4096]).to(dev) for x in ng.synthetic.training_rays(500 + rank, 4, 1024)]
         target = plain.render(*batch, seed=3)["rgb"]
-        train = {"batch_rays": 4096, "master_weights": "fp32"}
-        for tp in ("bf16", "fp32"):
+        train = {"batch_rays": 4096, "master_weights": "fp32",
+                 "backward": "autograd.RenderFunction: tape recomputed per tile of train_tile rays "
+                             "(*_stored_tape: the forward's tape kept instead)", "train_tile": args.train_tile}
+        for tp, tile in (("bf16", args.train_tile or None), ("bf16", None), ("fp32", args.train_tile or None)):
             student = ng.NeRF(params, precision=tp, seed=60)
-            tms = timed_steps(lambda i: student.train_step((tuple(batch), (target,))), args.train_steps, 1)
+            tms = timed_steps(lambda i: student.train_step((tuple(batch), (target,)), tile_rays=tile),
+                              args.train_steps, 1)
             student.coarse_model.check_device_errors()
-            train[tp] = {"rays_per_s": 4096 / (tms / 1000.0), "ms_per_step": tms,
-                         "gemms": "BF16 tcgen05 GEMMs forward and backward, FP32 accumulation"
-                         if tp == "bf16" else "FP32 SIMT"}
+            key = tp if tile is not None else tp + "_stored_tape"
+            train[key] = {"rays_per_s": 4096 / (tms / 1000.0), "ms_per_step": tms,
+                          "gemms": "BF16 tcgen05 GEMMs forward and backward, FP32 accumulation"
+                          if tp == "bf16" else "FP32 SIMT"}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -11,7 +11,7 @@ ray_utils.py), ``model`` (nerf/core/model.py) and ``render_loop`` (the
 files of nerf/main/render.py's loop). The kernels live in
 libnerfgb.so (C ABI: include/nerfgb.h), built by ``build.py``.
 """
-from . import h5, proposal, ray_utils, render_loop, synthetic, weights  # noqa: F401
+from . import autograd, h5, proposal, ray_utils, render_loop, synthetic, weights  # noqa: F401
 from ._lib import NerfgbError, lib  # noqa: F401
 from .config import make_params  # noqa: F401
 from .model import (NeRF, NerfMLP, PositionalEncoder,  # noqa: F401

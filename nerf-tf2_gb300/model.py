@@ -79,7 +79,8 @@ class NerfMLP:
 
     def set_weights(self, d):
         blob = from_dict(d, self.name)
-        self.params.copy_(torch.from_numpy(blob))
+        with torch.no_grad():
+            self.params.copy_(torch.from_numpy(blob))
         self.mark_updated()
 
     def load_weights(self, path):
@@ -211,66 +212,40 @@ class NeRF:
             self._opt = {"step": 0, "m": [z(), z()], "v": [z(), z()], "g": [z(), z()]}
         return self._opt
 
-    def train_step(self, data, *, u_coarse=None, u_fine=None, lr=None, precision=None):
-        """One step of NeRF.train_step (model.py:127-180): forward with the
-        activation tape, loss = MSE(coarse) + MSE(fine) (:157-168), gradients
-        by the hand-written backward (compositing, then the MLP), and a Keras
-        Adam step with ExponentialDecay(5e-4, 500000, 0.1) (:413-418) on the
-        FP32 master weights. ``precision``: "fp32" (FP32 GEMMs) or "bf16"
-        (BF16 tensor-core GEMMs forward and backward, FP32 accumulation);
-        default: "bf16" for a BF16 or FP8 model, else "fp32".
-        ``data`` = ((rays_o, rays_d, near, far), (rgb,)).
+    def train_step(self, data, *, u_coarse=None, u_fine=None, lr=None, precision=None, tile_rays=4096):
+        """One step of NeRF.train_step (model.py:127-180): the coarse and fine
+        maps through autograd.RenderFunction, loss = MSE(coarse) + MSE(fine)
+        (:157-168) through autograd.MSEFunction, ``loss.backward()`` (the
+        hand-written backward: compositing, then the MLP, recomputing the
+        activations per tile of ``tile_rays`` rays; None keeps the forward's
+        tape instead), and a Keras Adam step with ExponentialDecay(5e-4,
+        500000, 0.1) (:413-418) on the FP32 master weights. ``precision``:
+        "fp32" (FP32 GEMMs) or "bf16" (BF16 tensor-core GEMMs forward and
+        backward, FP32 accumulation); default: "bf16" for a BF16 or FP8
+        model, else "fp32". ``data`` = ((rays_o, rays_d, near, far), (rgb,)).
         Returns {"loss", "coarse_loss", "fine_loss", "psnr"} as floats."""
-        tp = precision or ("fp32" if self.precision == "fp32" else "bf16")
+        from . import autograd
         (rays_o, rays_d, near, far), (rgb,) = data
-        p = self.params
         rays_o = as_cuda(rays_o, name="rays_o")
         R = rays_o.shape[0]
-        rays_d = as_cuda(rays_d, shape=(R, 3), name="rays_d")
         target = as_cuda(rgb, shape=(R, 3), name="rgb")
         st = self._train_state()
         st["step"] += 1
-        d_cm = ray_utils.create_input_batch_coarse_model(p, rays_o, rays_d, near, far, u_vals=u_coarse)
-        t_c = d_cm["t_vals"]
-        Sc = t_c.shape[1]
-        rgb_c, sig_c, acts_c = self.coarse_model.forward_train(d_cm["xyz_inputs"], rays_d, rows_per_dir=Sc,
-                                                               precision=tp)
-        pp_c = ray_utils.post_process_model_output(rgb_c, sig_c, t_c, self.white_bg, trans_mode=self.trans_mode)
-        d_fm = ray_utils.create_input_batch_fine_model(p, rays_o, rays_d, pp_c["weights"], d_cm["bin_data"],
-                                                       t_c, u_vals=u_fine)
-        t_f = d_fm["t_vals"]
-        S = t_f.shape[1]
-        rgb_f, sig_f, acts_f = self.fine_model.forward_train(d_fm["xyz_inputs"], rays_d, rows_per_dir=S,
-                                                             precision=tp)
-        pp_f = ray_utils.post_process_model_output(rgb_f, sig_f, t_f, self.white_bg, trans_mode=self.trans_mode)
-        loss = torch.zeros(3, device=rays_o.device)
-        grads_map = []
-        for k, pp in enumerate((pp_c, pp_f)):
-            g = empty(R, 3)
-            _lib.call("nerfgb_mse_loss", ptr(pp["pred_rgb"]), ptr(target), R * 3, 1.0, ptr(loss[k:k + 1]),
-                      ptr(g), stream())
-            grads_map.append(g)
-        for k, (model, sig, t, rgb_s, acts) in enumerate(((self.coarse_model, sig_c, t_c, rgb_c, acts_c),
-                                                          (self.fine_model, sig_f, t_f, rgb_f, acts_f))):
-            n, Sk = t.shape
-            d_sig, d_rgb = empty(n * Sk), empty(n * Sk, 3)
-            _lib.call("nerfgb_composite_backward", ptr(sig), ptr(t), ptr(rgb_s), ptr(grads_map[k]), None, n, Sk,
-                      int(self.white_bg), ptr(d_sig), ptr(d_rgb), stream())
-            st["g"][k].zero_()
-            model.backward(acts, d_rgb, d_sig, st["g"][k])
-        # keep the step's tape until the next step (inspection and tests)
-        st["tape"] = {"coarse": (t_c, sig_c, rgb_c, acts_c, pp_c["pred_rgb"]),
-                      "fine": (t_f, sig_f, rgb_f, acts_f, pp_f["pred_rgb"])}
+        for model in (self.coarse_model, self.fine_model):
+            model.params.grad = None
+        rgb_c, rgb_f = autograd.render_with_grad(self, rays_o, rays_d, near, far, u_coarse=u_coarse, u_fine=u_fine,
+                                                 precision=precision, tile_rays=tile_rays)
+        loss_c, loss_f = autograd.mse(rgb_c, target), autograd.mse(rgb_f, target)
+        (loss_c + loss_f).backward()
+        st["g"] = [self.coarse_model.params.grad, self.fine_model.params.grad]
         step_lr = 5e-4 * 0.1 ** (st["step"] / 500000.0) if lr is None else lr
         for k, model in enumerate((self.coarse_model, self.fine_model)):
             _lib.call("nerfgb_adam_step", ptr(model.params), ptr(st["m"][k]), ptr(st["v"][k]), ptr(st["g"][k]),
                       PARAM_COUNT, step_lr, 0.9, 0.999, 1e-7, st["step"], stream())
             model.mark_updated()
-        _lib.call("nerfgb_mse_loss", ptr(pp_f["pred_rgb"]), ptr(target), R * 3, 1.0, ptr(loss[2:3]), None,
-                  stream())
-        lc, lf, mse_f = (float(x) for x in loss.tolist())
+        lc, lf = float(loss_c.detach()), float(loss_f.detach())
         return {"loss": lc + lf, "coarse_loss": lc, "fine_loss": lf,
-                "psnr": -10.0 * float(torch.log10(torch.tensor(max(mse_f, 1e-30))))}
+                "psnr": -10.0 * float(torch.log10(torch.tensor(max(lf, 1e-30))))}
 
     def gradients(self):
         """Flat parameter gradients of the last train_step: (coarse, fine)."""
