@@ -145,6 +145,21 @@ int nerfgb_mlp_forward_mapped(const void *packed, int precision,
                               float *rgb, float *sigma, int *err_word,
                               void *stream);
 
+/* Diagnostic of the tensor-core kernels' failure path (no counterpart in the
+ * reference, which surfaces TensorFlow's errors): nerfgb_mlp_forward at
+ * precision BF16 or FP8 with every bounded device wait limited to wait_ns
+ * (1e3 .. 1e10 ns; the default kernels use 2 s) and, when withhold_chunk >=
+ * 0, the weight chunk at that position of the (even) CTA's load sequence
+ * left unloaded, so that the MMA issuer's wait runs out. The kernel then
+ * writes NERFGB_E_TIMEOUT to *err_word, drains its copies and MMAs, frees
+ * its tensor memory and returns; the outputs are unspecified. */
+int nerfgb_mlp_forward_wait_test(const void *packed, int precision,
+                                 const float *xyz, const float *dirs,
+                                 long long n_rows, int rows_per_dir,
+                                 float *rgb, float *sigma, int *err_word,
+                                 unsigned long long wait_ns,
+                                 long long withhold_chunk, void *stream);
+
 /* ---- ray generation ------------------------------------------------- */
 
 /* Replaces get_rays_tf (nerf/utils/ray_utils.py:53-106): rays_o, rays_d

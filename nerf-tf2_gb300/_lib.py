@@ -43,6 +43,7 @@ SIGNATURES = {
     "nerfgb_positional_encode": (I, [P, LL, I, P, P]),
     "nerfgb_mlp_forward": (I, [P, I, P, P, LL, I, P, P, P, P]),
     "nerfgb_mlp_forward_mapped": (I, [P, I, P, P, LL, I, P, P, P, P, P, P]),
+    "nerfgb_mlp_forward_wait_test": (I, [P, I, P, P, LL, I, P, P, P, ctypes.c_ulonglong, LL, P]),
     "nerfgb_uniform": (I, [ULL, ULL, LL, P, P]),
     "nerfgb_get_rays": (I, [I, I, P, P, P, P, P]),
     "nerfgb_sample_rays": (I, [P, I, I, P, P, F, F, P, I, P, P, P, P, P, P]),

@@ -89,8 +89,8 @@ struct Geo {
   static constexpr uint32_t kBarDrain = kBar0 + 160;
   static constexpr uint32_t kBarB = kBar0 + 168;
   static constexpr uint32_t kTmemSlot = kBar0 + 176;
-  static constexpr uint32_t kAbort = kBar0 + 180;
-  static constexpr uint32_t kSmem = kBar0 + 192;
+  static constexpr uint32_t kAbort = kBar0 + 184;        // int, then the wait limit (u64) at +8
+  static constexpr uint32_t kSmem = kBar0 + 200;
   static constexpr int kBufs = MT == 1 ? 2 : 1;          // TMEM accumulators (256 columns per 128-row tile)
   static_assert(kNst <= 8 && kSmem <= 227 * 1024, "ring");
   static_assert(!B_RES || (!B_MN && MT == 1), "resident B: K-major, one M tile");
@@ -163,6 +163,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
     mbar_init(sbase + G::kBarDrain, 1);
     mbar_init(sbase + G::kBarB, kLoadThreads);
     *abort_flag = 0;
+    set_wait_limit(abort_flag, kWaitNs);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == kIssuerWarp) {

@@ -377,6 +377,19 @@ extern "C" int nerfgb_mlp_forward(const void *packed, int precision, const float
   return launch_mlp_bf16(packed, xyz, dirs, n_rows, rows_per_dir, rgb, sigma, err_word, as_stream(stream));
 }
 
+extern "C" int nerfgb_mlp_forward_wait_test(const void *packed, int precision, const float *xyz, const float *dirs,
+                                            long long n_rows, int rows_per_dir, float *rgb, float *sigma,
+                                            int *err_word, unsigned long long wait_ns, long long withhold_chunk,
+                                            void *stream) {
+  if (n_rows < 0 || rows_per_dir < 1) return NERFGB_E_INVALID_ARG;
+  if (precision != NERFGB_PREC_BF16 && precision != NERFGB_PREC_FP8) return NERFGB_E_UNSUPPORTED;
+  if (wait_ns < 1000ull || wait_ns > 10000000000ull) return NERFGB_E_INVALID_ARG;
+  if (n_rows == 0) return NERFGB_OK;
+  if (!packed || !xyz || !dirs || !rgb || !sigma || !err_word || !aligned(packed, 256)) return NERFGB_E_INVALID_ARG;
+  return launch_mlp_wait_test(packed, precision == NERFGB_PREC_FP8, xyz, dirs, n_rows, rows_per_dir, rgb, sigma,
+                              err_word, as_stream(stream), wait_ns, withhold_chunk);
+}
+
 extern "C" int nerfgb_mlp_forward_mapped(const void *packed, int precision, const float *xyz, const float *dirs,
                                          long long n_rows_max, int rows_per_dir, const int *row_map,
                                          const int *n_rows_dev, float *rgb, float *sigma, int *err_word,

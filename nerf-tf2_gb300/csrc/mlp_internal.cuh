@@ -53,6 +53,14 @@ int launch_gemm_dx(const __nv_bfloat16 *dz, long long M, int n_out, const __nv_b
 int launch_gemm_dw(const __nv_bfloat16 *in, long long ld_in, int k_in, const __nv_bfloat16 *dz, int n_out,
                    long long M, float *grads, float *part, int splits, int *err, cudaStream_t stream);
 long long gemm_dw_partial_floats(int splits);
+// The BF16 (pair) or FP8 tensor-core forward with a chosen limit on every
+// bounded wait (ns) and the weight chunk at position `withhold` of the load
+// sequence of the (even) CTA left unloaded, so that a wait runs out: the
+// failure path's test hook (mlp_tc.cu).
+int launch_mlp_wait_test(const void *packed, bool fp8, const float *xyz, const float *dirs, long long n, int rpd,
+                         float *rgb, float *sigma, int *err_word, cudaStream_t stream, unsigned long long wait_ns,
+                         long long withhold);
+
 // FP8-e4m3 tcgen05 forward (mlp_tc.cu).
 int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,
                    float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm = RowMap());

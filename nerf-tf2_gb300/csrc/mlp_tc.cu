@@ -83,9 +83,9 @@ struct Layout {
   static constexpr uint32_t kBarActr = kMiscOff + 272;   // [2]
   static constexpr uint32_t kBarDrain = kMiscOff + 288;
   static constexpr uint32_t kTmemSlot = kMiscOff + 296;
-  static constexpr uint32_t kAbort = kMiscOff + 300;
-  static constexpr uint32_t kBarHead = kMiscOff + 304;  // [2]
-  static constexpr uint32_t kSigPart = kMiscOff + 320;  // float [2][128] (single-CTA epilogue)
+  static constexpr uint32_t kAbort = kMiscOff + 304;    // int, then the wait limit (u64) at +8
+  static constexpr uint32_t kBarHead = kMiscOff + 320;  // [2]
+  static constexpr uint32_t kSigPart = kMiscOff + 384;  // float [2][128] (single-CTA epilogue)
   static constexpr uint32_t kSmemBytes = kSigPart + 2 * 128 * 4;
   // Pair epilogue: head partial sums (float), in regions idle at the time: sigma's [4][128]
   // in the upper half of the sub-tile's encoding region (enc_xyz's columns
@@ -253,12 +253,12 @@ constexpr uint32_t kDescHi = (128u >> 4) | (1u << 14);
 __device__ __forceinline__ uint64_t desc_lo(uint32_t lo) { return ((uint64_t)kDescHi << 32) | lo; }
 
 // Out-of-line slow path of a full-barrier wait: spins until the phase
-// completes, the CTA aborts, or kWaitNs passes (then raises the abort).
+// completes, the CTA aborts, or the wait limit passes (then raises the abort).
 __device__ __noinline__ void wait_slow(uint32_t bar, uint32_t parity, volatile int *abort_flag, int *err) {
   const uint64_t t0 = globaltimer();
   while (!mbar_try(bar, parity)) {
     if (*abort_flag) return;
-    if (globaltimer() - t0 > kWaitNs) {
+    if (globaltimer() - t0 > wait_limit(abort_flag)) {
       atomicExch(err, NERFGB_E_TIMEOUT);
       *abort_flag = 1;
       return;
@@ -472,7 +472,8 @@ template <int KCH, int NST, bool PINGPONG, bool TSMEM, bool F8, bool STORE, bool
 __global__ void __launch_bounds__(kThreads, 1)
     mlp_tc_kernel(const uint8_t *__restrict__ packed, const float *__restrict__ xyz,
                     const float *__restrict__ dirs, long long n_max, int rpd, float *__restrict__ rgb_out,
-                    float *__restrict__ sigma_out, int *__restrict__ err, RowMap rm, uint16_t *__restrict__ tape) {
+                    float *__restrict__ sigma_out, int *__restrict__ err, RowMap rm, uint16_t *__restrict__ tape,
+                    unsigned long long wait_ns, long long withhold) {
   static_assert(!(STORE && F8), "the activation tape is BF16");
   static_assert(!PAIR || (!F8 && PINGPONG && KCH == kPairKch), "pair path: BF16 ping-pong, the pair pack's chunks");
   using L = Layout<TSMEM, F8>;
@@ -529,10 +530,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       // pair: one arrival per epilogue warp of both CTAs; single CTA: one
       // per thread of the sub-tile's eight epilogue warps
       mbar_init(sbase + kBarActr + 8 * s, PAIR ? 32 : 256);
-      mbar_init(sbase + L::kBarHead + 8 * s, 16);
+      // head partial sums: one arrival per epilogue warp of the sub-tile's
+      // other half (single CTA: 4) or of all four column quarters (pair: 16)
+      mbar_init(sbase + L::kBarHead + 8 * s, PAIR ? 16 : 4);
     }
     mbar_init(sbase + kBarDrain, 1);
     *abort_flag = 0;
+    set_wait_limit(abort_flag, wait_ns);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -573,15 +577,19 @@ __global__ void __launch_bounds__(kThreads, 1)
         uint32_t used = 0;  // bit st: parity of the copies issued into stage st
         int st = 0;
         bool ok = true;
+        long long nq = 0;  // chunks of this CTA's load sequence
         for_each_load<KCH, NST, PINGPONG, PAIR>(t_first, t_step, ntiles, [&](int g, int c) {
           if (!wait_bar(sbase + kBarEmpty + 8 * st, ((used >> st) & 1u) ^ 1u, abort_flag, err)) {
             ok = false;
             return false;
           }
-          uint32_t bytes;
-          const uint8_t *src = chunk_src(g, c, bytes);
-          mbar_expect_tx(sbase + kBarFull + 8 * st, bytes);
-          bulk_g2s(sbase + kRingOff + st * kStageBytes, src, bytes, sbase + kBarFull + 8 * st);
+          // test hook of the failure path: the even CTA leaves chunk `withhold` unloaded
+          if (!(nq++ == withhold && crank == 0)) {
+            uint32_t bytes;
+            const uint8_t *src = chunk_src(g, c, bytes);
+            mbar_expect_tx(sbase + kBarFull + 8 * st, bytes);
+            bulk_g2s(sbase + kRingOff + st * kStageBytes, src, bytes, sbase + kBarFull + 8 * st);
+          }
           used ^= 1u << st;
           if (++st == NST) st = 0;
           return true;
@@ -613,12 +621,14 @@ __global__ void __launch_bounds__(kThreads, 1)
                 ok = false;
                 break;
               }
-              const int N = gemm_n(g), Kp = gemm_kp(g);
-              const int kc = Kp - c * KCH < KCH ? Kp - c * KCH : KCH;
-              const uint32_t bytes = (uint32_t)N * kc * kE;
-              mbar_expect_tx(full, bytes);
-              bulk_g2s(sbase + kRingOff + st * kStageBytes, packed + gemm_w_offset(g) * kE + (long long)c * KCH * N * kE,
-                       bytes, full);
+              if (q != withhold) {  // test hook of the failure path: chunk `withhold` left unloaded
+                const int N = gemm_n(g), Kp = gemm_kp(g);
+                const int kc = Kp - c * KCH < KCH ? Kp - c * KCH : KCH;
+                const uint32_t bytes = (uint32_t)N * kc * kE;
+                mbar_expect_tx(full, bytes);
+                bulk_g2s(sbase + kRingOff + st * kStageBytes,
+                         packed + gemm_w_offset(g) * kE + (long long)c * KCH * N * kE, bytes, full);
+              }
               issued = true;
               phase ^= 1;
             }
@@ -930,7 +940,8 @@ __global__ void __launch_bounds__(kThreads, 1)
       const uint32_t trow = tmem + ((uint32_t)(32 * qd) << 16) + s * 256 + hf * 128;
       const uint32_t bar_accf = sbase + kBarAccf + 8 * s, bar_actr = sbase + kBarActr + 8 * s;
       float *sig_part = reinterpret_cast<float *>(smem + kSigPart) + s * 128;
-      uint32_t accf_phase = 0;
+      const uint32_t bar_head = sbase + L::kBarHead + 8 * s;
+      uint32_t accf_phase = 0, head_phase = 0;
       bool ok = true;
       for (long long tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
         const long long grow = tile * kRows + s * 128 + r;
@@ -949,7 +960,8 @@ __global__ void __launch_bounds__(kThreads, 1)
         mbar_arrive(bar_actr);
         float rgb_acc[3] = {0.f, 0.f, 0.f};
         for (int g = 0; g < kNumGemm; ++g) {
-          if (!wait_bar(bar_accf, accf_phase, abort_flag, err)) {
+          // warp-uniform outcome, so that the warp's tcgen05.ld stay convergent
+          if (!__all_sync(0xffffffffu, wait_bar(bar_accf, accf_phase, abort_flag, err))) {
             ok = false;
             break;
           }
@@ -1054,10 +1066,21 @@ __global__ void __launch_bounds__(kThreads, 1)
             }
           }
           if (g == 7) {
-            // sigma = ReLU(h7 . w + b) (model.py:374-375), halves summed in FP32.
-            if (hf == 1) sig_part[r] = sig;
-            named_sync(1 + s, 256);
-            if (hf == 0 && valid) sigma_out[prow] = fmaxf(sig + sig_part[r] + table[kSigmaBOff], 0.0f);
+            // sigma = ReLU(h7 . w + b) (model.py:374-375), halves summed in FP32:
+            // the second half's warps publish theirs behind the head barrier
+            // (a bounded wait, so that an abort cannot strand a warp at it)
+            if (hf == 1) {
+              sig_part[r] = sig;
+              __syncwarp();
+              if (lane == 0) mbar_arrive(bar_head);
+            } else {
+              if (!__all_sync(0xffffffffu, wait_bar(bar_head, head_phase, abort_flag, err))) {
+                ok = false;
+                break;
+              }
+              head_phase ^= 1;
+              if (valid) sigma_out[prow] = fmaxf(sig + sig_part[r] + table[kSigmaBOff], 0.0f);
+            }
           }
           if (g == 8 && hf == 0) {
             // enc_dir into the enc region (enc_xyz was last read by dense_5).
@@ -1112,7 +1135,8 @@ __global__ void __launch_bounds__(kThreads, 1)
 template <int KCH, int NST, bool PP, bool TSMEM, bool F8, bool STORE = false, bool PAIR = false>
 static int launch_variant(const void *packed, const float *xyz, const float *dirs, long long n, int rpd,
                           float *rgb, float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm,
-                          uint16_t *tape = nullptr) {
+                          uint16_t *tape = nullptr, unsigned long long wait_ns = tc::kWaitNs,
+                          long long withhold = -1) {
   constexpr uint32_t smem = tc::Layout<TSMEM, F8>::kSmemBytes;
   static_assert(smem <= 227 * 1024, "shared memory");
   auto kern = tc::mlp_tc_kernel<KCH, NST, PP, TSMEM, F8, STORE, PAIR>;
@@ -1157,13 +1181,15 @@ static int launch_variant(const void *packed, const float *xyz, const float *dir
     if (max_pairs < 1) return NERFGB_E_UNSUPPORTED;
     const long long pairs = ntiles < max_pairs ? (ntiles > 0 ? ntiles : 1) : max_pairs;
     cfg.gridDim = dim3((unsigned)(2 * pairs));
-    if (cudaLaunchKernelEx(&cfg, kern, pk, xyz, dirs, n, rpd, rgb, sigma, err_word, rm, tape) != cudaSuccess)
+    if (cudaLaunchKernelEx(&cfg, kern, pk, xyz, dirs, n, rpd, rgb, sigma, err_word, rm, tape, wait_ns, withhold) !=
+        cudaSuccess)
       return NERFGB_E_CUDA;
     return launch_status();
   } else {
     const long long ntiles = (n + tc::kRows - 1) / tc::kRows;
     const int grid = (int)(ntiles < sms ? ntiles : sms);
-    kern<<<grid, tc::kThreads, smem, stream>>>(pk, xyz, dirs, n, rpd, rgb, sigma, err_word, rm, tape);
+    kern<<<grid, tc::kThreads, smem, stream>>>(pk, xyz, dirs, n, rpd, rgb, sigma, err_word, rm, tape, wait_ns,
+                                               withhold);
     return launch_status();
   }
 }
@@ -1190,6 +1216,17 @@ int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long
   // (16 KB per bulk copy). Ping-pong: 0.68 ms on 786,432 rows against 0.83
   // for lockstep; at half the weight bytes the doubled stream fits the ring.
   return launch_variant<64, 7, true, true, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream, rm);
+}
+
+int launch_mlp_wait_test(const void *packed, bool fp8, const float *xyz, const float *dirs, long long n, int rpd,
+                         float *rgb, float *sigma, int *err_word, cudaStream_t stream, unsigned long long wait_ns,
+                         long long withhold) {
+  // the kernels of launch_mlp_bf16 / launch_mlp_fp8 with the given wait limit and withheld chunk
+  if (fp8)
+    return launch_variant<64, 7, true, true, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream,
+                                                   RowMap(), nullptr, wait_ns, withhold);
+  return launch_variant<64, 4, true, false, false, false, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word,
+                                                                stream, RowMap(), nullptr, wait_ns, withhold);
 }
 
 }  // namespace nerfgb

@@ -12,7 +12,17 @@
 namespace nerfgb {
 namespace tc {
 
-constexpr unsigned long long kWaitNs = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long kWaitNs = 2000000000ull;  // default limit of one wait: 2 s
+
+// The kernels keep their wait limit (ns, 64-bit) in shared memory 8 bytes
+// after their abort flag (an int at an 8-byte aligned offset), so that the
+// bounded waits can read it without a register of their own.
+__device__ __forceinline__ unsigned long long wait_limit(volatile int *abort_flag) {
+  return *reinterpret_cast<volatile unsigned long long *>(reinterpret_cast<volatile char *>(abort_flag) + 8);
+}
+__device__ __forceinline__ void set_wait_limit(volatile int *abort_flag, unsigned long long ns) {
+  *reinterpret_cast<volatile unsigned long long *>(reinterpret_cast<volatile char *>(abort_flag) + 8) = ns;
+}
 
 // ---------------------------------------------------------------------------
 // PTX wrappers
@@ -239,7 +249,7 @@ __device__ __forceinline__ bool wait_bar(uint32_t bar, uint32_t parity, volatile
   while (true) {
     if (mbar_try(bar, parity)) return true;
     if (*abort_flag) return false;
-    if (globaltimer() - t0 > kWaitNs) {
+    if (globaltimer() - t0 > wait_limit(abort_flag)) {
       atomicExch(err, NERFGB_E_TIMEOUT);
       *abort_flag = 1;
       return false;
