@@ -160,6 +160,17 @@ int nerfgb_mlp_forward_wait_test(const void *packed, int precision,
                                  unsigned long long wait_ns,
                                  long long withhold_chunk, void *stream);
 
+/* Status of the bounds-check build (compiled with -DNERF_BOUNDS_CHECK, as
+ * libnerfgb_bounds.so): every index the kernels compute from data (the fine
+ * sampler's searchsorted bins and sort positions, the gates' sort-permutation
+ * entries and row-map slots, the MLP's row-map rows) is checked against its
+ * buffer; an index out of range is clamped to 0 and the first failing
+ * check's site code (1..9, see csrc/common.cuh) is recorded. Returns 0 when
+ * no check failed, the site code otherwise, NERFGB_E_UNSUPPORTED in the
+ * normal build. Synchronises the device; reset != 0 clears the record. No
+ * counterpart in the reference. */
+int nerfgb_bounds_check_status(int reset);
+
 /* ---- ray generation ------------------------------------------------- */
 
 /* Replaces get_rays_tf (nerf/utils/ray_utils.py:53-106): rays_o, rays_d

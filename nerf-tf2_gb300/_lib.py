@@ -4,10 +4,13 @@ The library is built in-tree (``build.py``). Nothing here falls back to a
 CPU or PyTorch implementation: if the library is missing, loading raises.
 """
 import ctypes
+import os
 import pathlib
 
 HERE = pathlib.Path(__file__).resolve().parent
-LIB_PATH = HERE / "libnerfgb.so"
+# NERFGB_LIBRARY names another build of the same library (the bounds-check
+# build, libnerfgb_bounds.so) to load instead.
+LIB_PATH = pathlib.Path(os.environ.get("NERFGB_LIBRARY", str(HERE / "libnerfgb.so")))
 
 P = ctypes.c_void_p
 I = ctypes.c_int
@@ -43,6 +46,7 @@ SIGNATURES = {
     "nerfgb_positional_encode": (I, [P, LL, I, P, P]),
     "nerfgb_mlp_forward": (I, [P, I, P, P, LL, I, P, P, P, P]),
     "nerfgb_mlp_forward_mapped": (I, [P, I, P, P, LL, I, P, P, P, P, P, P]),
+    "nerfgb_bounds_check_status": (I, [I]),
     "nerfgb_mlp_forward_wait_test": (I, [P, I, P, P, LL, I, P, P, P, ctypes.c_ulonglong, LL, P]),
     "nerfgb_uniform": (I, [ULL, ULL, LL, P, P]),
     "nerfgb_get_rays": (I, [I, I, P, P, P, P, P]),

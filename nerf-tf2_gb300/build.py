@@ -1,6 +1,7 @@
 """Builds libnerfgb.so in-tree with nvcc for sm_103a (no cmake, no torch build
-machinery). The translation units compile in parallel, then link into one
-shared library next to this file.
+machinery), and its bounds-check build libnerfgb_bounds.so. The translation
+units compile in parallel, then link into shared libraries next to this
+file.
 
     python nerf-tf2_gb300/build.py [--force] [--verbose]
 """
@@ -41,19 +42,36 @@ def _stale(target, deps):
     return any(d.stat().st_mtime > t for d in deps)
 
 
-def build(force=False, verbose=False, extra_flags=()):
-    BUILD.mkdir(exist_ok=True)
+# Build variants: the library, and the bounds-check build of the same sources
+# (every data-dependent index checked, csrc/common.cuh) for the tests.
+VARIANTS = {
+    "default": (BUILD, LIB, ()),
+    "bounds": (HERE / "_build_bounds", HERE / "libnerfgb_bounds.so", ("-DNERF_BOUNDS_CHECK",)),
+}
+
+
+def _plan(variant, force, verbose, extra_flags):
+    build_dir, lib, flags = VARIANTS[variant]
+    build_dir.mkdir(exist_ok=True)
     headers = list(CSRC.glob("*.cuh")) + list(INCLUDE.glob("*.h"))
     objs, jobs = [], []
     for src in SOURCES:
         s = CSRC / src
-        o = BUILD / (s.stem + ".o")
+        o = build_dir / (s.stem + ".o")
         objs.append(o)
         if force or _stale(o, [s, *headers, pathlib.Path(__file__)]):
-            cmd = [nvcc(), *_flags(extra_flags), "-c", str(s), "-o", str(o)]
+            cmd = [nvcc(), *_flags((*flags, *extra_flags)), "-c", str(s), "-o", str(o)]
             if verbose:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)
+    return lib, objs, jobs
+
+
+def build(force=False, verbose=False, extra_flags=(), variants=("default", "bounds")):
+    """Compiles the translation units of every variant in parallel and links
+    each library; returns the default library's path."""
+    plans = [_plan(v, force, verbose, extra_flags) for v in variants]
+    jobs = [j for _, _, js in plans for j in js]
 
     def run(cmd):
         r = subprocess.run(cmd, capture_output=True, text=True)
@@ -65,11 +83,12 @@ def build(force=False, verbose=False, extra_flags=()):
                 sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)
             if r.returncode != 0:
                 raise RuntimeError(f"nvcc failed on {cmd[-3]}")
-    if force or jobs or _stale(LIB, objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", str(LIB), *map(str, objs)]
-        r = subprocess.run(cmd, capture_output=True, text=True)
-        if r.returncode != 0:
-            raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
+    for lib, objs, js in plans:
+        if force or js or _stale(lib, objs):
+            cmd = [nvcc(), *ARCH, "-shared", "-o", str(lib), *map(str, objs)]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError("link failed:\n" + r.stdout + r.stderr)
     return LIB
 
 

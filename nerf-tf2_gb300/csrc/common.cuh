@@ -168,4 +168,51 @@ inline int num_sms() {
 
 inline bool aligned(const void *p, unsigned a) { return ((uintptr_t)p % a) == 0; }
 
+// ---------------------------------------------------------------------------
+// Bounds-check build (-DNERF_BOUNDS_CHECK): every index computed from data
+// (searchsorted results, sort ranks, sort permutations, gate row maps and
+// counts, MLP row maps) goes through NG_IDX(i, n, site). Out of [0, n) the
+// first failing site's code is recorded in this translation unit's device
+// word and the index is clamped to 0, so that the access stays in bounds;
+// nerfgb_bounds_check_status() reads and clears the words. Without the flag
+// NG_IDX(i, n, site) is i.
+// ---------------------------------------------------------------------------
+#ifdef NERF_BOUNDS_CHECK
+static __device__ int g_bounds_err;  // one per translation unit
+__device__ __forceinline__ long long ng_checked(long long i, long long n, int site) {
+  if (i < 0 || i >= n) {
+    atomicCAS(&g_bounds_err, 0, site);
+    return 0;
+  }
+  return i;
+}
+#define NG_IDX(i, n, site) ::nerfgb::ng_checked((long long)(i), (long long)(n), (site))
+// Reads (and with reset, clears) this translation unit's error word.
+#define NG_BOUNDS_READER(fn)                                                         \
+  int fn(int reset) {                                                                \
+    int v = 0;                                                                       \
+    if (cudaMemcpyFromSymbol(&v, g_bounds_err, sizeof(int)) != cudaSuccess) return -1; \
+    if (reset) {                                                                     \
+      const int z = 0;                                                               \
+      if (cudaMemcpyToSymbol(g_bounds_err, &z, sizeof(int)) != cudaSuccess) return -1; \
+    }                                                                                \
+    return v;                                                                        \
+  }
+#else
+#define NG_IDX(i, n, site) (i)
+#endif
+
+// Site codes of NG_IDX (reported by nerfgb_bounds_check_status).
+enum BoundsSite {
+  kSiteFinePiece = 1,     // fine sampler: searchsorted bin of a draw
+  kSiteSortCoarse = 2,    // fine sampler: merged position of a coarse depth
+  kSiteSortFine = 3,      // fine sampler: merged position of a fine draw
+  kSiteSortRank = 4,      // fine sampler: rank-sort position
+  kSiteGateCoarse = 5,    // coarse gate: row-map slot
+  kSiteGateFinePerm = 6,  // fine gate: sort permutation entry
+  kSiteGateFine = 7,      // fine gate: row-map slot
+  kSiteMlpRowMap = 8,     // MLP: physical row of a row-map entry (tensor-core kernels)
+  kSiteMlpRowMapFp32 = 9  // MLP: physical row of a row-map entry (FP32 kernel)
+};
+
 }  // namespace nerfgb

@@ -38,7 +38,7 @@ __global__ void gate_coarse_kernel(const float *__restrict__ w, int R, int S, fl
     const bool on = j < S && w[row0 + j] > tau;
     const unsigned b = __ballot_sync(0xffffffffu, on);
     if (j < S) mask[row0 + j] = on ? 1 : 0;
-    if (on) row_map[base + __popc(b & ((1u << lane) - 1u))] = (int)(row0 + j);
+    if (on) row_map[NG_IDX(base + __popc(b & ((1u << lane) - 1u)), (long long)R * S, kSiteGateCoarse)] = (int)(row0 + j);
     base += __popc(b);
   }
 }
@@ -51,7 +51,7 @@ __global__ void gate_fine_kernel(const int *__restrict__ perm, const unsigned ch
   const long long row0 = (long long)ray * S;
   auto keep = [&](int j) -> bool {
     if (j >= S) return false;
-    const int p = perm[row0 + j];
+    const int p = (int)NG_IDX(perm[row0 + j], S, kSiteGateFinePerm);
     // a fine draw, or a coarse sample whose gate is on
     return p >= Sc || (p >= 0 && mask_c[(long long)ray * Sc + p] != 0);
   };
@@ -64,7 +64,7 @@ __global__ void gate_fine_kernel(const int *__restrict__ perm, const unsigned ch
     const int j = j0 + lane;
     const bool on = keep(j);
     const unsigned b = __ballot_sync(0xffffffffu, on);
-    if (on) row_map[base + __popc(b & ((1u << lane) - 1u))] = (int)(row0 + j);
+    if (on) row_map[NG_IDX(base + __popc(b & ((1u << lane) - 1u)), (long long)R * S, kSiteGateFine)] = (int)(row0 + j);
     base += __popc(b);
   }
 }
@@ -105,3 +105,9 @@ extern "C" int nerfgb_gate_fine(const int *sort_perm, const unsigned char *mask_
   if (!sort_perm || !mask_coarse || !row_map || !count) return NERFGB_E_INVALID_ARG;
   return launch_gate_fine(sort_perm, mask_coarse, n_rays, n_coarse, n_samples, row_map, count, as_stream(stream));
 }
+
+#ifdef NERF_BOUNDS_CHECK
+namespace nerfgb {
+NG_BOUNDS_READER(bounds_read_gate)
+}  // namespace nerfgb
+#endif

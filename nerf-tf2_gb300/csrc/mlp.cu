@@ -182,7 +182,9 @@ __global__ void __launch_bounds__(256, 1)
   const int tid = threadIdx.x, tx = tid & 31, ty = tid >> 5;
   const long long n = rm.n_dev ? min((long long)*rm.n_dev, n_max) : n_max;
   const long long ntiles = (n + kTM - 1) / kTM;
-  auto phys = [&](long long k) -> long long { return rm.map ? (long long)rm.map[k] : k; };
+  auto phys = [&](long long k) -> long long {
+    return rm.map ? (long long)NG_IDX(rm.map[k], n_max, kSiteMlpRowMapFp32) : k;
+  };
 
   for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const long long row0 = tile * kTM;
@@ -406,3 +408,9 @@ extern "C" int nerfgb_mlp_forward_mapped(const void *packed, int precision, cons
   return launch_mlp(packed, precision, xyz, dirs, n_rows_max, rows_per_dir, rgb, sigma, err_word,
                     as_stream(stream), rm);
 }
+
+#ifdef NERF_BOUNDS_CHECK
+namespace nerfgb {
+NG_BOUNDS_READER(bounds_read_mlp)
+}  // namespace nerfgb
+#endif

@@ -95,4 +95,12 @@ int launch_composite_bwd(const float *sigma, const float *t, const float *rgb, c
                          const float *grad_w, int R, int S, int white_bg, float last_delta, float *grad_sigma,
                          float *grad_rgb, cudaStream_t stream);
 
+#ifdef NERF_BOUNDS_CHECK
+// Error words of the bounds-check build, one per translation unit (common.cuh).
+int bounds_read_ray_ops(int reset);
+int bounds_read_gate(int reset);
+int bounds_read_mlp(int reset);
+int bounds_read_mlp_tc(int reset);
+#endif
+
 }  // namespace nerfgb

@@ -507,7 +507,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   // physical row of logical row k.
   const long long n = rm.n_dev ? min((long long)*rm.n_dev, n_max) : n_max;
   const long long ntiles = (n + kTileRows - 1) / kTileRows;
-  auto phys = [&](long long k) -> long long { return rm.map ? (long long)rm.map[k] : k; };
+  auto phys = [&](long long k) -> long long {
+    return rm.map ? (long long)NG_IDX(rm.map[k], n_max, kSiteMlpRowMap) : k;
+  };
 
   if (TSMEM) {  // bias and head table (and scales) -> shared memory
     const float4 *src = reinterpret_cast<const float4 *>(packed + kTabOff);
@@ -1230,3 +1232,9 @@ int launch_mlp_wait_test(const void *packed, bool fp8, const float *xyz, const f
 }
 
 }  // namespace nerfgb
+
+#ifdef NERF_BOUNDS_CHECK
+namespace nerfgb {
+NG_BOUNDS_READER(bounds_read_mlp_tc)
+}  // namespace nerfgb
+#endif

@@ -296,6 +296,7 @@ __global__ void __launch_bounds__(32 * kFineWarps)
           count = step;
         }
       }
+      first = (int)NG_IDX(first, Sc, kSiteFinePiece);
       float a_ = s_agg[first], p_ = s_pdf[first], l_ = s_left[first];  // :366-368
       float mask = (p_ < 1e-8f) ? 0.0f : 1.0f;                          // :372
       p_ = fmaxf(p_, 1e-8f);                                            // :373
@@ -352,8 +353,9 @@ __global__ void __launch_bounds__(32 * kFineWarps)
             count = step;
           }
         }
-        s_srt[i + first] = v;
-        if (sort_perm) sort_perm[sb + i + first] = i;
+        const int pos = (int)NG_IDX(i + first, S, kSiteSortCoarse);
+        s_srt[pos] = v;
+        if (sort_perm) sort_perm[sb + pos] = i;
       }
       for (int j = lane; j < Sf; j += 32) {
         const float v = s_fk[j];
@@ -367,8 +369,9 @@ __global__ void __launch_bounds__(32 * kFineWarps)
             count = step;
           }
         }
-        s_srt[j + first] = v;
-        if (sort_perm) sort_perm[sb + j + first] = Sc + s_fi[j];
+        const int pos = (int)NG_IDX(j + first, S, kSiteSortFine);
+        s_srt[pos] = v;
+        if (sort_perm) sort_perm[sb + pos] = Sc + s_fi[j];
       }
     } else {
       // Rank sort: rank = number of elements that precede e in the stable order.
@@ -376,6 +379,7 @@ __global__ void __launch_bounds__(32 * kFineWarps)
         float v = s_t[e];
         int rank = 0;
         for (int q = 0; q < S; ++q) rank += sort_before(s_t[q], q, v, e) ? 1 : 0;
+        rank = (int)NG_IDX(rank, S, kSiteSortRank);
         s_srt[rank] = v;
         if (sort_perm) sort_perm[sb + rank] = e;
       }
@@ -673,3 +677,9 @@ extern "C" int nerfgb_depth_map(const float *pred_depth, long long n, float scal
                                                                     rays_o, rays_d, w2c, out);
   return launch_status();
 }
+
+#ifdef NERF_BOUNDS_CHECK
+namespace nerfgb {
+NG_BOUNDS_READER(bounds_read_ray_ops)
+}  // namespace nerfgb
+#endif

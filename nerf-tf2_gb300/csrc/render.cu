@@ -53,6 +53,21 @@ int launch_mlp(const void *packed, int precision, const float *xyz, const float 
 
 using namespace nerfgb;
 
+extern "C" int nerfgb_bounds_check_status(int reset) {
+#ifdef NERF_BOUNDS_CHECK
+  const int v[4] = {bounds_read_ray_ops(reset), bounds_read_gate(reset), bounds_read_mlp(reset),
+                    bounds_read_mlp_tc(reset)};
+  for (int i = 0; i < 4; ++i)
+    if (v[i] < 0) return NERFGB_E_CUDA;
+  for (int i = 0; i < 4; ++i)
+    if (v[i] != 0) return v[i];
+  return NERFGB_OK;
+#else
+  (void)reset;
+  return NERFGB_E_UNSUPPORTED;
+#endif
+}
+
 extern "C" long long nerfgb_render_workspace_bytes(int n_rays, int n_coarse, int n_fine) {
   if (n_rays < 0 || n_coarse < 1 || n_fine < 0) return -1;
   return carve(nullptr, n_rays, n_coarse, n_fine).bytes;
