@@ -362,13 +362,16 @@ def main():
                      "mode": args.proposal_mode, "gate_tau": args.gate_tau,
                      "loss_first": losses[0], "loss_last": losses[-1],
                      "train_s": round(time.perf_counter() - t0, 2)}
-    # kernels per chunk: 2 uniform draws, coarse sample, [coarse MLP | proposal
-    # forward + weights], composite, fine sample, fine MLP, composite; the
-    # gated path adds the proposal (2), two gates and keeps both MLPs
+    # kernels per chunk: plain = coarse sample (Philox draws inside), coarse
+    # MLP, fine sample (coarse compositing inside), fine MLP, composite;
+    # replace = coarse sample, proposal forward, proposal weights, fine
+    # sample, fine MLP, composite; gate = coarse sample, proposal forward,
+    # proposal weights + coarse gate, coarse MLP, fine sample (coarse
+    # compositing and fine gate inside), fine MLP, composite
     prop_kw = {}
     if proposal is not None:
         prop_kw = {"proposal": proposal, "proposal_mode": args.proposal_mode, "gate_tau": args.gate_tau}
-    launches_per_chunk = 8 if proposal is None else (12 if args.proposal_mode == "gate" else 8)
+    launches_per_chunk = 5 if proposal is None else (7 if args.proposal_mode == "gate" else 6)
 
     def timed_steps(fn, steps, warmup):
         for i in range(warmup):

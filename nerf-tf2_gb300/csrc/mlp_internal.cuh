@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "nerfgb.h"
+
 namespace nerfgb {
 
 // Optional indirection of an MLP launch's rows. Logical row k in [0, n) is
@@ -88,9 +90,49 @@ int launch_proposal_forward_bf16(const float *params, const float *xyz, long lon
 // Compositing with a chosen last interval (ray_ops.cu): last_delta >= 0 is
 // used as is (the reference uses 1e10), < 0 means the previous spacing.
 // sample_rgb and the map outputs may be NULL.
+// Optional gate on the compositor's weights (the coarse gate of the gated
+// render): sample j of a ray is on where w > tau (NaN: off); mask [R*S]
+// (0/1, may be NULL), the on samples' indices appended to row_map at slots
+// taken from *count, sig_zero (may be NULL) zeroed at the off samples.
+struct CompositeGate {
+  float tau = 0.0f;
+  unsigned char *mask = nullptr;
+  int *row_map = nullptr, *count = nullptr;
+  float *sig_zero = nullptr;
+};
 int launch_composite(const float *sample_rgb, const float *sigma, const float *t_vals, int n_rays, int n_samples,
                      int white_bg, int trans_mode, float last_delta, float *weights, float *pred_rgb,
-                     float *pred_depth, float *acc_map, cudaStream_t stream);
+                     float *pred_depth, float *acc_map, cudaStream_t stream,
+                     const CompositeGate &gate = CompositeGate());
+
+// Stratified coarse sampler (ray_ops.cu); u_vals NULL with perturb: the
+// Philox draws of nerfgb_uniform(seed, 0, R*S) are made in the kernel.
+int launch_coarse_sample(const float *rays_o, const float *rays_d, const float *near, const float *far,
+                         const float *u_vals, unsigned long long seed, int R, int S, int perturb, int lin_inv,
+                         float *xyz, float *dirs, float *t_vals, float *edges, float *widths, cudaStream_t stream);
+
+// What the fine sampler (ray_ops.cu) fuses around the sampling, all fields
+// optional: the coarse pass's compositing (the bin weights from sigma_c
+// [R*Sc] instead of bin_weights; with rgb_c [R*Sc,3] and map_* also the
+// coarse maps; w_c receives the weights), the fine gate of the gated render
+// (a member of the sorted union is on where it is a fine draw or its coarse
+// sample's mask_c entry is on; on members appended to row_map at slots from
+// *count, sig_zero / rgb_zero zeroed at the off members), and the Philox
+// draws of nerfgb_uniform(seed, R*Sc, R*Sf) when u_vals is NULL.
+struct FineFuse {
+  const float *sigma_c = nullptr, *rgb_c = nullptr;
+  int mode = NERFGB_TRANS_LOGSUM, white_bg = 0;
+  float *w_c = nullptr;
+  float *map_rgb = nullptr, *map_depth = nullptr, *map_acc = nullptr;
+  const unsigned char *mask_c = nullptr;
+  int *row_map = nullptr, *count = nullptr;
+  float *sig_zero = nullptr, *rgb_zero = nullptr;
+  unsigned long long seed = 0;
+};
+int launch_fine_sample(const float *rays_o, const float *rays_d, const float *bin_weights, const float *left_edges,
+                       int ld_left, const float *bin_widths, const float *t_vals_coarse, const float *u_vals,
+                       int n_rays, int n_coarse, int n_fine, float *xyz, float *dirs, float *t_vals,
+                       int *piece_idxs, int *sort_perm, cudaStream_t stream, const FineFuse &fz);
 int launch_composite_bwd(const float *sigma, const float *t, const float *rgb, const float *grad_map,
                          const float *grad_w, int R, int S, int white_bg, float last_delta, float *grad_sigma,
                          float *grad_rgb, cudaStream_t stream);

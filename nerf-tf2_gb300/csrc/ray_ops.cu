@@ -29,10 +29,12 @@ __device__ __forceinline__ float bin_edge(float nr, float fr, int S, int i, int 
   return fdiv(1.0f, linspace_at(fdiv(1.0f, nr), fdiv(1.0f, fr), S + 1, i));
 }
 
+// u NULL with perturb: the uniform of (ray r, bin i) is element r*S + i of
+// the Philox stream keyed by seed (nerfgb_uniform's element), drawn here.
 __global__ void coarse_sample_kernel(const float *__restrict__ rays_o, const float *__restrict__ rays_d,
                                      const float *__restrict__ near, const float *__restrict__ far,
-                                     const float *__restrict__ u, int R, int S, int perturb,
-                                     int lin_inv, float *__restrict__ xyz, float *__restrict__ dirs,
+                                     const float *__restrict__ u, unsigned long long seed, int R, int S,
+                                     int perturb, int lin_inv, float *__restrict__ xyz, float *__restrict__ dirs,
                                      float *__restrict__ t_out, float *__restrict__ edges,
                                      float *__restrict__ widths) {
   long long gid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -42,7 +44,8 @@ __global__ void coarse_sample_kernel(const float *__restrict__ rays_o, const flo
   float e0 = bin_edge(nr, fr, S, i, lin_inv);
   float e1 = bin_edge(nr, fr, S, i + 1, lin_inv);
   float w = fsub(e1, e0);                                        // :226
-  float t = perturb ? fadd(e0, fmul(u[gid], w))                  // :234
+  const float ug = perturb ? (u ? u[gid] : philox_uniform(seed, (unsigned long long)gid)) : 0.0f;
+  float t = perturb ? fadd(e0, fmul(ug, w))                      // :234
                     : fmul(0.5f, fadd(e0, e1));                  // :243
   t_out[gid] = t;
   widths[gid] = w;
@@ -99,109 +102,177 @@ __device__ __forceinline__ CSum two_sum_add(CSum a, CSum b) {
 
 constexpr int kCompWarps = 4;
 
+// One ray's compositing by one warp from shared copies: s_t, s_sig [S],
+// s_rgb [3S] or NULL. Writes the weights to w_out[0..S) (may be NULL) and
+// returns (r, g, b, depth, acc) in every lane (white_bg not applied). Lane l
+// owns the contiguous segment [l*k, (l+1)*k), k = ceil(S/32).
+__device__ __forceinline__ void composite_ray(int lane, const float *s_t, const float *s_sig, const float *s_rgb,
+                                              int S, int mode, float last_delta, float *w_out, float (&out)[5]) {
+  const int k = (S + 31) >> 5;
+  const int j0 = min(lane * k, S), j1 = min(j0 + k, S);
+  // Per-sample alpha and transmittance factor.
+  float loc_prod = 1.0f;
+  CSum loc{0.0f, 0.0f};
+  // Last interval: 1e10 as the reference (:462-468), or (last_delta < 0)
+  // the previous spacing.
+  const float dlast = last_delta >= 0.0f ? last_delta : (S > 1 ? fsub(s_t[S - 1], s_t[S - 2]) : 1e10f);
+  for (int j = j0; j < j1; ++j) {
+    float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : dlast;   // :462-468
+    float alpha = fsub(1.0f, expf(fmul(-s_sig[j], delta)));         // :423
+    float fac = fadd(fsub(1.0f, alpha), 1e-10f);                    // :480
+    if (mode == NERFGB_TRANS_CUMPROD) {
+      loc_prod = fmul(loc_prod, fac);
+    } else {
+      loc = two_sum_add(loc, CSum{logf(fac), 0.0f});
+    }
+  }
+  // Exclusive scan across lanes.
+  float ex_prod = 1.0f;
+  CSum ex{0.0f, 0.0f};
+  if (mode == NERFGB_TRANS_CUMPROD) {
+    float inc = loc_prod;
+    for (int off = 1; off < 32; off <<= 1) {
+      float o = __shfl_up_sync(0xffffffffu, inc, off);
+      if (lane >= off) inc = fmul(o, inc);
+    }
+    ex_prod = __shfl_up_sync(0xffffffffu, inc, 1);
+    if (lane == 0) ex_prod = 1.0f;
+  } else {
+    CSum inc = loc;
+    for (int off = 1; off < 32; off <<= 1) {
+      float os = __shfl_up_sync(0xffffffffu, inc.s, off);
+      float oc = __shfl_up_sync(0xffffffffu, inc.c, off);
+      if (lane >= off) inc = two_sum_add(CSum{os, oc}, inc);
+    }
+    ex.s = __shfl_up_sync(0xffffffffu, inc.s, 1);
+    ex.c = __shfl_up_sync(0xffffffffu, inc.c, 1);
+    if (lane == 0) ex = CSum{0.0f, 0.0f};
+  }
+  // Weights and partial sums.
+  float pr = 0.f, pg = 0.f, pb = 0.f, pd = 0.f, pa = 0.f;
+  float run_prod = ex_prod;
+  CSum run = ex;
+  for (int j = j0; j < j1; ++j) {
+    float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : dlast;
+    float alpha = fsub(1.0f, expf(fmul(-s_sig[j], delta)));
+    float fac = fadd(fsub(1.0f, alpha), 1e-10f);
+    float T;
+    if (mode == NERFGB_TRANS_CUMPROD) {
+      T = run_prod;
+      run_prod = fmul(run_prod, fac);
+    } else {
+      T = expf(fadd(run.s, run.c));
+      run = two_sum_add(run, CSum{logf(fac), 0.0f});
+    }
+    float w = fmul(alpha, T);                                       // :480
+    if (w_out) w_out[j] = w;
+    if (s_rgb) {
+      const float *c = s_rgb + 3 * j;
+      pr = fadd(pr, fmul(w, c[0]));                                 // :534
+      pg = fadd(pg, fmul(w, c[1]));
+      pb = fadd(pb, fmul(w, c[2]));
+    }
+    pd = fadd(pd, fmul(s_t[j], w));                                 // :537
+    pa = fadd(pa, w);                                               // :540
+  }
+  for (int off = 16; off > 0; off >>= 1) {
+    pr = fadd(pr, __shfl_xor_sync(0xffffffffu, pr, off));
+    pg = fadd(pg, __shfl_xor_sync(0xffffffffu, pg, off));
+    pb = fadd(pb, __shfl_xor_sync(0xffffffffu, pb, off));
+    pd = fadd(pd, __shfl_xor_sync(0xffffffffu, pd, off));
+    pa = fadd(pa, __shfl_xor_sync(0xffffffffu, pa, off));
+  }
+  out[0] = pr;
+  out[1] = pg;
+  out[2] = pb;
+  out[3] = pd;
+  out[4] = pa;
+}
+
+// The maps of lane 0's sums: rgb (+ 1 - acc with white_bg, :542-544), depth, acc.
+__device__ __forceinline__ void store_maps(int r, int white_bg, const float (&m)[5], float *pred_rgb,
+                                           float *pred_depth, float *acc_map) {
+  float pr = m[0], pg = m[1], pb = m[2];
+  if (white_bg) {
+    float bg = fsub(1.0f, m[4]);
+    pr = fadd(pr, bg);
+    pg = fadd(pg, bg);
+    pb = fadd(pb, bg);
+  }
+  pred_rgb[3 * r + 0] = pr;
+  pred_rgb[3 * r + 1] = pg;
+  pred_rgb[3 * r + 2] = pb;
+  pred_depth[r] = m[3];
+  acc_map[r] = m[4];
+}
+
+// Appends the ray's on samples (in order) to row_map at a slot taken by one
+// atomic on *count, writes mask (0/1) when given, and zeroes sig_zero (and
+// rgb_zero, 3 values) at the off samples, which the row-mapped MLP leaves
+// untouched. on(j) is the warp's predicate for sample j of the ray.
+template <typename On>
+__device__ __forceinline__ void gate_ray(int lane, long long row0, int S, int R, On on, unsigned char *mask,
+                                         int *row_map, int *count, float *sig_zero, float *rgb_zero, int site) {
+  int total = 0;
+  for (int j0 = 0; j0 < S; j0 += 32) total += __popc(__ballot_sync(0xffffffffu, j0 + lane < S && on(j0 + lane)));
+  int base = 0;
+  if (lane == 0 && total > 0) base = atomicAdd(count, total);
+  base = __shfl_sync(0xffffffffu, base, 0);
+  for (int j0 = 0; j0 < S; j0 += 32) {
+    const int j = j0 + lane;
+    const bool o = j < S && on(j);
+    const unsigned b = __ballot_sync(0xffffffffu, o);
+    if (j < S) {
+      if (mask) mask[row0 + j] = o ? 1 : 0;
+      if (!o) {
+        if (sig_zero) sig_zero[row0 + j] = 0.0f;
+        if (rgb_zero) {
+          rgb_zero[3 * (row0 + j)] = 0.0f;
+          rgb_zero[3 * (row0 + j) + 1] = 0.0f;
+          rgb_zero[3 * (row0 + j) + 2] = 0.0f;
+        }
+      }
+    }
+    if (o) row_map[NG_IDX(base + __popc(b & ((1u << lane) - 1u)), (long long)R * S, site)] = (int)(row0 + j);
+    base += __popc(b);
+  }
+}
+
+// Compositor (ray_utils.py:408-551), one warp per ray: t, sigma and rgb are
+// staged in shared memory with coalesced loads, the weights written back
+// from there. With gate_map != NULL the weights also gate the samples
+// (sample j on where w > tau, NaN off; gate_ray).
 __global__ void __launch_bounds__(32 * kCompWarps)
     composite_kernel(const float *__restrict__ rgb, const float *__restrict__ sigma,
                      const float *__restrict__ t, int R, int S, int white_bg, int mode, float last_delta,
                      float *__restrict__ weights, float *__restrict__ pred_rgb,
-                     float *__restrict__ pred_depth, float *__restrict__ acc_map) {
+                     float *__restrict__ pred_depth, float *__restrict__ acc_map, float tau,
+                     unsigned char *__restrict__ gate_mask, int *__restrict__ gate_map, int *__restrict__ gate_count,
+                     float *__restrict__ gate_sig_zero) {
   extern __shared__ float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  float *s_t = smem + warp * 2 * (S + 1);
+  float *s_t = smem + warp * (6 * S + 1);
   float *s_sig = s_t + (S + 1);
-  const int k = (S + 31) >> 5;
+  float *s_w = s_sig + S;
+  float *s_rgb = s_w + S;  // 3S
   for (int r = blockIdx.x * kCompWarps + warp; r < R; r += gridDim.x * kCompWarps) {
     const long long base = (long long)r * S;
     for (int j = lane; j < S; j += 32) {
       s_t[j] = t[base + j];
       s_sig[j] = sigma[base + j];
     }
+    if (rgb)
+      for (int j = lane; j < 3 * S; j += 32) s_rgb[j] = rgb[3 * base + j];
     __syncwarp();
-    const int j0 = min(lane * k, S), j1 = min(j0 + k, S);
-    // Per-sample alpha and transmittance factor.
-    float loc_prod = 1.0f;
-    CSum loc{0.0f, 0.0f};
-    // Last interval: 1e10 as the reference (:462-468), or (last_delta < 0)
-    // the previous spacing.
-    const float dlast = last_delta >= 0.0f ? last_delta : (S > 1 ? fsub(s_t[S - 1], s_t[S - 2]) : 1e10f);
-    for (int j = j0; j < j1; ++j) {
-      float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : dlast;   // :462-468
-      float alpha = fsub(1.0f, expf(fmul(-s_sig[j], delta)));         // :423
-      float fac = fadd(fsub(1.0f, alpha), 1e-10f);                    // :480
-      if (mode == NERFGB_TRANS_CUMPROD) {
-        loc_prod = fmul(loc_prod, fac);
-      } else {
-        loc = two_sum_add(loc, CSum{logf(fac), 0.0f});
-      }
-    }
-    // Exclusive scan across lanes.
-    float ex_prod = 1.0f;
-    CSum ex{0.0f, 0.0f};
-    if (mode == NERFGB_TRANS_CUMPROD) {
-      float inc = loc_prod;
-      for (int off = 1; off < 32; off <<= 1) {
-        float o = __shfl_up_sync(0xffffffffu, inc, off);
-        if (lane >= off) inc = fmul(o, inc);
-      }
-      ex_prod = __shfl_up_sync(0xffffffffu, inc, 1);
-      if (lane == 0) ex_prod = 1.0f;
-    } else {
-      CSum inc = loc;
-      for (int off = 1; off < 32; off <<= 1) {
-        float os = __shfl_up_sync(0xffffffffu, inc.s, off);
-        float oc = __shfl_up_sync(0xffffffffu, inc.c, off);
-        if (lane >= off) inc = two_sum_add(CSum{os, oc}, inc);
-      }
-      ex.s = __shfl_up_sync(0xffffffffu, inc.s, 1);
-      ex.c = __shfl_up_sync(0xffffffffu, inc.c, 1);
-      if (lane == 0) ex = CSum{0.0f, 0.0f};
-    }
-    // Weights and partial sums.
-    float pr = 0.f, pg = 0.f, pb = 0.f, pd = 0.f, pa = 0.f;
-    float run_prod = ex_prod;
-    CSum run = ex;
-    for (int j = j0; j < j1; ++j) {
-      float delta = (j < S - 1) ? fsub(s_t[j + 1], s_t[j]) : dlast;
-      float alpha = fsub(1.0f, expf(fmul(-s_sig[j], delta)));
-      float fac = fadd(fsub(1.0f, alpha), 1e-10f);
-      float T;
-      if (mode == NERFGB_TRANS_CUMPROD) {
-        T = run_prod;
-        run_prod = fmul(run_prod, fac);
-      } else {
-        T = expf(fadd(run.s, run.c));
-        run = two_sum_add(run, CSum{logf(fac), 0.0f});
-      }
-      float w = fmul(alpha, T);                                       // :480
-      if (weights) weights[base + j] = w;
-      if (rgb) {
-        const float *c = rgb + 3 * (base + j);
-        pr = fadd(pr, fmul(w, c[0]));                                 // :534
-        pg = fadd(pg, fmul(w, c[1]));
-        pb = fadd(pb, fmul(w, c[2]));
-      }
-      pd = fadd(pd, fmul(s_t[j], w));                                 // :537
-      pa = fadd(pa, w);                                               // :540
-    }
-    for (int off = 16; off > 0; off >>= 1) {
-      pr = fadd(pr, __shfl_xor_sync(0xffffffffu, pr, off));
-      pg = fadd(pg, __shfl_xor_sync(0xffffffffu, pg, off));
-      pb = fadd(pb, __shfl_xor_sync(0xffffffffu, pb, off));
-      pd = fadd(pd, __shfl_xor_sync(0xffffffffu, pd, off));
-      pa = fadd(pa, __shfl_xor_sync(0xffffffffu, pa, off));
-    }
-    if (lane == 0 && pred_rgb) {
-      if (white_bg) {                                                 // :542-544
-        float bg = fsub(1.0f, pa);
-        pr = fadd(pr, bg);
-        pg = fadd(pg, bg);
-        pb = fadd(pb, bg);
-      }
-      pred_rgb[3 * r + 0] = pr;
-      pred_rgb[3 * r + 1] = pg;
-      pred_rgb[3 * r + 2] = pb;
-      pred_depth[r] = pd;
-      acc_map[r] = pa;
-    }
+    float m[5];
+    composite_ray(lane, s_t, s_sig, rgb ? s_rgb : nullptr, S, mode, last_delta, s_w, m);
+    __syncwarp();
+    if (weights)
+      for (int j = lane; j < S; j += 32) weights[base + j] = s_w[j];
+    if (lane == 0 && pred_rgb) store_maps(r, white_bg, m, pred_rgb, pred_depth, acc_map);
+    if (gate_map)
+      gate_ray(lane, base, S, R, [&](int j) { return s_w[j] > tau; }, gate_mask, gate_map, gate_count,
+               gate_sig_zero, nullptr, kSiteGateCoarse);
     __syncwarp();
   }
 }
@@ -236,30 +307,56 @@ __global__ void __launch_bounds__(32 * kFineWarps)
                        const float *__restrict__ t_coarse, const float *__restrict__ u, int R, int Sc,
                        int Sf, float *__restrict__ xyz, float *__restrict__ dirs,
                        float *__restrict__ t_out, int *__restrict__ piece_idxs,
-                       int *__restrict__ sort_perm, int P) {
+                       int *__restrict__ sort_perm, int P, FineFuse fz) {
   extern __shared__ float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = Sc + Sf;
-  const int per_warp = 4 * Sc + (Sc + 1) + 2 * S + 2 * P;
+  const int per_warp = 4 * Sc + (Sc + 1) + 2 * S + 2 * P + S + 3 * Sc;
   float *s_w = smem + warp * per_warp;  // w + 1e-5, then pdf * width
   float *s_pdf = s_w + Sc;
   float *s_left = s_pdf + Sc;
   float *s_wid = s_left + Sc;
   float *s_agg = s_wid + Sc;      // Sc + 1
   float *s_t = s_agg + Sc + 1;    // concat(t_c, t_f), S
-  float *s_srt = s_t + S;         // sorted, S
+  float *s_srt = s_t + S;         // sorted, S (first holds sigma_c for the fused compositing)
   float *s_fk = s_srt + S;        // fast path: fine keys (P, a power of two >= Sf) ...
   int *s_fi = reinterpret_cast<int *>(s_fk + P);  // ... and their fine indices
+  int *s_perm = s_fi + P;         // the sort permutation, S
+  float *s_rgbc = reinterpret_cast<float *>(s_perm + S);  // rgb_c of the ray, 3 Sc
   for (int r = blockIdx.x * kFineWarps + warp; r < R; r += gridDim.x * kFineWarps) {
     const long long rb = (long long)r * Sc;
-    for (int j = lane; j < Sc; j += 32) {
-      float w = fadd(bin_weights[rb + j], 1e-5f);                     // :335
-      float wd = bin_widths[rb + j];
-      s_w[j] = w;
-      s_pdf[j] = fmul(w, wd);
-      s_wid[j] = wd;
-      s_left[j] = left_edges[(long long)r * ld_left + j];
-      s_t[j] = t_coarse[rb + j];
+    if (fz.sigma_c) {
+      // the coarse pass's compositing (ray_utils.py:426-482) of this ray
+      for (int j = lane; j < Sc; j += 32) {
+        s_wid[j] = bin_widths[rb + j];
+        s_left[j] = left_edges[(long long)r * ld_left + j];
+        s_t[j] = t_coarse[rb + j];
+        s_srt[j] = fz.sigma_c[rb + j];
+      }
+      const bool maps = fz.rgb_c && fz.map_rgb;
+      if (maps)
+        for (int j = lane; j < 3 * Sc; j += 32) s_rgbc[j] = fz.rgb_c[3 * rb + j];
+      __syncwarp();
+      float m[5];
+      composite_ray(lane, s_t, s_srt, maps ? s_rgbc : nullptr, Sc, fz.mode, 1e10f, s_w, m);
+      __syncwarp();
+      if (lane == 0 && maps) store_maps(r, fz.white_bg, m, fz.map_rgb, fz.map_depth, fz.map_acc);
+      for (int j = lane; j < Sc; j += 32) {
+        if (fz.w_c) fz.w_c[rb + j] = s_w[j];
+        float w = fadd(s_w[j], 1e-5f);                                // :335
+        s_w[j] = w;
+        s_pdf[j] = fmul(w, s_wid[j]);
+      }
+    } else {
+      for (int j = lane; j < Sc; j += 32) {
+        float w = fadd(bin_weights[rb + j], 1e-5f);                   // :335
+        float wd = bin_widths[rb + j];
+        s_w[j] = w;
+        s_pdf[j] = fmul(w, wd);
+        s_wid[j] = wd;
+        s_left[j] = left_edges[(long long)r * ld_left + j];
+        s_t[j] = t_coarse[rb + j];
+      }
     }
     __syncwarp();
     float denom = 0.0f;
@@ -284,7 +381,8 @@ __global__ void __launch_bounds__(32 * kFineWarps)
     __syncwarp();
     const long long ub = (long long)r * Sf;
     for (int k = lane; k < Sf; k += 32) {
-      float uk = u[ub + k];
+      // u NULL: element R*Sc + r*Sf + k of the Philox stream (after the coarse draws)
+      float uk = u ? u[ub + k] : philox_uniform(fz.seed, (unsigned long long)R * Sc + ub + k);
       // upper_bound over the inner edges agg[1..Sc-1] (:363).
       int first = 0, count = Sc - 1;
       while (count > 0) {
@@ -355,7 +453,7 @@ __global__ void __launch_bounds__(32 * kFineWarps)
         }
         const int pos = (int)NG_IDX(i + first, S, kSiteSortCoarse);
         s_srt[pos] = v;
-        if (sort_perm) sort_perm[sb + pos] = i;
+        s_perm[pos] = i;
       }
       for (int j = lane; j < Sf; j += 32) {
         const float v = s_fk[j];
@@ -371,7 +469,7 @@ __global__ void __launch_bounds__(32 * kFineWarps)
         }
         const int pos = (int)NG_IDX(j + first, S, kSiteSortFine);
         s_srt[pos] = v;
-        if (sort_perm) sort_perm[sb + pos] = Sc + s_fi[j];
+        s_perm[pos] = Sc + s_fi[j];
       }
     } else {
       // Rank sort: rank = number of elements that precede e in the stable order.
@@ -381,12 +479,24 @@ __global__ void __launch_bounds__(32 * kFineWarps)
         for (int q = 0; q < S; ++q) rank += sort_before(s_t[q], q, v, e) ? 1 : 0;
         rank = (int)NG_IDX(rank, S, kSiteSortRank);
         s_srt[rank] = v;
-        if (sort_perm) sort_perm[sb + rank] = e;
+        s_perm[rank] = e;
       }
     }
     __syncwarp();
     float o0 = rays_o[3 * r], o1 = rays_o[3 * r + 1], o2 = rays_o[3 * r + 2];
     float d0 = rays_d[3 * r], d1 = rays_d[3 * r + 1], d2 = rays_d[3 * r + 2];
+    if (sort_perm)
+      for (int p = lane; p < S; p += 32) sort_perm[sb + p] = s_perm[p];
+    if (fz.row_map) {
+      // the fine gate (the gated render): a fine draw, or a coarse sample whose gate is on
+      const unsigned char *mc = fz.mask_c + rb;
+      gate_ray(lane, sb, S, R,
+               [&](int j) {
+                 const int q = (int)NG_IDX(s_perm[j], S, kSiteGateFinePerm);
+                 return q >= Sc || mc[q] != 0;
+               },
+               nullptr, fz.row_map, fz.count, fz.sig_zero, fz.rgb_zero, kSiteGateFine);
+    }
     for (int p = lane; p < S; p += 32) {
       float tv = s_srt[p];
       t_out[sb + p] = tv;
@@ -523,6 +633,18 @@ extern "C" const char *nerfgb_status_string(int s) {
   }
 }
 
+namespace nerfgb {
+int launch_coarse_sample(const float *rays_o, const float *rays_d, const float *near, const float *far,
+                         const float *u_vals, unsigned long long seed, int R, int S, int perturb, int lin_inv,
+                         float *xyz, float *dirs, float *t_vals, float *edges, float *widths, cudaStream_t stream) {
+  const long long n = (long long)R * S;
+  if (n == 0) return NERFGB_OK;
+  coarse_sample_kernel<<<grid_for(n, 256), 256, 0, stream>>>(rays_o, rays_d, near, far, u_vals, seed, R, S,
+                                                             perturb, lin_inv, xyz, dirs, t_vals, edges, widths);
+  return launch_status();
+}
+}  // namespace nerfgb
+
 extern "C" int nerfgb_coarse_sample(const float *rays_o, const float *rays_d, const float *near,
                                     const float *far, const float *u_vals, int n_rays, int n_coarse,
                                     int perturb, int lin_inv_depth, float *xyz, float *dirs,
@@ -533,11 +655,8 @@ extern "C" int nerfgb_coarse_sample(const float *rays_o, const float *rays_d, co
   if (!rays_o || !rays_d || !near || !far || !xyz || !t_vals || !bin_edges || !bin_widths ||
       (perturb && !u_vals))
     return NERFGB_E_INVALID_ARG;
-  long long n = (long long)n_rays * n_coarse;
-  coarse_sample_kernel<<<grid_for(n, 256), 256, 0, as_stream(stream)>>>(
-      rays_o, rays_d, near, far, u_vals, n_rays, n_coarse, perturb, lin_inv_depth, xyz, dirs, t_vals,
-      bin_edges, bin_widths);
-  return launch_status();
+  return launch_coarse_sample(rays_o, rays_d, near, far, u_vals, 0, n_rays, n_coarse, perturb, lin_inv_depth, xyz,
+                              dirs, t_vals, bin_edges, bin_widths, as_stream(stream));
 }
 
 extern "C" int nerfgb_positional_encode(const float *x, long long n, int L, float *out, void *stream) {
@@ -553,8 +672,8 @@ extern "C" int nerfgb_positional_encode(const float *x, long long n, int L, floa
 namespace nerfgb {
 int launch_composite(const float *sample_rgb, const float *sigma, const float *t_vals, int n_rays, int n_samples,
                      int white_bg, int trans_mode, float last_delta, float *weights, float *pred_rgb,
-                     float *pred_depth, float *acc_map, cudaStream_t stream) {
-  size_t smem = (size_t)kCompWarps * 2 * (n_samples + 1) * sizeof(float);
+                     float *pred_depth, float *acc_map, cudaStream_t stream, const CompositeGate &gate) {
+  size_t smem = (size_t)kCompWarps * (6 * n_samples + 1) * sizeof(float);
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(composite_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess)
@@ -564,7 +683,7 @@ int launch_composite(const float *sample_rgb, const float *sigma, const float *t
   int cap = (sms > 0 ? sms : 148) * 16;
   composite_kernel<<<blocks < cap ? blocks : cap, 32 * kCompWarps, smem, stream>>>(
       sample_rgb, sigma, t_vals, n_rays, n_samples, white_bg, trans_mode, last_delta, weights, pred_rgb,
-      pred_depth, acc_map);
+      pred_depth, acc_map, gate.tau, gate.mask, gate.row_map, gate.count, gate.sig_zero);
   return launch_status();
 }
 }  // namespace nerfgb
@@ -604,6 +723,17 @@ extern "C" int nerfgb_fine_sample(const float *rays_o, const float *rays_d, cons
   if (!rays_o || !rays_d || !bin_weights || !left_edges || !bin_widths || !t_vals_coarse ||
       !u_vals || !xyz || !t_vals)
     return NERFGB_E_INVALID_ARG;
+  return launch_fine_sample(rays_o, rays_d, bin_weights, left_edges, ld_left, bin_widths, t_vals_coarse, u_vals,
+                            n_rays, n_coarse, n_fine, xyz, dirs, t_vals, piece_idxs, sort_perm, as_stream(stream),
+                            FineFuse());
+}
+
+namespace nerfgb {
+int launch_fine_sample(const float *rays_o, const float *rays_d, const float *bin_weights, const float *left_edges,
+                       int ld_left, const float *bin_widths, const float *t_vals_coarse, const float *u_vals,
+                       int n_rays, int n_coarse, int n_fine, float *xyz, float *dirs, float *t_vals,
+                       int *piece_idxs, int *sort_perm, cudaStream_t stream, const FineFuse &fz) {
+  if (n_rays == 0) return NERFGB_OK;
   int S = n_coarse + n_fine;
   // Fast stable sort for up to 512 fine draws: keys padded to a power of two.
   int P = 0;
@@ -611,7 +741,8 @@ extern "C" int nerfgb_fine_sample(const float *rays_o, const float *rays_d, cons
     P = 32;
     while (P < n_fine) P <<= 1;
   }
-  size_t smem = (size_t)kFineWarps * (4 * n_coarse + (n_coarse + 1) + 2 * S + 2 * P) * sizeof(float);
+  size_t smem =
+      (size_t)kFineWarps * (4 * n_coarse + (n_coarse + 1) + 2 * S + 2 * P + S + 3 * n_coarse) * sizeof(float);
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(fine_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess)
@@ -619,11 +750,12 @@ extern "C" int nerfgb_fine_sample(const float *rays_o, const float *rays_d, cons
   int sms = num_sms();
   int blocks = (n_rays + kFineWarps - 1) / kFineWarps;
   int cap = (sms > 0 ? sms : 148) * 16;
-  fine_sample_kernel<<<blocks < cap ? blocks : cap, 32 * kFineWarps, smem, as_stream(stream)>>>(
-      rays_o, rays_d, bin_weights, left_edges, ld_left, bin_widths, t_vals_coarse, u_vals, n_rays,
-      n_coarse, n_fine, xyz, dirs, t_vals, piece_idxs, sort_perm, P);
+  fine_sample_kernel<<<blocks < cap ? blocks : cap, 32 * kFineWarps, smem, stream>>>(
+      rays_o, rays_d, bin_weights, left_edges, ld_left, bin_widths, t_vals_coarse, u_vals, n_rays, n_coarse,
+      n_fine, xyz, dirs, t_vals, piece_idxs, sort_perm, P, fz);
   return launch_status();
 }
+}  // namespace nerfgb
 
 extern "C" int nerfgb_uniform(unsigned long long seed, unsigned long long offset, long long n, float *out,
                               void *stream) {

@@ -92,31 +92,29 @@ extern "C" int nerfgb_render_rays(const void *packed_coarse, const void *packed_
   const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
   RenderWs w = carve(workspace, R, Sc, Sf);
   int rc;
-  const float *uc = u_coarse, *uf = u_fine;
-  // Uniforms: coarse draws use counters [0, R*Sc), fine draws [R*Sc, R*S).
-  if (perturb && !uc) {
-    if ((rc = nerfgb_uniform(seed, 0, (long long)R * Sc, w.u_c, stream)) != NERFGB_OK) return rc;
-    uc = w.u_c;
-  }
-  if (!uf) {
-    if ((rc = nerfgb_uniform(seed, (unsigned long long)R * Sc, (long long)R * Sf, w.u_f, stream)) != NERFGB_OK)
-      return rc;
-    uf = w.u_f;
-  }
-  if ((rc = nerfgb_coarse_sample(rays_o, rays_d, near, far, uc, R, Sc, perturb, lin_inv_depth, w.xyz_c, nullptr,
-                                 w.t_c, w.edges, w.widths, stream)) != NERFGB_OK)
+  // Uniforms not supplied are drawn in the samplers from Philox keyed by
+  // seed: coarse draws use counters [0, R*Sc), fine draws [R*Sc, R*S).
+  if (trans_mode != NERFGB_TRANS_CUMPROD && trans_mode != NERFGB_TRANS_LOGSUM) return NERFGB_E_UNSUPPORTED;
+  if ((rc = launch_coarse_sample(rays_o, rays_d, near, far, u_coarse, seed, R, Sc, perturb, lin_inv_depth, w.xyz_c,
+                                 nullptr, w.t_c, w.edges, w.widths, st)) != NERFGB_OK)
     return rc;
   if ((rc = launch_mlp(packed_coarse, precision, w.xyz_c, rays_d, (long long)R * Sc, Sc, w.rgb_c, w.sig_c,
                        err_word, st)) != NERFGB_OK)
     return rc;
-  float *rc_rgb = rgb_coarse ? rgb_coarse : w.map_rgb_c;
-  float *rc_dep = depth_coarse ? depth_coarse : w.map_depth_c;
-  float *rc_acc = acc_coarse ? acc_coarse : w.map_acc_c;
-  if ((rc = nerfgb_composite(w.rgb_c, w.sig_c, w.t_c, R, Sc, white_bg, trans_mode, w.w_c, rc_rgb, rc_dep, rc_acc,
-                             stream)) != NERFGB_OK)
-    return rc;
-  if ((rc = nerfgb_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, uf, R, Sc, Sf, w.xyz_f,
-                               nullptr, w.t_f, nullptr, nullptr, stream)) != NERFGB_OK)
+  // the coarse pass's compositing (and its maps, when asked for) inside the fine sampler
+  FineFuse fz;
+  fz.sigma_c = w.sig_c;
+  fz.mode = trans_mode;
+  fz.white_bg = white_bg;
+  fz.seed = seed;
+  if (rgb_coarse || depth_coarse || acc_coarse) {
+    fz.rgb_c = w.rgb_c;
+    fz.map_rgb = rgb_coarse ? rgb_coarse : w.map_rgb_c;
+    fz.map_depth = depth_coarse ? depth_coarse : w.map_depth_c;
+    fz.map_acc = acc_coarse ? acc_coarse : w.map_acc_c;
+  }
+  if ((rc = launch_fine_sample(rays_o, rays_d, nullptr, w.edges, Sc + 1, w.widths, w.t_c, u_fine, R, Sc, Sf, w.xyz_f,
+                               nullptr, w.t_f, nullptr, nullptr, st, fz)) != NERFGB_OK)
     return rc;
   if ((rc = launch_mlp(packed_fine, precision, w.xyz_f, rays_d, (long long)R * S, S, w.rgb_f, w.sig_f, err_word,
                        st)) != NERFGB_OK)
@@ -144,25 +142,17 @@ extern "C" int nerfgb_render_rays_proposal(const float *proposal_params, const v
   const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
   RenderWs w = carve(workspace, R, Sc, Sf);
   int rc;
-  const float *uc = u_coarse, *uf = u_fine;
-  if (perturb && !uc) {
-    if ((rc = nerfgb_uniform(seed, 0, (long long)R * Sc, w.u_c, stream)) != NERFGB_OK) return rc;
-    uc = w.u_c;
-  }
-  if (!uf) {
-    if ((rc = nerfgb_uniform(seed, (unsigned long long)R * Sc, (long long)R * Sf, w.u_f, stream)) != NERFGB_OK)
-      return rc;
-    uf = w.u_f;
-  }
-  if ((rc = nerfgb_coarse_sample(rays_o, rays_d, near, far, uc, R, Sc, perturb, lin_inv_depth, w.xyz_c, nullptr,
-                                 w.t_c, w.edges, w.widths, stream)) != NERFGB_OK)
+  if ((rc = launch_coarse_sample(rays_o, rays_d, near, far, u_coarse, seed, R, Sc, perturb, lin_inv_depth, w.xyz_c,
+                                 nullptr, w.t_c, w.edges, w.widths, st)) != NERFGB_OK)
     return rc;
   // The proposal density at the stratified samples replaces the coarse MLP.
   if ((rc = launch_proposal(precision, proposal_params, w.xyz_c, (long long)R * Sc, w.sig_c, st)) != NERFGB_OK)
     return rc;
   if ((rc = nerfgb_proposal_weights(w.sig_c, w.t_c, R, Sc, trans_mode, w.w_c, stream)) != NERFGB_OK) return rc;
-  if ((rc = nerfgb_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, uf, R, Sc, Sf, w.xyz_f,
-                               nullptr, w.t_f, nullptr, nullptr, stream)) != NERFGB_OK)
+  FineFuse fz;
+  fz.seed = seed;
+  if ((rc = launch_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, u_fine, R, Sc, Sf, w.xyz_f,
+                               nullptr, w.t_f, nullptr, nullptr, st, fz)) != NERFGB_OK)
     return rc;
   if ((rc = launch_mlp(packed_fine, precision, w.xyz_f, rays_d, (long long)R * S, S, w.rgb_f, w.sig_f, err_word,
                        st)) != NERFGB_OK)
@@ -235,47 +225,50 @@ extern "C" int nerfgb_render_rays_gated(const float *proposal_params, const void
   if (precision != NERFGB_PREC_FP32 && !err_word) return NERFGB_E_INVALID_ARG;
   cudaStream_t st = as_stream(stream);
   const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
+  if (trans_mode != NERFGB_TRANS_CUMPROD && trans_mode != NERFGB_TRANS_LOGSUM) return NERFGB_E_UNSUPPORTED;
   RenderWs w = carve(workspace, R, Sc, Sf);
   GateWs g = carve_gate(workspace, R, Sc, Sf);
   int rc;
-  const float *uc = u_coarse, *uf = u_fine;
-  // Uniforms: the counters of nerfgb_render_rays, so equal seeds give equal draws.
-  if (perturb && !uc) {
-    if ((rc = nerfgb_uniform(seed, 0, (long long)R * Sc, w.u_c, stream)) != NERFGB_OK) return rc;
-    uc = w.u_c;
-  }
-  if (!uf) {
-    if ((rc = nerfgb_uniform(seed, (unsigned long long)R * Sc, (long long)R * Sf, w.u_f, stream)) != NERFGB_OK)
-      return rc;
-    uf = w.u_f;
-  }
-  if ((rc = nerfgb_coarse_sample(rays_o, rays_d, near, far, uc, R, Sc, perturb, lin_inv_depth, w.xyz_c, nullptr,
-                                 w.t_c, w.edges, w.widths, stream)) != NERFGB_OK)
+  // Uniforms: the counters of nerfgb_render_rays (drawn in the samplers), so
+  // equal seeds give equal draws.
+  if (cudaMemsetAsync(g.counts, 0, 2 * sizeof(int), st) != cudaSuccess) return NERFGB_E_CUDA;
+  if ((rc = launch_coarse_sample(rays_o, rays_d, near, far, u_coarse, seed, R, Sc, perturb, lin_inv_depth, w.xyz_c,
+                                 nullptr, w.t_c, w.edges, w.widths, st)) != NERFGB_OK)
     return rc;
-  // Proposal weights over the coarse bins, then the coarse gate.
+  // Proposal weights over the coarse bins and the coarse gate in one pass:
+  // the off samples' sigma is zeroed (the row-mapped MLP writes the others).
   if ((rc = launch_proposal(precision, proposal_params, w.xyz_c, (long long)R * Sc, g.sig_p, st)) != NERFGB_OK)
     return rc;
-  if ((rc = nerfgb_proposal_weights(g.sig_p, w.t_c, R, Sc, trans_mode, g.w_p, stream)) != NERFGB_OK) return rc;
-  if (cudaMemsetAsync(g.counts, 0, 2 * sizeof(int), st) != cudaSuccess ||
-      cudaMemsetAsync(w.sig_c, 0, (size_t)R * Sc * sizeof(float), st) != cudaSuccess ||
-      cudaMemsetAsync(w.sig_f, 0, (size_t)R * S * sizeof(float), st) != cudaSuccess ||
-      cudaMemsetAsync(w.rgb_f, 0, (size_t)R * S * 3 * sizeof(float), st) != cudaSuccess)
-    return NERFGB_E_CUDA;
-  if ((rc = launch_gate_coarse(g.w_p, R, Sc, gate_tau, g.mask_c, g.map_c, g.counts, st)) != NERFGB_OK) return rc;
+  CompositeGate cg;
+  cg.tau = gate_tau;
+  cg.mask = g.mask_c;
+  cg.row_map = g.map_c;
+  cg.count = g.counts;
+  cg.sig_zero = w.sig_c;
+  if ((rc = launch_composite(nullptr, g.sig_p, w.t_c, R, Sc, 0, trans_mode, -1.0f, nullptr, nullptr, nullptr, nullptr,
+                             st, cg)) != NERFGB_OK)
+    return rc;
   RowMap rm_c;
   rm_c.map = g.map_c;
   rm_c.n_dev = g.counts;
   if ((rc = launch_mlp(packed_coarse, precision, w.xyz_c, rays_d, (long long)R * Sc, Sc, w.rgb_c, w.sig_c,
                        err_word, st, rm_c)) != NERFGB_OK)
     return rc;
-  // Coarse weights exactly as the plain chain computes them (last interval 1e10).
-  if ((rc = launch_composite(nullptr, w.sig_c, w.t_c, R, Sc, white_bg, trans_mode, 1e10f, w.w_c, nullptr, nullptr,
-                             nullptr, st)) != NERFGB_OK)
+  // The fine sampler composites the coarse weights as the plain chain does
+  // (last interval 1e10), samples, sorts and gates the sorted union.
+  FineFuse fz;
+  fz.sigma_c = w.sig_c;
+  fz.mode = trans_mode;
+  fz.white_bg = white_bg;
+  fz.mask_c = g.mask_c;
+  fz.row_map = g.map_f;
+  fz.count = g.counts + 1;
+  fz.sig_zero = w.sig_f;
+  fz.rgb_zero = w.rgb_f;
+  fz.seed = seed;
+  if ((rc = launch_fine_sample(rays_o, rays_d, nullptr, w.edges, Sc + 1, w.widths, w.t_c, u_fine, R, Sc, Sf, w.xyz_f,
+                               nullptr, w.t_f, nullptr, nullptr, st, fz)) != NERFGB_OK)
     return rc;
-  if ((rc = nerfgb_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, uf, R, Sc, Sf, w.xyz_f,
-                               nullptr, w.t_f, nullptr, g.perm, stream)) != NERFGB_OK)
-    return rc;
-  if ((rc = launch_gate_fine(g.perm, g.mask_c, R, Sc, S, g.map_f, g.counts + 1, st)) != NERFGB_OK) return rc;
   RowMap rm_f;
   rm_f.map = g.map_f;
   rm_f.n_dev = g.counts + 1;
