@@ -56,8 +56,10 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--kernel", default=None, choices=["mlp", "train"],
-                    help="run only the MLP kernel at the fine-pass launch shape (for ncu)")
+    ap.add_argument("--kernel", default=None, choices=["mlp", "train", "chain"],
+                    help="mlp: the MLP kernel alone at the fine-pass launch shape; train: training steps; "
+                         "chain: the gated render of --chunks 4096-ray chunks (for ncu captures)")
+    ap.add_argument("--chunks", type=int, default=4)
     ap.add_argument("--rows", type=int, default=CHUNK * (SC + SF))
     ap.add_argument("--proposal", type=int, default=1, help="1: BF16 + learned proposal (headline)")
     ap.add_argument("--proposal-mode", default="gate", choices=["gate", "replace"])
@@ -122,6 +124,33 @@ def train_only(args):
     student.coarse_model.check_device_errors()
     print(json.dumps({"kernel": f"train_{args.path}", "batch_rays": 4096, "tile_rays": tile,
                       "step_ms": statistics.median(ts)}), flush=True)
+
+
+def chain_only(args):
+    """The gated render (untrained proposal) of the benchmark frame's first
+    `--chunks` 4096-ray chunks, `--warmup` + `--steps` times: the ray
+    kernels of one chunk at their render shapes, for ncu captures. Prints the
+    median step time."""
+    import torch
+    ng = importlib.import_module("nerf-tf2_gb300")
+    dev = torch.device("cuda", 0)
+    params = ng.make_params(N_coarse=SC, N_fine=SF)
+    blob = ng.synthetic.sparse_scene_blob(SCENE_SEED, max_freq_log2=SCENE_MAX_FREQ_LOG2)
+    nerf = ng.NeRF(params, precision=args.path, coarse_params=blob, fine_params=blob)
+    prop = ng.ProposalNetwork(seed=7)
+    n = CHUNK * args.chunks
+    rays = [torch.from_numpy(x[:n]).to(dev) for x in ng.synthetic.frame_rays(0, H, W, FOCAL)]
+    ts = []
+    for i in range(args.warmup + args.steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        nerf.render(*rays, chunk=CHUNK, seed=i, proposal=prop, proposal_mode="gate", gate_tau=args.gate_tau)
+        e1.record()
+        torch.cuda.synchronize()
+        if i >= args.warmup:
+            ts.append(e0.elapsed_time(e1))
+    nerf.coarse_model.check_device_errors()
+    print(json.dumps({"kernel": "chain", "rays": n, "step_ms": statistics.median(ts)}), flush=True)
 
 
 def dist_env():
@@ -317,6 +346,8 @@ def main():
         return kernel_only(args)
     if args.kernel == "train":
         return train_only(args)
+    if args.kernel == "chain":
+        return chain_only(args)
     import torch
     import torch.distributed as tdist
 
