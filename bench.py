@@ -63,12 +63,16 @@ def parse():
     ap.add_argument("--rows", type=int, default=CHUNK * (SC + SF))
     ap.add_argument("--proposal", type=int, default=1, help="1: BF16 + learned proposal (headline)")
     ap.add_argument("--proposal-mode", default="gate", choices=["gate", "replace"])
-    ap.add_argument("--gate-tau", type=float, default=1e-5)
+    ap.add_argument("--gate-tau", type=float, default=1e-4)
+    ap.add_argument("--gate-fine-draws", type=int, default=1,
+                    help="1: the gate also skips fine draws in coarse bins the proposal calls empty")
     ap.add_argument("--proposal-steps", type=int, default=2000)
     ap.add_argument("--train-steps", type=int, default=3)
     ap.add_argument("--train-tile", type=int, default=4096,
                     help="rays per recompute tile of the training backward (0: keep the forward's tape)")
     ap.add_argument("--sweep", type=int, default=1, help="1: FP32/BF16/FP8 sweep at 65536 rays x 256")
+    ap.add_argument("--glorot-scene", type=int, default=1,
+                    help="1: the gated path also on a plain Glorot-initialised scene with its own proposal")
     return ap.parse_args()
 
 
@@ -144,7 +148,8 @@ def chain_only(args):
     for i in range(args.warmup + args.steps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        nerf.render(*rays, chunk=CHUNK, seed=i, proposal=prop, proposal_mode="gate", gate_tau=args.gate_tau)
+        nerf.render(*rays, chunk=CHUNK, seed=i, proposal=prop, proposal_mode="gate", gate_tau=args.gate_tau,
+                    gate_fine_draws=bool(args.gate_fine_draws))
         e1.record()
         torch.cuda.synchronize()
         if i >= args.warmup:
@@ -391,6 +396,7 @@ def main():
         torch.cuda.synchronize()
         prop_info = {"train_rays": int(tr[0].shape[0]), "train_cameras": 100, "steps": args.proposal_steps,
                      "mode": args.proposal_mode, "gate_tau": args.gate_tau,
+                     "gate_fine_draws": bool(args.gate_fine_draws),
                      "loss_first": losses[0], "loss_last": losses[-1],
                      "train_s": round(time.perf_counter() - t0, 2)}
     # kernels per chunk: plain = coarse sample (Philox draws inside), coarse
@@ -401,7 +407,8 @@ def main():
     # compositing and fine gate inside), fine MLP, composite
     prop_kw = {}
     if proposal is not None:
-        prop_kw = {"proposal": proposal, "proposal_mode": args.proposal_mode, "gate_tau": args.gate_tau}
+        prop_kw = {"proposal": proposal, "proposal_mode": args.proposal_mode, "gate_tau": args.gate_tau,
+                   "gate_fine_draws": bool(args.gate_fine_draws)}
     launches_per_chunk = 5 if proposal is None else (7 if args.proposal_mode == "gate" else 6)
 
     def timed_steps(fn, steps, warmup):
@@ -482,6 +489,48 @@ def main():
             "rays_per_s": whole_job_rate(world, R, fp8_ms), "psnr_db": ng.psnr(gt, img_fp8["rgb"]),
             "psnr_gap_db": psnr_plain - ng.psnr(gt, img_fp8["rgb"]),
             "gate_met": bool(psnr_plain - ng.psnr(gt, img_fp8["rgb"]) <= 0.1)}
+    if proposal is not None and args.proposal_mode == "gate" and args.gate_fine_draws:
+        # the gate as it was before the fine draws were gated: coarse samples
+        # only, threshold 1e-5
+        co_kw = {"proposal": proposal, "proposal_mode": "gate", "gate_tau": 1e-5, "gate_fine_draws": False}
+        co_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, seed=1000 * i, **co_kw), args.plain_steps, 1)
+        co_psnr = ng.psnr(gt, fast.render(*sr, chunk=CHUNK, seed=7, **co_kw)["rgb"])
+        quality["gate_coarse_only_tau_1e-5"] = {"rays_per_s": whole_job_rate(world, R, co_ms), "psnr_db": co_psnr,
+                                                "psnr_gap_db": psnr_plain - co_psnr,
+                                                "gate_met": bool(psnr_plain - co_psnr <= 0.1)}
+    # the same gated path on a literal random-init scene: separate Glorot-uniform
+    # coarse and fine networks with zero biases, no density shaping, and a
+    # proposal trained on that scene's coarse histograms the same way. The
+    # plain FP32 path evaluates every sample whatever the scene, so its rate
+    # above is this scene's denominator too.
+    glorot = None
+    if proposal is not None and args.glorot_scene:
+        t0 = time.perf_counter()
+        bc, bfn = ng.weights.glorot_blob(31), ng.weights.glorot_blob(32)
+        g_fast = ng.NeRF(params, precision=args.path, coarse_params=bc, fine_params=bfn)
+        g_plain = ng.NeRF(params, precision="fp32", coarse_params=bc, fine_params=bfn)
+        g_prop = ng.ProposalNetwork(seed=7)
+        g_loss = ng.ProposalTrainer(g_prop, params, lr=3e-3).fit(*tr, uc, ng.proposal.coarse_histograms(g_fast, *tr, uc),
+                                                                  steps=args.proposal_steps)
+        g_kw = {"proposal": g_prop, "proposal_mode": "gate", "gate_tau": args.gate_tau,
+                "gate_fine_draws": bool(args.gate_fine_draws)}
+        g_ms = timed_steps(lambda i: g_fast.render(*rays, chunk=CHUNK, seed=1000 * i, **g_kw), args.plain_steps, 1)
+        g_gt = ng.NeRF(ng.make_params(N_coarse=SC, N_fine=512), precision="fp32", coarse_params=bc,
+                       fine_params=bfn).render(*sr, chunk=CHUNK, seed=9)["rgb"]
+        g_img_plain = g_plain.render(*sr, chunk=CHUNK, seed=7)
+        g_img = g_fast.render(*sr, chunk=CHUNK, seed=7, **g_kw)
+        g_bf16 = ng.psnr(g_gt, g_fast.render(*sr, chunk=CHUNK, seed=7)["rgb"])
+        g_fast.coarse_model.check_device_errors()
+        gp, gf = ng.psnr(g_gt, g_img_plain["rgb"]), ng.psnr(g_gt, g_img["rgb"])
+        glorot = {"scene": "coarse = Glorot-uniform blob seed 31, fine = seed 32, zero biases",
+                  "path": f"{args.path}+proposal (gate, tau {args.gate_tau:g}"
+                          + (", fine draws gated)" if args.gate_fine_draws else ")"), "rays_per_s": whole_job_rate(world, R, g_ms),
+                  "speedup_vs_plain_fp32": plain_ms / g_ms, "psnr_plain_fp32_db": gp, "psnr_fast_db": gf,
+                  "psnr_gap_db": gp - gf, "gate_met": bool(gp - gf <= 0.1),
+                  f"psnr_{args.path}_plain_db": g_bf16, f"psnr_gap_{args.path}_plain_db": gp - g_bf16,
+                  "depth_mae_fast_vs_plain": float((g_img_plain["depth"] - g_img["depth"]).abs().mean()),
+                  "mean_acc": float(g_img_plain["acc"].mean()), "proposal_loss_last": g_loss[-1],
+                  "setup_s": round(time.perf_counter() - t0, 2)}
     if proposal is not None:
         prop_info[other_mode] = {"rays_per_s": world * R / (other_ms / 1000.0),
                                  "psnr_db": ng.psnr(gt, img_other["rgb"]),
@@ -509,7 +558,8 @@ def main():
         if args.proposal_mode == "gate":
             w_gate, _, _, _ = oracle.nerf_render_gated(params, proposal.params.cpu().numpy(), p64, p64, *hsub,
                                                        uc_s.astype(np.float64), uf_s.astype(np.float64),
-                                                       args.gate_tau, np.float64)
+                                                       args.gate_tau, np.float64,
+                                                       gate_draws=bool(args.gate_fine_draws))
             fp64["headline_vs_gated_chain"] = fp64_errors(got, w_gate["pred_rgb"])
     cfg1 = config1(ng, dev)
 
@@ -612,7 +662,10 @@ def main():
                          "here); OpenBLAS on all host cores"}
 
     if rank == 0:
-        path = f"{args.path}+proposal ({args.proposal_mode})" if proposal is not None \
+        mode = args.proposal_mode
+        if mode == "gate":
+            mode += f", tau {args.gate_tau:g}" + (", fine draws gated" if args.gate_fine_draws else "")
+        path = f"{args.path}+proposal ({mode})" if proposal is not None \
             else f"{args.path} plain hierarchical"
         line = {
             "metric": METRIC, "value": value, "unit": "rays/s", "n_gpus": world, "steps": args.steps,
@@ -625,6 +678,7 @@ def main():
                            "speedup": plain_ms / ms},
             "bf16_plain": {"value": world * R / (bf16_ms / 1000.0), "unit": "rays/s"},
             "quality": quality,
+            "glorot_scene": glorot,
             "fp64_oracle": fp64,
             "config1_coarse_pass": cfg1,
             "proposal": prop_info,

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define NERFGB_ABI_VERSION 1
+#define NERFGB_ABI_VERSION 2
 
 /* Status codes. */
 #define NERFGB_OK 0
@@ -41,6 +41,9 @@ extern "C" {
 #define NERFGB_E_TIMEOUT (-4)     /* a bounded device wait ran out            */
 #define NERFGB_E_DEVICE (-5)      /* no usable sm_103 device                  */
 #define NERFGB_E_SCRATCH_LIMIT (-6) /* request needs more than the built-in scratch */
+
+/* Flags of nerfgb_render_rays_gated. */
+#define NERFGB_GATE_FINE_DRAWS 1 /* gate the fine draws by their coarse bins too */
 
 /* MLP arithmetic precision. */
 #define NERFGB_PREC_FP32 0 /* FP32 SIMT, FP32 accumulate                      */
@@ -304,11 +307,14 @@ int nerfgb_gate_coarse(const float *weights, int n_rays, int n_samples,
                        int *count, void *stream);
 
 /* Fine sample gate over the sorted coarse+fine union [R, n_samples]: member
- * j is on where it is a fine draw (sort_perm >= n_coarse) or its coarse
- * sample's mask is on. Appends r*n_samples + j to row_map, adds to *count. */
+ * j is on where it is a coarse sample whose mask is on, or a fine draw
+ * (sort_perm >= n_coarse). With piece_idxs (the fine sampler's bin of each
+ * draw, [R, n_samples - n_coarse]; NULL: every draw on) a fine draw is on
+ * only where its bin's coarse mask is on. Appends r*n_samples + j to
+ * row_map, adds to *count. */
 int nerfgb_gate_fine(const int *sort_perm, const unsigned char *mask_coarse,
-                     int n_rays, int n_coarse, int n_samples, int *row_map,
-                     int *count, void *stream);
+                     const int *piece_idxs, int n_rays, int n_coarse,
+                     int n_samples, int *row_map, int *count, void *stream);
 
 /* Workspace bytes of nerfgb_render_rays_gated (more than
  * nerfgb_render_workspace_bytes: the gates' masks and row maps). */
@@ -321,8 +327,11 @@ long long nerfgb_render_gated_workspace_bytes(int n_rays, int n_coarse,
  * samples whose proposal weight (nerfgb_proposal_weights of the proposal
  * density at the stratified samples) is at most gate_tau get sigma = 0 and
  * are not evaluated, in the coarse pass and again in the fine pass's sorted
- * union; fine draws are always evaluated. gate_tau < 0 evaluates every
- * sample and reproduces nerfgb_render_rays' fine maps bit for bit. */
+ * union. The fine draws are evaluated unless gate_flags has
+ * NERFGB_GATE_FINE_DRAWS: then a draw whose coarse bin is off is not
+ * evaluated either (sigma = 0; a ray whose bins are all off costs no MLP
+ * rows). gate_tau < 0 evaluates every sample and reproduces
+ * nerfgb_render_rays' fine maps bit for bit. */
 int nerfgb_render_rays_gated(const float *proposal_params,
                              const void *packed_coarse,
                              const void *packed_fine, int precision,
@@ -332,7 +341,7 @@ int nerfgb_render_rays_gated(const float *proposal_params,
                              unsigned long long seed, int n_rays,
                              int n_coarse, int n_fine, int perturb,
                              int lin_inv_depth, int white_bg, int trans_mode,
-                             float gate_tau, float *rgb_fine,
+                             float gate_tau, int gate_flags, float *rgb_fine,
                              float *depth_fine, float *acc_fine,
                              void *workspace, int *err_word, void *stream);
 

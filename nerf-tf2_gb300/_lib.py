@@ -29,6 +29,7 @@ E_SCRATCH_LIMIT = -6
 PREC_FP32 = 0
 PREC_BF16 = 1
 PREC_FP8 = 2
+GATE_FINE_DRAWS = 1
 TRANS_CUMPROD = 0
 TRANS_LOGSUM = 1
 
@@ -65,9 +66,9 @@ SIGNATURES = {
     "nerfgb_render_rays_proposal": (I, [P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I,
                                         P, P, P, P, P, P]),
     "nerfgb_gate_coarse": (I, [P, I, I, F, P, P, P, P]),
-    "nerfgb_gate_fine": (I, [P, P, I, I, I, P, P, P]),
+    "nerfgb_gate_fine": (I, [P, P, P, I, I, I, P, P, P]),
     "nerfgb_render_gated_workspace_bytes": (LL, [I, I, I]),
-    "nerfgb_render_rays_gated": (I, [P, P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I, F,
+    "nerfgb_render_rays_gated": (I, [P, P, P, I, P, P, P, P, P, P, ULL, I, I, I, I, I, I, I, F, I,
                                      P, P, P, P, P, P]),
     "nerfgb_composite_backward": (I, [P, P, P, P, P, I, I, I, P, P, P]),
     "nerfgb_mse_loss": (I, [P, P, LL, F, P, P, P]),

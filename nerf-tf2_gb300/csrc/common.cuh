@@ -212,7 +212,8 @@ enum BoundsSite {
   kSiteGateFinePerm = 6,  // fine gate: sort permutation entry
   kSiteGateFine = 7,      // fine gate: row-map slot
   kSiteMlpRowMap = 8,     // MLP: physical row of a row-map entry (tensor-core kernels)
-  kSiteMlpRowMapFp32 = 9  // MLP: physical row of a row-map entry (FP32 kernel)
+  kSiteMlpRowMapFp32 = 9,  // MLP: physical row of a row-map entry (FP32 kernel)
+  kSiteGateFinePiece = 10  // fine gate: coarse bin of a fine draw
 };
 
 }  // namespace nerfgb

@@ -43,8 +43,9 @@ __global__ void gate_coarse_kernel(const float *__restrict__ w, int R, int S, fl
   }
 }
 
-__global__ void gate_fine_kernel(const int *__restrict__ perm, const unsigned char *__restrict__ mask_c, int R,
-                                 int Sc, int S, int *__restrict__ row_map, int *__restrict__ count) {
+__global__ void gate_fine_kernel(const int *__restrict__ perm, const unsigned char *__restrict__ mask_c,
+                                 const int *__restrict__ piece, int R, int Sc, int S, int *__restrict__ row_map,
+                                 int *__restrict__ count) {
   const int ray = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
   const int lane = threadIdx.x & 31;
   if (ray >= R) return;
@@ -52,8 +53,14 @@ __global__ void gate_fine_kernel(const int *__restrict__ perm, const unsigned ch
   auto keep = [&](int j) -> bool {
     if (j >= S) return false;
     const int p = (int)NG_IDX(perm[row0 + j], S, kSiteGateFinePerm);
-    // a fine draw, or a coarse sample whose gate is on
-    return p >= Sc || (p >= 0 && mask_c[(long long)ray * Sc + p] != 0);
+    // a coarse sample whose gate is on, or a fine draw (given the draws'
+    // bins: one whose coarse bin's gate is on)
+    if (p >= Sc) {
+      if (!piece) return true;
+      const int bin = (int)NG_IDX(piece[(long long)ray * (S - Sc) + (p - Sc)], Sc, kSiteGateFinePiece);
+      return mask_c[(long long)ray * Sc + bin] != 0;
+    }
+    return p >= 0 && mask_c[(long long)ray * Sc + p] != 0;
   };
   int total = 0;
   for (int j0 = 0; j0 < S; j0 += 32) total += __popc(__ballot_sync(0xffffffffu, keep(j0 + lane)));
@@ -78,10 +85,10 @@ int launch_gate_coarse(const float *w, int R, int S, float tau, unsigned char *m
   return launch_status();
 }
 
-int launch_gate_fine(const int *perm, const unsigned char *mask_c, int R, int Sc, int S, int *row_map, int *count,
-                     cudaStream_t stream) {
+int launch_gate_fine(const int *perm, const unsigned char *mask_c, const int *piece, int R, int Sc, int S,
+                     int *row_map, int *count, cudaStream_t stream) {
   if (R == 0) return NERFGB_OK;
-  gate_fine_kernel<<<gate_grid(R), 256, 0, stream>>>(perm, mask_c, R, Sc, S, row_map, count);
+  gate_fine_kernel<<<gate_grid(R), 256, 0, stream>>>(perm, mask_c, piece, R, Sc, S, row_map, count);
   return launch_status();
 }
 
@@ -97,13 +104,14 @@ extern "C" int nerfgb_gate_coarse(const float *weights, int n_rays, int n_sample
   return launch_gate_coarse(weights, n_rays, n_samples, tau, mask, row_map, count, as_stream(stream));
 }
 
-extern "C" int nerfgb_gate_fine(const int *sort_perm, const unsigned char *mask_coarse, int n_rays, int n_coarse,
-                                int n_samples, int *row_map, int *count, void *stream) {
+extern "C" int nerfgb_gate_fine(const int *sort_perm, const unsigned char *mask_coarse, const int *piece_idxs,
+                                int n_rays, int n_coarse, int n_samples, int *row_map, int *count, void *stream) {
   if (n_rays < 0 || n_coarse < 1 || n_samples < n_coarse || (long long)n_rays * n_samples > 0x7fffffffLL)
     return NERFGB_E_INVALID_ARG;
   if (n_rays == 0) return NERFGB_OK;
   if (!sort_perm || !mask_coarse || !row_map || !count) return NERFGB_E_INVALID_ARG;
-  return launch_gate_fine(sort_perm, mask_coarse, n_rays, n_coarse, n_samples, row_map, count, as_stream(stream));
+  return launch_gate_fine(sort_perm, mask_coarse, piece_idxs, n_rays, n_coarse, n_samples, row_map, count,
+                          as_stream(stream));
 }
 
 #ifdef NERF_BOUNDS_CHECK

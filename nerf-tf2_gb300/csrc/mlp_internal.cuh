@@ -75,11 +75,13 @@ int launch_mlp(const void *packed, int precision, const float *xyz, const float 
 // writes mask[r*S + j] (0/1), appends the on samples' indices r*S + j to
 // row_map (rays in any order, samples of a ray in order) and adds their
 // number to *count. Fine: sample (r, j) of the sorted union is on where it is
-// a fine draw (perm >= Sc) or its coarse sample's mask is on.
+// a coarse sample whose mask is on, or a fine draw (perm >= Sc); with the
+// draws' bins (piece [R, S - Sc], not NULL) only a fine draw whose bin's mask
+// is on.
 int launch_gate_coarse(const float *w, int R, int S, float tau, unsigned char *mask, int *row_map, int *count,
                        cudaStream_t stream);
-int launch_gate_fine(const int *perm, const unsigned char *mask_c, int R, int Sc, int S, int *row_map, int *count,
-                     cudaStream_t stream);
+int launch_gate_fine(const int *perm, const unsigned char *mask_c, const int *piece, int R, int Sc, int S,
+                     int *row_map, int *count, cudaStream_t stream);
 
 // Proposal network forward (proposal.cu).
 int launch_proposal_forward(const float *params, const float *xyz, long long n, float *sigma, cudaStream_t stream);
@@ -127,6 +129,7 @@ struct FineFuse {
   const unsigned char *mask_c = nullptr;
   int *row_map = nullptr, *count = nullptr;
   float *sig_zero = nullptr, *rgb_zero = nullptr;
+  int gate_draws = 0;  // 1: a fine draw is on only where its coarse bin's gate is
   unsigned long long seed = 0;
 };
 int launch_fine_sample(const float *rays_o, const float *rays_d, const float *bin_weights, const float *left_edges,

@@ -300,6 +300,15 @@ __device__ __forceinline__ bool sort_before(float a, int ia, float b, int ib) {
   return a < b || (a == b && ia < ib);
 }
 
+// Shared-memory words per warp of fine_sample_kernel: w, pdf, left edges,
+// widths (4 Sc), the CDF (Sc + 1), concat and sorted t (2 S), the bitonic
+// keys and indices (2 P), the permutation (S), rgb_c (3 Sc), the draws'
+// bins (Sf).
+__host__ __device__ __forceinline__ int fine_smem_floats(int Sc, int Sf, int P) {
+  const int S = Sc + Sf;
+  return 4 * Sc + (Sc + 1) + 2 * S + 2 * P + S + 3 * Sc + Sf;
+}
+
 __global__ void __launch_bounds__(32 * kFineWarps)
     fine_sample_kernel(const float *__restrict__ rays_o, const float *__restrict__ rays_d,
                        const float *__restrict__ bin_weights, const float *__restrict__ left_edges,
@@ -311,7 +320,7 @@ __global__ void __launch_bounds__(32 * kFineWarps)
   extern __shared__ float smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int S = Sc + Sf;
-  const int per_warp = 4 * Sc + (Sc + 1) + 2 * S + 2 * P + S + 3 * Sc;
+  const int per_warp = fine_smem_floats(Sc, Sf, P);
   float *s_w = smem + warp * per_warp;  // w + 1e-5, then pdf * width
   float *s_pdf = s_w + Sc;
   float *s_left = s_pdf + Sc;
@@ -323,6 +332,7 @@ __global__ void __launch_bounds__(32 * kFineWarps)
   int *s_fi = reinterpret_cast<int *>(s_fk + P);  // ... and their fine indices
   int *s_perm = s_fi + P;         // the sort permutation, S
   float *s_rgbc = reinterpret_cast<float *>(s_perm + S);  // rgb_c of the ray, 3 Sc
+  int *s_pc = reinterpret_cast<int *>(s_rgbc + 3 * Sc);   // each fine draw's coarse bin, Sf
   for (int r = blockIdx.x * kFineWarps + warp; r < R; r += gridDim.x * kFineWarps) {
     const long long rb = (long long)r * Sc;
     if (fz.sigma_c) {
@@ -400,6 +410,7 @@ __global__ void __launch_bounds__(32 * kFineWarps)
       p_ = fmaxf(p_, 1e-8f);                                            // :373
       s_t[Sc + k] = fadd(fmul(fdiv(fsub(uk, a_), p_), mask), l_);       // :376
       if (piece_idxs) piece_idxs[ub + k] = first;
+      s_pc[k] = first;
     }
     __syncwarp();
     // Stable sort of concat(t_c, t_f) (:380-385).
@@ -488,12 +499,14 @@ __global__ void __launch_bounds__(32 * kFineWarps)
     if (sort_perm)
       for (int p = lane; p < S; p += 32) sort_perm[sb + p] = s_perm[p];
     if (fz.row_map) {
-      // the fine gate (the gated render): a fine draw, or a coarse sample whose gate is on
+      // the fine gate (the gated render): a coarse sample whose gate is on,
+      // or a fine draw (with gate_draws: one whose coarse bin's gate is on)
       const unsigned char *mc = fz.mask_c + rb;
+      const bool draws = fz.gate_draws != 0;
       gate_ray(lane, sb, S, R,
                [&](int j) {
                  const int q = (int)NG_IDX(s_perm[j], S, kSiteGateFinePerm);
-                 return q >= Sc || mc[q] != 0;
+                 return q >= Sc ? (!draws || mc[s_pc[q - Sc]] != 0) : mc[q] != 0;
                },
                nullptr, fz.row_map, fz.count, fz.sig_zero, fz.rgb_zero, kSiteGateFine);
     }
@@ -741,8 +754,7 @@ int launch_fine_sample(const float *rays_o, const float *rays_d, const float *bi
     P = 32;
     while (P < n_fine) P <<= 1;
   }
-  size_t smem =
-      (size_t)kFineWarps * (4 * n_coarse + (n_coarse + 1) + 2 * S + 2 * P + S + 3 * n_coarse) * sizeof(float);
+  size_t smem = (size_t)kFineWarps * fine_smem_floats(n_coarse, n_fine, P) * sizeof(float);
   if (smem > 48 * 1024 &&
       cudaFuncSetAttribute(fine_sample_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
           cudaSuccess)

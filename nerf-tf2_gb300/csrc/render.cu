@@ -167,7 +167,8 @@ extern "C" int nerfgb_render_rays_proposal(const float *proposal_params, const v
 // whose proposal weight (finite-bin compositing of the proposal density) is
 // at most gate_tau get sigma = 0 and are not evaluated, in the coarse pass
 // and again as members of the fine pass's sorted union; the fine draws are
-// always evaluated. With gate_tau < 0 every sample is evaluated and the
+// evaluated unless NERFGB_GATE_FINE_DRAWS gates them by their coarse bins'
+// decisions as well. With gate_tau < 0 every sample is evaluated and the
 // result equals nerfgb_render_rays bit for bit.
 // ---------------------------------------------------------------------------
 namespace nerfgb {
@@ -211,7 +212,8 @@ extern "C" int nerfgb_render_rays_gated(const float *proposal_params, const void
                                         const float *rays_d, const float *near, const float *far,
                                         const float *u_coarse, const float *u_fine, unsigned long long seed,
                                         int n_rays, int n_coarse, int n_fine, int perturb, int lin_inv_depth,
-                                        int white_bg, int trans_mode, float gate_tau, float *rgb_fine,
+                                        int white_bg, int trans_mode, float gate_tau, int gate_flags,
+                                        float *rgb_fine,
                                         float *depth_fine, float *acc_fine, void *workspace, int *err_word,
                                         void *stream) {
   if (n_rays < 0 || n_coarse < 2 || n_fine < 1) return NERFGB_E_INVALID_ARG;
@@ -226,6 +228,7 @@ extern "C" int nerfgb_render_rays_gated(const float *proposal_params, const void
   cudaStream_t st = as_stream(stream);
   const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
   if (trans_mode != NERFGB_TRANS_CUMPROD && trans_mode != NERFGB_TRANS_LOGSUM) return NERFGB_E_UNSUPPORTED;
+  if (gate_flags & ~NERFGB_GATE_FINE_DRAWS) return NERFGB_E_INVALID_ARG;
   RenderWs w = carve(workspace, R, Sc, Sf);
   GateWs g = carve_gate(workspace, R, Sc, Sf);
   int rc;
@@ -265,6 +268,7 @@ extern "C" int nerfgb_render_rays_gated(const float *proposal_params, const void
   fz.count = g.counts + 1;
   fz.sig_zero = w.sig_f;
   fz.rgb_zero = w.rgb_f;
+  fz.gate_draws = (gate_flags & NERFGB_GATE_FINE_DRAWS) ? 1 : 0;
   fz.seed = seed;
   if ((rc = launch_fine_sample(rays_o, rays_d, nullptr, w.edges, Sc + 1, w.widths, w.t_c, u_fine, R, Sc, Sf, w.xyz_f,
                                nullptr, w.t_f, nullptr, nullptr, st, fz)) != NERFGB_OK)

@@ -282,7 +282,7 @@ class NeRF:
 
     def render(self, rays_o, rays_d, near, far, *, chunk=4096, u_coarse=None, u_fine=None, seed=0,
                precision=None, return_coarse=False, proposal=None, proposal_mode="replace",
-               gate_tau=1e-5):
+               gate_tau=1e-4, gate_fine_draws=True):
         """Fine (and optionally coarse) rgb/depth/acc maps for every ray, in
         chunks of `chunk` rays (the reference renders 4096-ray batches,
         base_dataset.py:853-857). Uniforms come from Philox keyed by `seed`
@@ -291,7 +291,9 @@ class NeRF:
         "replace": its weights replace the coarse MLP's as the fine sampler's
         PDF (the coarse MLP does not run); "gate": the coarse and fine MLPs
         run as in the plain chain but skip the coarse samples whose proposal
-        weight is at most `gate_tau` (sigma = 0 there)."""
+        weight is at most `gate_tau` (sigma = 0 there); with
+        `gate_fine_draws` they also skip the fine draws that fall in such a
+        coarse bin."""
         if proposal is not None and proposal_mode not in ("replace", "gate"):
             raise ValueError(f"proposal_mode must be 'replace' or 'gate', not {proposal_mode!r}")
         gated = proposal is not None and proposal_mode == "gate"
@@ -327,7 +329,8 @@ class NeRF:
                           ctypes.c_ulonglong(int(seed) + s), e - s, Sc, Sf,
                           int(bool(self.params.sampling.perturb)),
                           int(bool(self.params.sampling.lin_inv_depth)), int(self.white_bg),
-                          int(self.trans_mode), ctypes.c_float(gate_tau), ptr(out["rgb"][sl]),
+                          int(self.trans_mode), ctypes.c_float(gate_tau),
+                          _lib.GATE_FINE_DRAWS if gate_fine_draws else 0, ptr(out["rgb"][sl]),
                           ptr(out["depth"][sl]), ptr(out["acc"][sl]), ptr(ws),
                           ptr(self.coarse_model.err_word), stream())
                 continue

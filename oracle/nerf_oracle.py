@@ -573,23 +573,33 @@ def gate_coarse(w_prop, tau):
     return np.asarray(w_prop) > tau
 
 
-def gate_fine(sort_perm, mask_c):
-    """On/off of each member of the sorted union [R, S]: a fine draw
-    (sort_perm >= Sc) or a coarse sample whose gate is on."""
+def gate_fine(sort_perm, mask_c, piece_idxs=None):
+    """On/off of each member of the sorted union [R, S]: a coarse sample
+    whose gate is on, or a fine draw (sort_perm >= Sc). With piece_idxs
+    [R, Sf] (the fine sampler's bin of each draw) a fine draw is on only
+    where its bin's coarse gate is on."""
     mask_c = np.asarray(mask_c, bool)
     Sc = mask_c.shape[1]
     perm = np.asarray(sort_perm)
     on_c = np.take_along_axis(mask_c, np.minimum(perm, Sc - 1), axis=1)
-    return (perm >= Sc) | on_c
+    if piece_idxs is None:
+        on_f = np.ones(perm.shape, bool)
+    else:
+        piece = np.asarray(piece_idxs)
+        bins = np.take_along_axis(piece, np.clip(perm - Sc, 0, piece.shape[1] - 1), axis=1)
+        on_f = np.take_along_axis(mask_c, bins, axis=1)
+    return np.where(perm >= Sc, on_f, on_c)
 
 
 def nerf_render_gated(params, prop_blob, p_coarse, p_fine, rays_o, rays_d, near, far,
-                      u_coarse, u_fine, tau, dtype=F32, mlp=None, prop=None, mask_c=None):
+                      u_coarse, u_fine, tau, dtype=F32, mlp=None, prop=None, mask_c=None,
+                      gate_draws=False):
     """Returns (fine post_process_model_output, coarse mask [R,Sc], union
     mask [R,S], proposal weights [R,Sc]). ``mlp(p, xyz, dirs)`` and
     ``prop(blob, xyz)`` replace mlp_forward and prop_forward when given;
     ``mask_c`` [R,Sc] replaces the coarse gate's decisions (e.g. the ones a
-    device run made)."""
+    device run made); ``gate_draws`` gates the fine draws by their bins'
+    coarse decisions too."""
     if mlp is None:
         mlp = lambda p, x, d: mlp_forward(p, x, d, dtype)  # noqa: E731
     if prop is None:
@@ -605,7 +615,7 @@ def nerf_render_gated(params, prop_blob, p_coarse, p_fine, rays_o, rays_d, near,
     d_fm = create_input_batch_fine_model(params, rays_o, rays_d, w_c, d_cm["bin_data"], t_c,
                                          u_fine, dtype, return_indices=True)
     rgb_f, sig_f = mlp(p_fine, d_fm["xyz_inputs"], d_fm["dir_inputs"])
-    m_f = gate_fine(d_fm["sort_perm"], m_c)
+    m_f = gate_fine(d_fm["sort_perm"], m_c, d_fm["piece_idxs"] if gate_draws else None)
     on = m_f.reshape(-1)
     sig_f = np.where(on, sig_f.reshape(-1), dtype(0))
     rgb_f = np.where(on[:, None], rgb_f, dtype(0))

@@ -29,7 +29,7 @@ def test_every_declared_symbol_is_exported_and_bound(lib, ng):
 
 
 def test_version_and_status_strings(lib, ng):
-    assert lib.nerfgb_abi_version() == 1
+    assert lib.nerfgb_abi_version() == 2
     assert ng._lib.status_name(0) == "NERFGB_OK"
     assert ng._lib.status_name(-4) == "NERFGB_E_TIMEOUT"
     assert ng._lib.status_name(-99) == "NERFGB_E_UNKNOWN"

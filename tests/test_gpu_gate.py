@@ -53,17 +53,19 @@ def test_gate_coarse_matches_oracle(ng, oracle, cuda, R, S):
 
 
 @pytest.mark.parametrize("R,Sc,Sf", [(41, 64, 128), (3, 7, 30), (1, 2, 1)])
-def test_gate_fine_matches_oracle(ng, oracle, cuda, R, Sc, Sf):
+@pytest.mark.parametrize("draws", [False, True])
+def test_gate_fine_matches_oracle(ng, oracle, cuda, R, Sc, Sf, draws):
     rng = np.random.default_rng(R + Sc)
     S = Sc + Sf
     perm = np.stack([rng.permutation(S) for _ in range(R)]).astype(np.int32)
     mask_c = rng.random((R, Sc)) < 0.3
+    piece = rng.integers(0, Sc, (R, Sf)).astype(np.int32)
     row_map = torch.full((R * S,), -1, dtype=torch.int32, device="cuda")
     count = torch.zeros(1, dtype=torch.int32, device="cuda")
-    pd, md = dev(perm), dev(mask_c.astype(np.uint8))
-    ng._lib.call("nerfgb_gate_fine", pd.data_ptr(), md.data_ptr(), R, Sc, S, row_map.data_ptr(),
-                 count.data_ptr(), _stream())
-    want = oracle.gate_fine(perm, mask_c)
+    pd, md, bd = dev(perm), dev(mask_c.astype(np.uint8)), dev(piece)
+    ng._lib.call("nerfgb_gate_fine", pd.data_ptr(), md.data_ptr(), bd.data_ptr() if draws else None, R, Sc, S,
+                 row_map.data_ptr(), count.data_ptr(), _stream())
+    want = oracle.gate_fine(perm, mask_c, piece if draws else None)
     assert int(count.item()) == int(want.sum())
     _check_map(row_map, int(count.item()), want, S)
 
@@ -140,8 +142,8 @@ def _close_most(got, want, atol, worst, frac_rays=0.04):
     assert err.max() < worst, float(err.max())
 
 
-@pytest.mark.parametrize("white_bg", [False, True])
-def test_gated_render_vs_oracle(ng, oracle, cuda, case, white_bg):
+@pytest.mark.parametrize("white_bg,draws", [(False, False), (True, False), (False, True)])
+def test_gated_render_vs_oracle(ng, oracle, cuda, case, white_bg, draws):
     R, o, d, n, f, uc, uf = case
     p = ng.make_params(white_bg=white_bg)
     bc, bf = ng.weights.glorot_blob(1), ng.weights.glorot_blob(2)
@@ -154,10 +156,15 @@ def test_gated_render_vs_oracle(ng, oracle, cuda, case, white_bg):
     nerf = ng.NeRF(p, precision="fp32", coarse_params=bc, fine_params=bf,
                    trans_mode=ng._lib.TRANS_CUMPROD)
     got = nerf.render(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc), u_fine=dev(uf), proposal=prop,
-                      proposal_mode="gate", gate_tau=tau)
+                      proposal_mode="gate", gate_tau=tau, gate_fine_draws=draws)
     want, m_c, m_f, _ = oracle.nerf_render_gated(p, blob, oracle.unpack_params(bc), oracle.unpack_params(bf),
-                                                 o, d, n, f, uc, uf, tau, F32)
+                                                 o, d, n, f, uc, uf, tau, F32, gate_draws=draws)
     assert 0.2 < m_c.mean() < 0.8
+    n_draws = m_f.shape[0] * (m_f.shape[1] - m_c.shape[1])
+    if draws:  # some fine draws are gated off too, not all
+        assert m_c.sum() < m_f.sum() < m_c.sum() + n_draws
+    else:
+        assert m_f.sum() == m_c.sum() + n_draws
     # Tolerance: as the plain FP32 chain against the fp32 oracle (1e-4 rgb/acc,
     # 5e-4 depth) on all but 4% of the rays. The fine sampler's bin choice is
     # discontinuous in the CDF, and FP32 rounding that differs between the
@@ -171,8 +178,8 @@ def test_gated_render_vs_oracle(ng, oracle, cuda, case, white_bg):
     assert float((plain["rgb"] - got["rgb"]).abs().max()) > 1e-3
 
 
-@pytest.mark.parametrize("precision", ["bf16", "fp8"])
-def test_gated_render_lowp_vs_oracle(ng, oracle, cuda, case, precision):
+@pytest.mark.parametrize("precision,draws", [("bf16", False), ("fp8", False), ("bf16", True)])
+def test_gated_render_lowp_vs_oracle(ng, oracle, cuda, case, precision, draws):
     """The headline path: the gated render with BF16 (or FP8) NeRF MLPs and
     the BF16 proposal kernel, against the oracle's gated chain with both
     networks emulated in the kernels' arithmetic (oracle.mlp_forward_lowp,
@@ -197,13 +204,13 @@ def test_gated_render_lowp_vs_oracle(ng, oracle, cuda, case, precision):
     nerf = ng.NeRF(p, precision=precision, coarse_params=bc, fine_params=bf,
                    trans_mode=ng._lib.TRANS_CUMPROD)
     got = nerf.render(dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc), u_fine=dev(uf), proposal=prop,
-                      proposal_mode="gate", gate_tau=tau)
+                      proposal_mode="gate", gate_tau=tau, gate_fine_draws=draws)
     nerf.coarse_model.check_device_errors()
     emul = lambda pp, x, dd: oracle.mlp_forward_lowp(pp, x, dd, precision)  # noqa: E731
     want, m_c, _, w_emul = oracle.nerf_render_gated(p, blob, oracle.unpack_params(bc), oracle.unpack_params(bf),
                                                     o, d, n, f, uc, uf, tau, F32, mlp=emul,
                                                     prop=lambda b, x: oracle.prop_forward_bf16(b, x),
-                                                    mask_c=mask_c)
+                                                    mask_c=mask_c, gate_draws=draws)
     # the emulated proposal agrees with the kernel's on all but a handful of gates
     assert ((w_emul > tau) != mask_c).mean() < 0.01
     tight = {"bf16": 5e-4, "fp8": 5e-3}[precision]
@@ -212,7 +219,8 @@ def test_gated_render_lowp_vs_oracle(ng, oracle, cuda, case, precision):
     _close_most(host(got["acc"]), want["acc_map"], tight, worst)
     _close_most(host(got["depth"]), want["pred_depth"], 10 * tight, 10 * worst)
     w64, _, _, _ = oracle.nerf_render_gated(p, blob, oracle.unpack_params(bc, F64), oracle.unpack_params(bf, F64),
-                                            o, d, n, f, uc.astype(F64), uf.astype(F64), tau, F64, mask_c=mask_c)
+                                            o, d, n, f, uc.astype(F64), uf.astype(F64), tau, F64, mask_c=mask_c,
+                                            gate_draws=draws)
     e64 = np.abs(host(got["rgb"]).astype(F64) - w64["pred_rgb"]).max(axis=1)
     print(f"gated {precision} vs FP64 gated oracle: rgb max {e64.max():.2e} mean {e64.mean():.2e}")
     assert e64.mean() < {"bf16": 5e-3, "fp8": 3e-2}[precision]
@@ -239,8 +247,14 @@ def test_gated_render_meets_quality_gate(ng, cuda):
     gt = ng.NeRF(ng.make_params(N_fine=512), precision="fp32", coarse_params=blob,
                  fine_params=blob).render(*rays, seed=9)["rgb"]
     psnr_plain = ng.psnr(gt, plain.render(*rays, seed=5)["rgb"])
-    psnr_gate = ng.psnr(gt, fast.render(*rays, seed=5, proposal=prop, proposal_mode="gate")["rgb"])
+    # the headline gate (threshold 1e-4, fine draws gated by their bins) and
+    # the coarse-samples-only gate at 1e-5
+    psnr_gate = ng.psnr(gt, fast.render(*rays, seed=5, proposal=prop, proposal_mode="gate", gate_tau=1e-4,
+                                        gate_fine_draws=True)["rgb"])
+    psnr_coarse = ng.psnr(gt, fast.render(*rays, seed=5, proposal=prop, proposal_mode="gate", gate_tau=1e-5,
+                                          gate_fine_draws=False)["rgb"])
     psnr_repl = ng.psnr(gt, fast.render(*rays, seed=5, proposal=prop)["rgb"])
     fast.coarse_model.check_device_errors()
     assert psnr_plain - psnr_gate <= 0.1, (psnr_plain, psnr_gate)
+    assert psnr_plain - psnr_coarse <= 0.1, (psnr_plain, psnr_coarse)
     assert psnr_plain - psnr_repl > 0.5, (psnr_plain, psnr_repl)

@@ -291,6 +291,11 @@ def test_gate_fine_hand_case(oracle):
     m_c = np.array([[True, False], [True, False]])
     want = np.array([[True, True, False, True], [False, True, True, True]])
     assert np.array_equal(oracle.gate_fine(perm, m_c), want)
+    # with the draws' bins: ray 0's draw 0 (perm 2) lies in bin 1 (off), draw 1
+    # (perm 3) in bin 0 (on); ray 1's draws both in bin 1 (off)
+    piece = np.array([[1, 0], [1, 1]])
+    want_d = np.array([[True, False, False, True], [False, True, False, False]])
+    assert np.array_equal(oracle.gate_fine(perm, m_c, piece), want_d)
     assert not oracle.gate_coarse(np.array([np.nan, 0.5, 0.1]), 0.1).tolist()[0]
     assert oracle.gate_coarse(np.array([np.nan, 0.5, 0.1]), 0.1).tolist() == [False, True, False]
 
@@ -322,6 +327,9 @@ def test_gated_render_skips_gated_samples(oracle, ng):
     got, m_c, m_f, _ = oracle.nerf_render_gated(p, blob, pc, pf, o, d, n, f, uc, uf, 10.0, F64)
     assert not m_c.any() and m_f.sum() == 4 * 128
     assert np.all(got["weights"][~m_f] == 0)
+    # gating the draws by their bins as well leaves nothing: empty rays
+    got, _, m_f, _ = oracle.nerf_render_gated(p, blob, pc, pf, o, d, n, f, uc, uf, 10.0, F64, gate_draws=True)
+    assert not m_f.any() and np.all(got["acc_map"] == 0) and np.all(got["pred_rgb"] == 0)
 
 
 # --- ray generation ----------------------------------------------------------
