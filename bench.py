@@ -401,15 +401,17 @@ def main():
                      "train_s": round(time.perf_counter() - t0, 2)}
     # kernels per chunk: plain = coarse sample (Philox draws inside), coarse
     # MLP, fine sample (coarse compositing inside), fine MLP, composite;
-    # replace = coarse sample, proposal forward, proposal weights, fine
-    # sample, fine MLP, composite; gate = coarse sample, proposal forward,
-    # proposal weights + coarse gate, coarse MLP, fine sample (coarse
-    # compositing and fine gate inside), fine MLP, composite
+    # BF16/FP8 replace = proposal front end (samples, proposal density and
+    # weights), fine sample, fine MLP, composite; BF16/FP8 gate = proposal
+    # front end (+ coarse gate), coarse MLP, fine sample (coarse compositing
+    # and fine gate inside), fine MLP, composite. The FP32 proposal paths run
+    # the sampler, proposal forward and weights as three kernels.
     prop_kw = {}
     if proposal is not None:
         prop_kw = {"proposal": proposal, "proposal_mode": args.proposal_mode, "gate_tau": args.gate_tau,
                    "gate_fine_draws": bool(args.gate_fine_draws)}
-    launches_per_chunk = 5 if proposal is None else (7 if args.proposal_mode == "gate" else 6)
+    launches_per_chunk = 5 if proposal is None else (5 if args.proposal_mode == "gate" else 4) + \
+        (2 if args.path == "fp32" else 0)
 
     def timed_steps(fn, steps, warmup):
         for i in range(warmup):

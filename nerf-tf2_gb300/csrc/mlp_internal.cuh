@@ -140,11 +140,21 @@ int launch_composite_bwd(const float *sigma, const float *t, const float *rgb, c
                          const float *grad_w, int R, int S, int white_bg, float last_delta, float *grad_sigma,
                          float *grad_rgb, cudaStream_t stream);
 
+// The BF16/FP8 proposal paths' front end (proposal.cu), one warp per ray:
+// stratified samples (xyz, t_vals, edges [R, S+1], widths), the BF16
+// proposal density at them, its weights over the bins (to w_out when not
+// NULL) and, with gate.row_map, the coarse gate.
+int launch_prop_front(const float *params, const float *rays_o, const float *rays_d, const float *near,
+                      const float *far, const float *u, unsigned long long seed, int R, int S, int perturb,
+                      int lin_inv, int mode, float *xyz, float *t_vals, float *edges, float *widths, float *w_out,
+                      const CompositeGate &gate, cudaStream_t stream);
+
 #ifdef NERF_BOUNDS_CHECK
 // Error words of the bounds-check build, one per translation unit (common.cuh).
 int bounds_read_ray_ops(int reset);
 int bounds_read_gate(int reset);
 int bounds_read_mlp(int reset);
+int bounds_read_proposal(int reset);
 int bounds_read_mlp_tc(int reset);
 #endif
 

@@ -23,6 +23,7 @@
 
 #include "common.cuh"
 #include "mlp_internal.cuh"
+#include "ray_device.cuh"
 
 namespace nerfgb {
 namespace prop {
@@ -132,122 +133,222 @@ __device__ __forceinline__ void mma_bf16(float (&d)[4], const uint32_t (&a)[4], 
       : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
       : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
 }
-__global__ void __launch_bounds__(32 * kFwdWarps)
-    prop_fwd_bf16_kernel(const float *__restrict__ params, const float *__restrict__ xyz, long long n,
-                         float *__restrict__ sigma) {
-  __shared__ __align__(16) __nv_bfloat16 sW1[kH * kLd1];
-  __shared__ __align__(16) __nv_bfloat16 sW2[kH * kLd2];
-  __shared__ float sB1[kH], sB2[kH], sW3[kH], sB3;
-  __shared__ __align__(16) __nv_bfloat16 sEnc[kFwdWarps][16 * kEncLdB];
-  // weights transposed into [n][k] (reads follow the [k][n] source, coalesced)
+// The proposal's weights in shared memory for the BF16 forward.
+struct PropSmemBf16 {
+  __nv_bfloat16 W1[kH * kLd1];
+  __nv_bfloat16 W2[kH * kLd2];
+  float B1[kH], B2[kH], W3[kH], B3;
+};
+
+// All threads of the block; the caller synchronises. Weights transposed into
+// [n][k] (reads follow the [k][n] source, coalesced).
+__device__ __forceinline__ void stage_weights_bf16(const float *__restrict__ params, PropSmemBf16 &sp) {
   for (int e = threadIdx.x; e < kLd1 * kH; e += blockDim.x) {
     const int k = e / kH, nn = e % kH;
-    sW1[nn * kLd1 + k] = __float2bfloat16_rn(k < kIn ? params[kW1 + k * kH + nn] : 0.0f);
+    sp.W1[nn * kLd1 + k] = __float2bfloat16_rn(k < kIn ? params[kW1 + k * kH + nn] : 0.0f);
   }
   for (int e = threadIdx.x; e < kLd2 * kH; e += blockDim.x) {
     const int k = e / kH, nn = e % kH;
-    sW2[nn * kLd2 + k] = __float2bfloat16_rn(k < kH ? params[kW2 + k * kH + nn] : 0.0f);
+    sp.W2[nn * kLd2 + k] = __float2bfloat16_rn(k < kH ? params[kW2 + k * kH + nn] : 0.0f);
   }
   for (int j = threadIdx.x; j < kH; j += blockDim.x) {
-    sB1[j] = params[kB1 + j];
-    sB2[j] = params[kB2 + j];
-    sW3[j] = params[kW3 + j];
+    sp.B1[j] = params[kB1 + j];
+    sp.B2[j] = params[kB2 + j];
+    sp.W3[j] = params[kW3 + j];
   }
-  if (threadIdx.x == 0) sB3 = params[kB3];
+  if (threadIdx.x == 0) sp.B3 = params[kB3];
+}
+
+// One 16-row tile's encodings (BF16) into the warp's buffer: two lanes per
+// row (row = lane / 2), each computing nine of the row's eighteen sin/cos
+// pairs (angles a = h, h + 2, ..., a = 6c + l) plus the three coordinates
+// (h = 0) or the zero padding (h = 1). x: the lane's row's point.
+__device__ __forceinline__ void encode_row_bf16(__nv_bfloat16 *enc, int lane, const float (&x)[3]) {
+  const int row = lane >> 1, h = lane & 1;
+  __nv_bfloat16 *er = enc + row * kEncLdB;
+  if (h == 0) {
+    er[0] = __float2bfloat16_rn(x[0]);
+    er[1] = __float2bfloat16_rn(x[1]);
+    er[2] = __float2bfloat16_rn(x[2]);
+  } else {
+#pragma unroll
+    for (int k = kIn; k < kK1; ++k) er[k] = __float2bfloat16_rn(0.0f);
+  }
+#pragma unroll
+  for (int a = h; a < 18; a += 2) {
+    const int c = a / 6, l = a % 6;
+    float sn, cs;
+    sincosf(fmul(x[c], enc_multiplier(l)), &sn, &cs);
+    er[3 + c * 12 + 2 * l] = __float2bfloat16_rn(sn);
+    er[3 + c * 12 + 2 * l + 1] = __float2bfloat16_rn(cs);
+  }
+}
+
+// The densities of the tile's rows g = lane / 4 (s0) and g + 8 (s1), valid
+// in the lanes with lane % 4 == 0, from the encodings in the warp's buffer.
+__device__ __forceinline__ void tile_sigma_bf16(const PropSmemBf16 &sp, const __nv_bfloat16 *enc, int lane,
+                                                float &s0, float &s1) {
+  const int g = lane >> 2, t = lane & 3;
+  // layer 1: [16 x 48] enc x [48 x 64] W1, accumulators start at b1
+  float d1[8][4];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    d1[j][0] = d1[j][2] = sp.B1[8 * j + 2 * t];
+    d1[j][1] = d1[j][3] = sp.B1[8 * j + 2 * t + 1];
+  }
+#pragma unroll
+  for (int ks = 0; ks < kK1 / 16; ++ks) {
+    const int k0 = 16 * ks + 2 * t;
+    const uint32_t *e0 = reinterpret_cast<const uint32_t *>(enc + g * kEncLdB + k0);
+    const uint32_t *e1 = reinterpret_cast<const uint32_t *>(enc + (g + 8) * kEncLdB + k0);
+    const uint32_t a[4] = {e0[0], e1[0], e0[4], e1[4]};
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const __nv_bfloat16 *b = sp.W1 + (8 * j + g) * kLd1 + k0;
+      mma_bf16(d1[j], a, *reinterpret_cast<const uint32_t *>(b), *reinterpret_cast<const uint32_t *>(b + 8));
+    }
+  }
+  // layer 2: relu(h1) as BF16 A fragments straight from the layer-1 accumulators
+  float d2[8][4];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    d2[j][0] = d2[j][2] = sp.B2[8 * j + 2 * t];
+    d2[j][1] = d2[j][3] = sp.B2[8 * j + 2 * t + 1];
+  }
+#pragma unroll
+  for (int ks = 0; ks < kH / 16; ++ks) {
+    const uint32_t a[4] = {bf16x2_relu(d1[2 * ks][0], d1[2 * ks][1]), bf16x2_relu(d1[2 * ks][2], d1[2 * ks][3]),
+                           bf16x2_relu(d1[2 * ks + 1][0], d1[2 * ks + 1][1]),
+                           bf16x2_relu(d1[2 * ks + 1][2], d1[2 * ks + 1][3])};
+    const int k0 = 16 * ks + 2 * t;
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const __nv_bfloat16 *b = sp.W2 + (8 * j + g) * kLd2 + k0;
+      mma_bf16(d2[j], a, *reinterpret_cast<const uint32_t *>(b), *reinterpret_cast<const uint32_t *>(b + 8));
+    }
+  }
+  // layer 3 (FP32): relu(z2) . w3 over this thread's 16 columns, then the quad
+  float p0 = 0.0f, p1 = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const float w0 = sp.W3[8 * j + 2 * t], w1 = sp.W3[8 * j + 2 * t + 1];
+    p0 = fmaf(fmaxf(d2[j][0], 0.0f), w0, fmaf(fmaxf(d2[j][1], 0.0f), w1, p0));
+    p1 = fmaf(fmaxf(d2[j][2], 0.0f), w0, fmaf(fmaxf(d2[j][3], 0.0f), w1, p1));
+  }
+  p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
+  p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
+  p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
+  p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
+  s0 = softplus(sp.B3 + p0);
+  s1 = softplus(sp.B3 + p1);
+}
+
+__global__ void __launch_bounds__(32 * kFwdWarps)
+    prop_fwd_bf16_kernel(const float *__restrict__ params, const float *__restrict__ xyz, long long n,
+                         float *__restrict__ sigma) {
+  __shared__ __align__(16) PropSmemBf16 sp;
+  __shared__ __align__(16) __nv_bfloat16 sEnc[kFwdWarps][16 * kEncLdB];
+  stage_weights_bf16(params, sp);
   __syncthreads();
   const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
   const long long ntiles = (n + 15) / 16;
   const long long wstride = (long long)gridDim.x * kFwdWarps;
+  __nv_bfloat16 *enc = sEnc[threadIdx.x >> 5];
   for (long long tile = (long long)blockIdx.x * kFwdWarps + (threadIdx.x >> 5); tile < ntiles; tile += wstride) {
     const long long r0 = tile * 16 + g, r1 = r0 + 8;
-    // The tile's encodings (BF16) into the warp's buffer: two lanes per row,
-    // each computing nine of the row's eighteen sin/cos pairs (angles a = h,
-    // h + 2, ..., a = 6c + l) plus the three coordinates (h = 0) or the zero
-    // padding (h = 1).
-    __nv_bfloat16 *enc = sEnc[threadIdx.x >> 5];
     {
-      const int row = lane >> 1, h = lane & 1;
-      const long long gr = tile * 16 + row;
+      const long long gr = tile * 16 + (lane >> 1);
       float x[3] = {0.f, 0.f, 0.f};
       if (gr < n) {
         x[0] = xyz[3 * gr];
         x[1] = xyz[3 * gr + 1];
         x[2] = xyz[3 * gr + 2];
       }
-      __nv_bfloat16 *er = enc + row * kEncLdB;
-      if (h == 0) {
-        er[0] = __float2bfloat16_rn(x[0]);
-        er[1] = __float2bfloat16_rn(x[1]);
-        er[2] = __float2bfloat16_rn(x[2]);
-      } else {
-#pragma unroll
-        for (int k = kIn; k < kK1; ++k) er[k] = __float2bfloat16_rn(0.0f);
-      }
-#pragma unroll
-      for (int a = h; a < 18; a += 2) {
-        const int c = a / 6, l = a % 6;
-        float sn, cs;
-        sincosf(fmul(x[c], enc_multiplier(l)), &sn, &cs);
-        er[3 + c * 12 + 2 * l] = __float2bfloat16_rn(sn);
-        er[3 + c * 12 + 2 * l + 1] = __float2bfloat16_rn(cs);
-      }
+      encode_row_bf16(enc, lane, x);
     }
     __syncwarp();
-    // layer 1: [16 x 48] enc x [48 x 64] W1, accumulators start at b1
-    float d1[8][4];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      d1[j][0] = d1[j][2] = sB1[8 * j + 2 * t];
-      d1[j][1] = d1[j][3] = sB1[8 * j + 2 * t + 1];
-    }
-#pragma unroll
-    for (int ks = 0; ks < kK1 / 16; ++ks) {
-      const int k0 = 16 * ks + 2 * t;
-      const uint32_t *e0 = reinterpret_cast<const uint32_t *>(enc + g * kEncLdB + k0);
-      const uint32_t *e1 = reinterpret_cast<const uint32_t *>(enc + (g + 8) * kEncLdB + k0);
-      const uint32_t a[4] = {e0[0], e1[0], e0[4], e1[4]};
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const __nv_bfloat16 *b = sW1 + (8 * j + g) * kLd1 + k0;
-        mma_bf16(d1[j], a, *reinterpret_cast<const uint32_t *>(b), *reinterpret_cast<const uint32_t *>(b + 8));
-      }
-    }
-    // layer 2: relu(h1) as BF16 A fragments straight from the layer-1 accumulators
-    float d2[8][4];
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      d2[j][0] = d2[j][2] = sB2[8 * j + 2 * t];
-      d2[j][1] = d2[j][3] = sB2[8 * j + 2 * t + 1];
-    }
-#pragma unroll
-    for (int ks = 0; ks < kH / 16; ++ks) {
-      const uint32_t a[4] = {bf16x2_relu(d1[2 * ks][0], d1[2 * ks][1]), bf16x2_relu(d1[2 * ks][2], d1[2 * ks][3]),
-                             bf16x2_relu(d1[2 * ks + 1][0], d1[2 * ks + 1][1]),
-                             bf16x2_relu(d1[2 * ks + 1][2], d1[2 * ks + 1][3])};
-      const int k0 = 16 * ks + 2 * t;
-#pragma unroll
-      for (int j = 0; j < 8; ++j) {
-        const __nv_bfloat16 *b = sW2 + (8 * j + g) * kLd2 + k0;
-        mma_bf16(d2[j], a, *reinterpret_cast<const uint32_t *>(b), *reinterpret_cast<const uint32_t *>(b + 8));
-      }
-    }
-    // layer 3 (FP32): relu(z2) . w3 over this thread's 16 columns, then the quad
-    float p0 = 0.0f, p1 = 0.0f;
-#pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      const float w0 = sW3[8 * j + 2 * t], w1 = sW3[8 * j + 2 * t + 1];
-      p0 = fmaf(fmaxf(d2[j][0], 0.0f), w0, fmaf(fmaxf(d2[j][1], 0.0f), w1, p0));
-      p1 = fmaf(fmaxf(d2[j][2], 0.0f), w0, fmaf(fmaxf(d2[j][3], 0.0f), w1, p1));
-    }
-    p0 += __shfl_xor_sync(0xffffffffu, p0, 1);
-    p1 += __shfl_xor_sync(0xffffffffu, p1, 1);
-    p0 += __shfl_xor_sync(0xffffffffu, p0, 2);
-    p1 += __shfl_xor_sync(0xffffffffu, p1, 2);
+    float s0, s1;
+    tile_sigma_bf16(sp, enc, lane, s0, s1);
     if (t == 0) {
-      if (r0 < n) sigma[r0] = softplus(sB3 + p0);
-      if (r1 < n) sigma[r1] = softplus(sB3 + p1);
+      if (r0 < n) sigma[r0] = s0;
+      if (r1 < n) sigma[r1] = s1;
     }
     __syncwarp();  // the buffer is rewritten by the next tile
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Front end of the BF16/FP8 proposal paths, one warp per ray: the ray's S
+// stratified samples (coarse_sample_kernel's arithmetic: Philox draws
+// inside, t, bin edges, widths, points written out), the proposal density
+// at them (prop_fwd_bf16_kernel's arithmetic, 16 samples per tile), the
+// proposal weights over the bins (composite_ray with the finite last
+// interval, nerfgb_proposal_weights' arithmetic) written to w_out when
+// given, and with gate_map the coarse gate (sample j on where its weight >
+// tau; gate_ray zeroes the coarse sigma at the off samples). Replaces the
+// coarse sampler, proposal forward and proposal compositing launches.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(32 * kFwdWarps)
+    prop_front_kernel(const float *__restrict__ params, const float *__restrict__ rays_o,
+                      const float *__restrict__ rays_d, const float *__restrict__ near,
+                      const float *__restrict__ far, const float *__restrict__ u, unsigned long long seed, int R,
+                      int S, int perturb, int lin_inv, int mode, float *__restrict__ xyz, float *__restrict__ t_out,
+                      float *__restrict__ edges, float *__restrict__ widths, float *__restrict__ w_out, float tau,
+                      unsigned char *__restrict__ gate_mask, int *__restrict__ gate_map,
+                      int *__restrict__ gate_count, float *__restrict__ gate_sig_zero) {
+  __shared__ __align__(16) PropSmemBf16 sp;
+  __shared__ __align__(16) __nv_bfloat16 sEnc[kFwdWarps][16 * kEncLdB];
+  extern __shared__ float fsm[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t4 = lane & 3;
+  float *s_t = fsm + warp * 6 * S;  // t [S], sigma [S], weights [S], points [3S]
+  float *s_sig = s_t + S;
+  float *s_w = s_sig + S;
+  float *s_x = s_w + S;
+  __nv_bfloat16 *enc = sEnc[warp];
+  stage_weights_bf16(params, sp);
+  __syncthreads();
+  for (int r = blockIdx.x * kFwdWarps + warp; r < R; r += gridDim.x * kFwdWarps) {
+    const long long base = (long long)r * S;
+    const float nr = near[r], fr = far[r];
+    for (int i = lane; i < S; i += 32) {
+      const BinSample b = coarse_bin_sample(rays_o, rays_d, nr, fr, u, seed, r, S, i, perturb, lin_inv);
+      t_out[base + i] = b.t;
+      widths[base + i] = b.w;
+      edges[(long long)r * (S + 1) + i] = b.e0;
+      if (i == S - 1) edges[(long long)r * (S + 1) + S] = b.e1;
+      s_t[i] = b.t;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) s_x[3 * i + c] = b.x[c];
+    }
+    __syncwarp();
+    for (int j = lane; j < 3 * S; j += 32) xyz[3 * base + j] = s_x[j];
+    for (int i0 = 0; i0 < S; i0 += 16) {
+      const int i = i0 + (lane >> 1);
+      float x[3] = {0.f, 0.f, 0.f};
+      if (i < S) {
+        x[0] = s_x[3 * i];
+        x[1] = s_x[3 * i + 1];
+        x[2] = s_x[3 * i + 2];
+      }
+      encode_row_bf16(enc, lane, x);
+      __syncwarp();
+      float s0, s1;
+      tile_sigma_bf16(sp, enc, lane, s0, s1);
+      if (t4 == 0) {
+        if (i0 + g < S) s_sig[i0 + g] = s0;
+        if (i0 + g + 8 < S) s_sig[i0 + g + 8] = s1;
+      }
+      __syncwarp();  // the buffer is rewritten by the next tile; s_sig complete
+    }
+    float m[5];
+    composite_ray(lane, s_t, s_sig, nullptr, S, mode, -1.0f, s_w, m);
+    __syncwarp();
+    if (w_out)
+      for (int j = lane; j < S; j += 32) w_out[base + j] = s_w[j];
+    if (gate_map)
+      gate_ray(lane, base, S, R, [&](int j) { return s_w[j] > tau; }, gate_mask, gate_map, gate_count,
+               gate_sig_zero, nullptr, kSiteGateCoarse);
+    __syncwarp();
   }
 }
 
@@ -376,6 +477,26 @@ int launch_proposal_forward_bf16(const float *params, const float *xyz, long lon
   return launch_status();
 }
 
+int launch_prop_front(const float *params, const float *rays_o, const float *rays_d, const float *near,
+                      const float *far, const float *u, unsigned long long seed, int R, int S, int perturb,
+                      int lin_inv, int mode, float *xyz, float *t_vals, float *edges, float *widths, float *w_out,
+                      const CompositeGate &gate, cudaStream_t stream) {
+  if (R == 0) return NERFGB_OK;
+  const size_t smem = (size_t)prop::kFwdWarps * 6 * S * sizeof(float);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute(prop::prop_front_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) !=
+          cudaSuccess)
+    return NERFGB_E_CUDA;
+  // persistent: each CTA converts the weights once for many rays
+  const long long blocks = (R + prop::kFwdWarps - 1) / prop::kFwdWarps;
+  const int sms = num_sms();
+  const long long cap = (long long)(sms > 0 ? sms : 148) * 4;
+  prop::prop_front_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 32 * prop::kFwdWarps, smem, stream>>>(
+      params, rays_o, rays_d, near, far, u, seed, R, S, perturb, lin_inv, mode, xyz, t_vals, edges, widths, w_out,
+      gate.tau, gate.mask, gate.row_map, gate.count, gate.sig_zero);
+  return launch_status();
+}
+
 }  // namespace nerfgb
 
 using namespace nerfgb;
@@ -434,3 +555,9 @@ extern "C" int nerfgb_proposal_backward(const float *params, const float *xyz, c
                                                                                       grad_params);
   return launch_status();
 }
+
+#ifdef NERF_BOUNDS_CHECK
+namespace nerfgb {
+NG_BOUNDS_READER(bounds_read_proposal)
+}  // namespace nerfgb
+#endif

@@ -55,11 +55,11 @@ using namespace nerfgb;
 
 extern "C" int nerfgb_bounds_check_status(int reset) {
 #ifdef NERF_BOUNDS_CHECK
-  const int v[4] = {bounds_read_ray_ops(reset), bounds_read_gate(reset), bounds_read_mlp(reset),
-                    bounds_read_mlp_tc(reset)};
-  for (int i = 0; i < 4; ++i)
+  const int v[5] = {bounds_read_ray_ops(reset), bounds_read_gate(reset), bounds_read_mlp(reset),
+                    bounds_read_mlp_tc(reset), bounds_read_proposal(reset)};
+  for (int i = 0; i < 5; ++i)
     if (v[i] < 0) return NERFGB_E_CUDA;
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < 5; ++i)
     if (v[i] != 0) return v[i];
   return NERFGB_OK;
 #else
@@ -142,13 +142,20 @@ extern "C" int nerfgb_render_rays_proposal(const float *proposal_params, const v
   const int R = n_rays, Sc = n_coarse, Sf = n_fine, S = Sc + Sf;
   RenderWs w = carve(workspace, R, Sc, Sf);
   int rc;
-  if ((rc = launch_coarse_sample(rays_o, rays_d, near, far, u_coarse, seed, R, Sc, perturb, lin_inv_depth, w.xyz_c,
-                                 nullptr, w.t_c, w.edges, w.widths, st)) != NERFGB_OK)
+  // The proposal density at the stratified samples replaces the coarse MLP;
+  // its weights are the fine sampler's PDF.
+  if (precision == NERFGB_PREC_FP32) {
+    if ((rc = launch_coarse_sample(rays_o, rays_d, near, far, u_coarse, seed, R, Sc, perturb, lin_inv_depth,
+                                   w.xyz_c, nullptr, w.t_c, w.edges, w.widths, st)) != NERFGB_OK)
+      return rc;
+    if ((rc = launch_proposal(precision, proposal_params, w.xyz_c, (long long)R * Sc, w.sig_c, st)) != NERFGB_OK)
+      return rc;
+    if ((rc = nerfgb_proposal_weights(w.sig_c, w.t_c, R, Sc, trans_mode, w.w_c, stream)) != NERFGB_OK) return rc;
+  } else if ((rc = launch_prop_front(proposal_params, rays_o, rays_d, near, far, u_coarse, seed, R, Sc, perturb,
+                                     lin_inv_depth, trans_mode, w.xyz_c, w.t_c, w.edges, w.widths, w.w_c,
+                                     CompositeGate(), st)) != NERFGB_OK) {
     return rc;
-  // The proposal density at the stratified samples replaces the coarse MLP.
-  if ((rc = launch_proposal(precision, proposal_params, w.xyz_c, (long long)R * Sc, w.sig_c, st)) != NERFGB_OK)
-    return rc;
-  if ((rc = nerfgb_proposal_weights(w.sig_c, w.t_c, R, Sc, trans_mode, w.w_c, stream)) != NERFGB_OK) return rc;
+  }
   FineFuse fz;
   fz.seed = seed;
   if ((rc = launch_fine_sample(rays_o, rays_d, w.w_c, w.edges, Sc + 1, w.widths, w.t_c, u_fine, R, Sc, Sf, w.xyz_f,
@@ -235,22 +242,29 @@ extern "C" int nerfgb_render_rays_gated(const float *proposal_params, const void
   // Uniforms: the counters of nerfgb_render_rays (drawn in the samplers), so
   // equal seeds give equal draws.
   if (cudaMemsetAsync(g.counts, 0, 2 * sizeof(int), st) != cudaSuccess) return NERFGB_E_CUDA;
-  if ((rc = launch_coarse_sample(rays_o, rays_d, near, far, u_coarse, seed, R, Sc, perturb, lin_inv_depth, w.xyz_c,
-                                 nullptr, w.t_c, w.edges, w.widths, st)) != NERFGB_OK)
-    return rc;
   // Proposal weights over the coarse bins and the coarse gate in one pass:
   // the off samples' sigma is zeroed (the row-mapped MLP writes the others).
-  if ((rc = launch_proposal(precision, proposal_params, w.xyz_c, (long long)R * Sc, g.sig_p, st)) != NERFGB_OK)
-    return rc;
   CompositeGate cg;
   cg.tau = gate_tau;
   cg.mask = g.mask_c;
   cg.row_map = g.map_c;
   cg.count = g.counts;
   cg.sig_zero = w.sig_c;
-  if ((rc = launch_composite(nullptr, g.sig_p, w.t_c, R, Sc, 0, trans_mode, -1.0f, nullptr, nullptr, nullptr, nullptr,
-                             st, cg)) != NERFGB_OK)
+  if (precision == NERFGB_PREC_FP32) {
+    if ((rc = launch_coarse_sample(rays_o, rays_d, near, far, u_coarse, seed, R, Sc, perturb, lin_inv_depth,
+                                   w.xyz_c, nullptr, w.t_c, w.edges, w.widths, st)) != NERFGB_OK)
+      return rc;
+    if ((rc = launch_proposal(precision, proposal_params, w.xyz_c, (long long)R * Sc, g.sig_p, st)) != NERFGB_OK)
+      return rc;
+    if ((rc = launch_composite(nullptr, g.sig_p, w.t_c, R, Sc, 0, trans_mode, -1.0f, nullptr, nullptr, nullptr,
+                               nullptr, st, cg)) != NERFGB_OK)
+      return rc;
+  } else if ((rc = launch_prop_front(proposal_params, rays_o, rays_d, near, far, u_coarse, seed, R, Sc, perturb,
+                                     lin_inv_depth, trans_mode, w.xyz_c, w.t_c, w.edges, w.widths, nullptr, cg,
+                                     st)) != NERFGB_OK) {
+    // BF16/FP8: samples, proposal density, weights and gate in one kernel
     return rc;
+  }
   RowMap rm_c;
   rm_c.map = g.map_c;
   rm_c.n_dev = g.counts;

@@ -123,6 +123,31 @@ def test_gated_all_on_equals_plain(ng, cuda, case, precision):
         assert torch.equal(gated[k], plain[k]), k
 
 
+@pytest.mark.parametrize("precision", ["bf16", "fp8"])
+def test_replace_render_equals_op_by_op(ng, cuda, case, precision):
+    """The BF16/FP8 proposal paths' front end (stratified samples, the BF16
+    proposal density and its weights over the bins in one kernel) gives the
+    op-by-op chain's maps bit for bit: coarse sampler, proposal forward,
+    proposal weights, fine sampler, fine MLP, compositor."""
+    R, o, d, n, f, uc, uf = case
+    p = ng.make_params()
+    nerf = ng.NeRF(p, precision=precision, coarse_params=ng.weights.glorot_blob(1),
+                   fine_params=ng.weights.glorot_blob(2))
+    prop = ng.ProposalNetwork(seed=3)
+    args = [dev(x) for x in (o, d, n, f)]
+    got = nerf.render(*args, u_coarse=dev(uc), u_fine=dev(uf), chunk=40, proposal=prop, proposal_mode="replace")
+    d_cm = ng.ray_utils.create_input_batch_coarse_model(p, *args, u_vals=dev(uc))
+    w = ng.proposal.proposal_weights(prop(d_cm["xyz_inputs"], precision="bf16"), d_cm["t_vals"],
+                                     trans_mode=nerf.trans_mode)
+    d_fm = ng.ray_utils.create_input_batch_fine_model(p, args[0], args[1], w, d_cm["bin_data"], d_cm["t_vals"],
+                                                      u_vals=dev(uf))
+    rgb, sig = nerf.fine_model((d_fm["xyz_inputs"], args[1]), rows_per_dir=d_fm["t_vals"].shape[1])
+    want = ng.ray_utils.post_process_model_output(rgb, sig, d_fm["t_vals"], nerf.white_bg, trans_mode=nerf.trans_mode)
+    nerf.fine_model.check_device_errors()
+    for k, kk in (("rgb", "pred_rgb"), ("depth", "pred_depth"), ("acc", "acc_map")):
+        assert torch.equal(got[k], want[kk].reshape(got[k].shape)), k
+
+
 def _margin_tau(w, q, gap=1.0005):
     """A gate threshold near the q-quantile of w with no weight within a
     factor sqrt(gap) of it (FP32 rounding moves a weight by ~1e-6 relative;
