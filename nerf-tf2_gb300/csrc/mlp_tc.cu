@@ -19,13 +19,13 @@
 //     weight chunk streamed once per sub-tile, 8 epilogue warps per sub-tile.
 //
 // Warp roles (18 warps):
-//   warp 0      weight producer: cp.async.bulk of KCH-row weight chunks into
+//   warp 0      weight producer: bulk copies of KCH-row weight chunks into
 //               an NST-stage ring (full/empty mbarriers); pair: one thread in
-//               ring order, single CTA: one lane per stage
+//               ring order issuing 2-SM tensor copies that complete on the
+//               even CTA's barrier, single CTA: one lane per stage
 //   warp 1      TMEM allocator and MMA issuer (one thread; its issue code is
 //               generated per layer at compile time, see issue_run); in the
-//               odd CTA of a pair it relays each landed weight half to the
-//               even CTA's full barrier
+//               odd CTA of a pair only the allocator
 //   warps 2-17  epilogue: compute the positional encodings, then per layer
 //               read the accumulator (tcgen05.ld), add bias, apply ReLU,
 //               round to BF16 (or E4M3) and write the next layer's A operand;
@@ -44,6 +44,7 @@
 // drains its own bulk copies and MMAs (bounded), frees TMEM and returns (a
 // pair meets at a cluster barrier first, so that neither CTA leaves while
 // the other's MMAs or arrivals may still touch it).
+#include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's entry-point query)
 #include <cuda_bf16.h>
 #include <cuda_fp8.h>
 #include <stdint.h>
@@ -60,6 +61,13 @@ namespace tc {
 
 constexpr int kRows = 256;          // rows per CTA tile
 constexpr int kThreads = 18 * 32;
+
+// Tensor maps of the pair pack's weights (2-D, 256-byte rows of 128 BF16),
+// one per weight-half size: 64 rows (16 KB), 32 (8 KB), 16 (4 KB).
+struct PairMaps {
+  CUtensorMap map[3];
+};
+__host__ __device__ constexpr int pair_map_of(uint32_t bytes) { return bytes == 16384u ? 0 : bytes == 8192u ? 1 : 2; }
 
 // Shared-memory layout. Operands take E = 2 (BF16) or 1 (FP8) bytes per
 // element. TSMEM: the bias/head table (and, for FP8, the per-channel weight
@@ -465,15 +473,16 @@ __device__ __forceinline__ void for_each_load(long long t_first, long long t_ste
 // sub-tile s of both CTAs) and each CTA streams only its N/2 half of every
 // weight chunk (kBf16PairOff layout), halving the bytes an SM takes in; with
 // half chunks of 16 KB a 4-stage ring holds a whole 256-K layer, so such a
-// layer is streamed once for both sub-tiles. The odd CTA's producer relays
-// each landed half to the even CTA's full barrier, and its epilogue warps
-// arrive on the even CTA's operand barriers; commits reach both CTAs.
+// layer is streamed once for both sub-tiles. Both CTAs' halves are 2-SM
+// tensor copies (maps: the pair pack as 256-byte rows) completing on the even
+// CTA's full barrier; the odd CTA's epilogue warps arrive on the even CTA's
+// operand barriers; commits reach both CTAs.
 template <int KCH, int NST, bool PINGPONG, bool TSMEM, bool F8, bool STORE, bool PAIR = false>
 __global__ void __launch_bounds__(kThreads, 1)
     mlp_tc_kernel(const uint8_t *__restrict__ packed, const float *__restrict__ xyz,
                     const float *__restrict__ dirs, long long n_max, int rpd, float *__restrict__ rgb_out,
                     float *__restrict__ sigma_out, int *__restrict__ err, RowMap rm, uint16_t *__restrict__ tape,
-                    unsigned long long wait_ns, long long withhold) {
+                    unsigned long long wait_ns, long long withhold, const __grid_constant__ PairMaps maps) {
   static_assert(!(STORE && F8), "the activation tape is BF16");
   static_assert(!PAIR || (!F8 && PINGPONG && KCH == kPairKch), "pair path: BF16 ping-pong, the pair pack's chunks");
   using L = Layout<TSMEM, F8>;
@@ -522,9 +531,9 @@ __global__ void __launch_bounds__(kThreads, 1)
   }
   if (threadIdx.x == 0) {
     for (int s = 0; s < NST; ++s) {
-      // pair: the even CTA's stage completes on its own copy and the odd
-      // CTA's relayed arrival
-      mbar_init(sbase + kBarFull + 8 * s, PAIR && crank == 0 ? 2 : 1);
+      // pair: the even CTA's stage completes on its producer's arrival and
+      // the bytes of both CTAs' copies (the odd CTA's signal it directly)
+      mbar_init(sbase + kBarFull + 8 * s, 1);
       mbar_init(sbase + kBarEmpty + 8 * s, 1);
     }
     for (int s = 0; s < 2; ++s) {
@@ -574,7 +583,9 @@ __global__ void __launch_bounds__(kThreads, 1)
       // One thread issues the loads in ring order (stage q % NST): a stage
       // frees once per chunk of MMAs, and the copies of one thread complete
       // at a few hundred cycles' spacing, so one thread keeps pace without
-      // lanes of one warp spinning on different barriers.
+      // lanes of one warp spinning on different barriers. Each CTA copies
+      // its N-half with a 2-SM tensor copy that completes on the even CTA's
+      // full barrier, whose producer expects both halves' bytes.
       if (lane == 0) {
         uint32_t used = 0;  // bit st: parity of the copies issued into stage st
         int st = 0;
@@ -589,15 +600,18 @@ __global__ void __launch_bounds__(kThreads, 1)
           if (!(nq++ == withhold && crank == 0)) {
             uint32_t bytes;
             const uint8_t *src = chunk_src(g, c, bytes);
-            mbar_expect_tx(sbase + kBarFull + 8 * st, bytes);
-            bulk_g2s(sbase + kRingOff + st * kStageBytes, src, bytes, sbase + kBarFull + 8 * st);
+            const uint32_t full = sbase + kBarFull + 8 * st;
+            if (crank == 0) mbar_expect_tx(full, 2 * bytes);
+            tma_2d_pair(sbase + kRingOff + st * kStageBytes, &maps.map[pair_map_of(bytes)], 0,
+                        (int)((src - packed - kBf16PairOff) >> 8), crank == 0 ? full : peer_addr(full, 0));
           }
           used ^= 1u << st;
           if (++st == NST) st = 0;
           return true;
         });
-        if (!ok) {
-          // Drain: wait (bounded) for the copies still in flight.
+        if (!ok && crank == 0) {
+          // Drain: wait (bounded) for the stages' last copies (both CTAs';
+          // the odd CTA's own drain is at the kernel's end).
           const uint64_t t0 = globaltimer();
           for (int k = 0; k < NST; ++k)
             while (!mbar_try(sbase + kBarFull + 8 * k, ((used >> k) & 1u) ^ 1u) && globaltimer() - t0 < 10000000ull) {
@@ -644,24 +658,10 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
     }
-  } else if (PAIR && warp == 1 && crank == 1) {
-    // ---------------- relay (odd CTA of a pair) ----------------
-    // In ring order: once this CTA's half of a chunk has landed, arrive on
-    // the even CTA's full barrier of that stage (its MMAs read both halves).
-    if (lane == 0) {
-      uint32_t used = 0;
-      int st = 0;
-      for_each_load<KCH, NST, PINGPONG, PAIR>(t_first, t_step, ntiles, [&](int, int) {
-        if (!wait_bar(sbase + kBarFull + 8 * st, (used >> st) & 1u, abort_flag, err)) return false;
-        mbar_arrive_remote(peer_addr(sbase + kBarFull + 8 * st, 0));
-        used ^= 1u << st;
-        if (++st == NST) st = 0;
-        return true;
-      });
-    }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
-    // pair: the even CTA issues for both (the odd CTA's warp 1 relays).
+    // pair: the even CTA issues for both (the odd CTA's warp 1 only holds
+    // the TMEM allocation).
     const bool issued_any = t_first < ntiles;
     if (lane == 0 && crank == 0) {
       if (PAIR) {
@@ -1114,8 +1114,20 @@ __global__ void __launch_bounds__(kThreads, 1)
     if (crank == 1 && warp == 1 && lane == 0 && t_first < ntiles) {
       // the even CTA's last commit (after every MMA on this CTA's data) has
       // reached this CTA
-      const uint64_t t0 = globaltimer();
+      uint64_t t0 = globaltimer();
       while (!mbar_try(sbase + kBarDrain, 0) && globaltimer() - t0 < 100000000ull) {
+      }
+      // Without a timeout every copy of this CTA was waited for by the even
+      // CTA's issuer. After one (in either CTA) copies may still be in
+      // flight, and they complete on the even CTA's barriers, which this CTA
+      // cannot wait on: give them 100 us (copies from L2 take microseconds).
+      uint32_t peer_abort;
+      asm volatile("ld.shared::cluster.u32 %0, [%1];" : "=r"(peer_abort) : "r"(peer_addr(sbase + kAbort, 0))
+                   : "memory");
+      if (*abort_flag || peer_abort) {
+        t0 = globaltimer();
+        while (globaltimer() - t0 < 100000ull) {
+        }
       }
     }
     __syncwarp();
@@ -1133,6 +1145,47 @@ __global__ void __launch_bounds__(kThreads, 1)
 }
 
 }  // namespace tc
+
+// cuTensorMapEncodeTiled, looked up once through the runtime (the library
+// does not link the driver library).
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+  });
+  return fn;
+}
+
+// The pair pack's weights (kBf16WBytes from kBf16PairOff) as a 2-D tensor of
+// 256-byte rows (128 16-bit elements), boxes of 64, 32 and 16 rows: every
+// weight half of the pair layout starts on a row (its byte offset is a
+// multiple of 256) and is one such box.
+static int pair_maps(const uint8_t *packed, tc::PairMaps &m) {
+  const EncodeTiledFn enc = encode_tiled();
+  if (!enc) return NERFGB_E_CUDA;
+  static_assert(kBf16PairOff % 1024 == 0 && kBf16WBytes % 256 == 0, "pair pack rows");
+  if (reinterpret_cast<uintptr_t>(packed) % 256 != 0) return NERFGB_E_INVALID_ARG;
+  const cuuint64_t dims[2] = {128, (cuuint64_t)(kBf16WBytes / 256)};
+  const cuuint64_t strides[1] = {256};
+  const cuuint32_t estr[2] = {1, 1};
+  const cuuint32_t rows[3] = {64, 32, 16};
+  for (int i = 0; i < 3; ++i) {
+    const cuuint32_t box[2] = {128, rows[i]};
+    if (enc(&m.map[i], CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<uint8_t *>(packed + kBf16PairOff), dims,
+            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+      return NERFGB_E_CUDA;
+  }
+  return NERFGB_OK;
+}
 
 template <int KCH, int NST, bool PP, bool TSMEM, bool F8, bool STORE = false, bool PAIR = false>
 static int launch_variant(const void *packed, const float *xyz, const float *dirs, long long n, int rpd,
@@ -1183,15 +1236,19 @@ static int launch_variant(const void *packed, const float *xyz, const float *dir
     if (max_pairs < 1) return NERFGB_E_UNSUPPORTED;
     const long long pairs = ntiles < max_pairs ? (ntiles > 0 ? ntiles : 1) : max_pairs;
     cfg.gridDim = dim3((unsigned)(2 * pairs));
-    if (cudaLaunchKernelEx(&cfg, kern, pk, xyz, dirs, n, rpd, rgb, sigma, err_word, rm, tape, wait_ns, withhold) !=
-        cudaSuccess)
+    tc::PairMaps maps;
+    int rc = pair_maps(pk, maps);
+    if (rc != NERFGB_OK) return rc;
+    if (cudaLaunchKernelEx(&cfg, kern, pk, xyz, dirs, n, rpd, rgb, sigma, err_word, rm, tape, wait_ns, withhold,
+                           maps) != cudaSuccess)
       return NERFGB_E_CUDA;
     return launch_status();
   } else {
     const long long ntiles = (n + tc::kRows - 1) / tc::kRows;
     const int grid = (int)(ntiles < sms ? ntiles : sms);
+    tc::PairMaps none{};  // the single-CTA kernels copy with cp.async.bulk
     kern<<<grid, tc::kThreads, smem, stream>>>(pk, xyz, dirs, n, rpd, rgb, sigma, err_word, rm, tape, wait_ns,
-                                               withhold);
+                                               withhold, none);
     return launch_status();
   }
 }

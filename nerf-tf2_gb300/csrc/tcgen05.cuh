@@ -85,6 +85,18 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void *src, uint32_t
                "l"(src), "r"(bytes), "r"(bar)
                : "memory");
 }
+// 2-D tensor copy (TMA) of one box into this CTA's shared memory at dst,
+// completing on the mbarrier at cluster address bar: with .cta_group::2 the
+// barrier may be the pair's other CTA's (the one that issues the 2-SM MMAs
+// reading this data). map: the generic address of a CUtensorMap kernel
+// parameter; (x, y) the box's first element.
+__device__ __forceinline__ void tma_2d_pair(uint32_t dst, const void *map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.cta_group::2.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+      "[%4];" ::"r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
 __device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
