@@ -1253,20 +1253,25 @@ static int launch_variant(const void *packed, const float *xyz, const float *dir
   }
 }
 
+// Ring stages of the pair kernel: kPairKch-K chunks (one N-half each per CTA),
+// a whole 256-K layer. Eight stages of 32-K chunks ran 1.21 ms against 0.91
+// on the 786,432-row fine pass: per-chunk barrier and copy overheads.
+constexpr int kPairNst = 4;
+
 int launch_mlp_bf16(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
                     float *sigma, int *err_word, cudaStream_t stream, const RowMap &rm) {
   // Cluster pairs with 2-SM MMAs: ping-pong, 64-K chunks, each CTA's ring 4
   // stages of 16 KB N-halves (a whole 256-K layer), bias/head table read
   // through L1.
-  return launch_variant<64, 4, true, false, false, false, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word,
-                                                                stream, rm);
+  return launch_variant<kPairKch, kPairNst, true, false, false, false, true>(packed, xyz, dirs, n, rpd, rgb, sigma,
+                                                                            err_word, stream, rm);
 }
 
 int launch_mlp_bf16_train(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
                           float *sigma, uint16_t *tape, int *err_word, cudaStream_t stream) {
   // The inference kernel plus the tape stores (the same outputs bit for bit).
-  return launch_variant<64, 4, true, false, false, true, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word,
-                                                               stream, RowMap(), tape);
+  return launch_variant<kPairKch, kPairNst, true, false, false, true, true>(packed, xyz, dirs, n, rpd, rgb, sigma,
+                                                                           err_word, stream, RowMap(), tape);
 }
 
 int launch_mlp_fp8(const void *packed, const float *xyz, const float *dirs, long long n, int rpd, float *rgb,
@@ -1284,8 +1289,9 @@ int launch_mlp_wait_test(const void *packed, bool fp8, const float *xyz, const f
   if (fp8)
     return launch_variant<64, 7, true, true, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word, stream,
                                                    RowMap(), nullptr, wait_ns, withhold);
-  return launch_variant<64, 4, true, false, false, false, true>(packed, xyz, dirs, n, rpd, rgb, sigma, err_word,
-                                                                stream, RowMap(), nullptr, wait_ns, withhold);
+  return launch_variant<kPairKch, kPairNst, true, false, false, false, true>(packed, xyz, dirs, n, rpd, rgb, sigma,
+                                                                            err_word, stream, RowMap(), nullptr,
+                                                                            wait_ns, withhold);
 }
 
 }  // namespace nerfgb
