@@ -107,31 +107,50 @@ __global__ void __launch_bounds__(32 * kCbWarps)
 
 // MSE (keras.losses.MeanSquaredError, model.py:32,157-168): loss += scale *
 // mean((p - y)^2); grad = scale * 2 (p - y) / n.
-__global__ void mse_kernel(const float *__restrict__ pred, const float *__restrict__ target, long long n,
-                           float scale, float *__restrict__ loss, float *__restrict__ grad) {
+// The loss kernels run as one block of kLossThreads so that the loss is
+// reproducible bit for bit: each thread sums a fixed stride of the elements
+// in order, warps reduce by a fixed shuffle tree, and thread 0 adds the
+// warps' sums in order to *loss (one add).
+constexpr int kLossThreads = 1024;
+
+__device__ __forceinline__ float block_sum_ordered(float part) {
+  __shared__ float warp_sums[kLossThreads / 32];
+  for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
+  if ((threadIdx.x & 31) == 0) warp_sums[threadIdx.x >> 5] = part;
+  __syncthreads();
+  float total = 0.0f;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += warp_sums[w];
+  return total;  // thread 0
+}
+
+__global__ void __launch_bounds__(kLossThreads)
+    mse_kernel(const float *__restrict__ pred, const float *__restrict__ target, long long n, float scale,
+               float *__restrict__ loss, float *__restrict__ grad) {
   float part = 0.0f;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
     const float d = pred[i] - target[i];
     part += d * d;
     if (grad) grad[i] = scale * 2.0f * d / (float)n;
   }
-  for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-  if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, scale * part / (float)n);
+  const float total = block_sum_ordered(part);
+  if (threadIdx.x == 0 && loss) *loss += scale * total / (float)n;
 }
 
 // Envelope loss of the proposal sampler on weight histograms [R,S]:
 // sum (1 + lam [w_p < w_t]) (w_p - w_t)^2 / R.
-__global__ void envelope_loss_kernel(const float *__restrict__ wp, const float *__restrict__ wt, long long n,
-                                     int R, float lam, float *__restrict__ loss, float *__restrict__ grad) {
+__global__ void __launch_bounds__(kLossThreads)
+    envelope_loss_kernel(const float *__restrict__ wp, const float *__restrict__ wt, long long n, int R, float lam,
+                         float *__restrict__ loss, float *__restrict__ grad) {
   float part = 0.0f;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+  for (long long i = threadIdx.x; i < n; i += blockDim.x) {
     const float d = wp[i] - wt[i];
     const float rho = d < 0.0f ? 1.0f + lam : 1.0f;
     part += rho * d * d;
     grad[i] = 2.0f * rho * d / (float)R;
   }
-  for (int off = 16; off > 0; off >>= 1) part += __shfl_xor_sync(0xffffffffu, part, off);
-  if ((threadIdx.x & 31) == 0 && loss) atomicAdd(loss, part / (float)R);
+  const float total = block_sum_ordered(part);
+  if (threadIdx.x == 0 && loss) *loss += total / (float)R;
 }
 
 // TensorFlow ApplyAdam (Keras Adam, model.py:418): m += (g - m)(1 - b1);
@@ -194,7 +213,7 @@ extern "C" int nerfgb_mse_loss(const float *pred, const float *target, long long
   if (n < 0) return NERFGB_E_INVALID_ARG;
   if (n == 0) return NERFGB_OK;
   if (!pred || !target || (!loss && !grad)) return NERFGB_E_INVALID_ARG;
-  mse_kernel<<<grid_cap(n, 256), 256, 0, as_stream(stream)>>>(pred, target, n, scale, loss, grad);
+  mse_kernel<<<1, kLossThreads, 0, as_stream(stream)>>>(pred, target, n, scale, loss, grad);
   return launch_status();
 }
 
@@ -204,8 +223,7 @@ extern "C" int nerfgb_envelope_loss(const float *w_prop, const float *w_target, 
   if (n_rays == 0) return NERFGB_OK;
   if (!w_prop || !w_target || !grad) return NERFGB_E_INVALID_ARG;
   long long n = (long long)n_rays * n_bins;
-  envelope_loss_kernel<<<grid_cap(n, 256), 256, 0, as_stream(stream)>>>(w_prop, w_target, n, n_rays, lam, loss,
-                                                                          grad);
+  envelope_loss_kernel<<<1, kLossThreads, 0, as_stream(stream)>>>(w_prop, w_target, n, n_rays, lam, loss, grad);
   return launch_status();
 }
 
