@@ -68,8 +68,8 @@ def parse():
                     help="1: the gate also skips fine draws in coarse bins the proposal calls empty")
     ap.add_argument("--proposal-steps", type=int, default=2000)
     ap.add_argument("--train-steps", type=int, default=3)
-    ap.add_argument("--train-tile", type=int, default=4096,
-                    help="rays per recompute tile of the training backward (0: keep the forward's tape)")
+    ap.add_argument("--train-tile", type=int, default=1024,
+                    help="rays per recompute tile of the training backward's tiled line (0: keep the forward's tape)")
     ap.add_argument("--sweep", type=int, default=1, help="1: FP32/BF16/FP8 sweep at 65536 rays x 256")
     ap.add_argument("--glorot-scene", type=int, default=1,
                     help="1: the gated path also on a plain Glorot-initialised scene with its own proposal")
@@ -643,14 +643,15 @@ def main():
         batch = [torch.from_numpy(x[:4096]).to(dev) for x in ng.synthetic.training_rays(500 + rank, 4, 1024)]
         target = plain.render(*batch, seed=3)["rgb"]
         train = {"batch_rays": 4096, "master_weights": "fp32",
-                 "backward": "autograd.RenderFunction: tape recomputed per tile of train_tile rays "
-                             "(*_stored_tape: the forward's tape kept instead)", "train_tile": args.train_tile}
-        for tp, tile in (("bf16", args.train_tile or None), ("bf16", None), ("fp32", args.train_tile or None)):
+                 "backward": "autograd.RenderFunction with tiles of 4096 rays (one tile: its tape is kept from "
+                             "the forward); *_recompute: tiles of train_tile rays, each tile's tape recomputed "
+                             "in backward", "train_tile": args.train_tile}
+        for tp, tile in (("bf16", 4096), ("bf16", args.train_tile or None), ("fp32", 4096)):
             student = ng.NeRF(params, precision=tp, seed=60)
             tms = timed_steps(lambda i: student.train_step((tuple(batch), (target,)), tile_rays=tile),
                               args.train_steps, 1)
             student.coarse_model.check_device_errors()
-            key = tp if tile is not None else tp + "_stored_tape"
+            key = tp if tile == 4096 else tp + "_recompute"
             train[key] = {"rays_per_s": 4096 / (tms / 1000.0), "ms_per_step": tms,
                           "gemms": "BF16 tcgen05 GEMMs forward and backward, FP32 accumulation"
                           if tp == "bf16" else "FP32 SIMT"}

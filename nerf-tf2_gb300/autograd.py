@@ -14,7 +14,9 @@ two networks' flat parameter blobs. Two ways to keep what backward needs:
   backward, accumulating the parameter gradients. The tape never holds more
   than one tile (T x (Nc + Nc + Nf) rows).
 * ``tile_rays=None`` (stored tape): forward runs the taped passes over all
-  rays once and backward uses that tape; faster, R rows of tape.
+  rays once and backward uses that tape; faster, R rows of tape. A tile that
+  covers every ray (tile_rays >= R) is the same single tile, so forward keeps
+  its tape then too rather than rendering twice.
 
 The fine samples' positions do not carry gradient into the coarse network
 (ray_utils.py:377 stop_gradient), so each network's gradient comes from its
@@ -73,7 +75,10 @@ class RenderFunction(torch.autograd.Function):
 
     @staticmethod
     def forward(ctx, params_c, params_f, nerf, rays_o, rays_d, near, far, u_c, u_f, tp, tile_rays):
-        ctx.nerf, ctx.tp, ctx.tile_rays, ctx.R = nerf, tp, tile_rays, rays_o.shape[0]
+        R = rays_o.shape[0]
+        if tile_rays is not None and int(tile_rays) >= R:
+            tile_rays = None  # one tile: its tape is the forward's
+        ctx.nerf, ctx.tp, ctx.tile_rays, ctx.R = nerf, tp, tile_rays, R
         if tile_rays is None:
             passes = _taped_passes(nerf, rays_o, rays_d, near, far, u_c, u_f, tp)
             ctx.passes = passes

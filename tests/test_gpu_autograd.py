@@ -94,3 +94,26 @@ def test_only_fine_loss_leaves_coarse_gradient_zero(ng, cuda):
     nerf.coarse_model.check_device_errors()
     assert float(nerf.coarse_model.params.grad.abs().max()) == 0.0
     assert float(nerf.fine_model.params.grad.abs().max()) > 0.0
+
+
+def test_single_tile_keeps_forward_tape(ng, cuda):
+    """A tile covering every ray is one tile: the forward keeps its tape (no
+    second render); maps as the stored tape's bit for bit, gradients up to the
+    FP32 order of the backward's atomic row reductions (bias and head sums)."""
+    (o, d, n, f), uc, uf, target = _case(ng, R=40, seed=13)
+    p = ng.make_params()
+    bc, bf = biased_blob(ng, 21), biased_blob(ng, 22)
+    res = []
+    for tile in (None, 40, 4096):
+        nerf = ng.NeRF(p, precision="bf16", coarse_params=bc, fine_params=bf)
+        rgb_c, rgb_f = ng.autograd.render_with_grad(nerf, dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc),
+                                                    u_fine=dev(uf), tile_rays=tile)
+        (ng.autograd.mse(rgb_c, dev(target)) + ng.autograd.mse(rgb_f, dev(target))).backward()
+        nerf.coarse_model.check_device_errors()
+        assert "tape" in nerf._train_state()  # the forward's tape was kept
+        res.append((host(nerf.coarse_model.params.grad), host(nerf.fine_model.params.grad), host(rgb_c),
+                    host(rgb_f)))
+    for r in res[1:]:
+        assert np.array_equal(r[2], res[0][2]) and np.array_equal(r[3], res[0][3])
+        for ga, gb in ((res[0][0], r[0]), (res[0][1], r[1])):
+            np.testing.assert_allclose(gb, ga, rtol=1e-4, atol=1e-6 * np.abs(ga).max())
