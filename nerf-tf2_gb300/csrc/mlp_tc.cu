@@ -798,7 +798,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                   *reinterpret_cast<float4 *>(b + i) = *reinterpret_cast<const float4 *>(bias + col0 + i);
                 tmem_wait32(raw);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(raw[i]) + b[i];
+                for (int i = 0; i < 32; i += 2)
+                  add_f32x2(v[i], v[i + 1], __uint_as_float(raw[i]), __uint_as_float(raw[i + 1]), b[i], b[i + 1]);
               }
               if (g == 7) {
 #pragma unroll

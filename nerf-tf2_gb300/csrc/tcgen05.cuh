@@ -175,6 +175,15 @@ __device__ __forceinline__ void tmem_wait32(uint32_t (&r)[32]) {
                : "memory");
 }
 
+// (x0 + y0, x1 + y1) in one paired FP32 add (round to nearest even, as two
+// FADDs).
+__device__ __forceinline__ void add_f32x2(float &d0, float &d1, float x0, float x1, float y0, float y1) {
+  asm("{\n.reg .b64 a, b, d;\nmov.b64 a, {%2, %3};\nmov.b64 b, {%4, %5};\nadd.rn.f32x2 d, a, b;\n"
+      "mov.b64 {%0, %1}, d;\n}"
+      : "=f"(d0), "=f"(d1)
+      : "f"(x0), "f"(x1), "f"(y0), "f"(y1));
+}
+
 // Shared-memory matrix descriptor: K-major, no swizzle (layout type 0),
 // descriptor version 1 at bit 46. lbo = byte stride between core matrices
 // adjacent in K, sbo = byte stride between 8-row groups.
