@@ -786,10 +786,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int i = 0; i < 32; i += 4) {
                   const float4 b4 = *reinterpret_cast<const float4 *>(bias + col0 + i);
                   const float4 s4 = *reinterpret_cast<const float4 *>(scales + bias_offset(g) + col0 + i);
-                  v[i] = fmaf(__uint_as_float(raw[i]), s4.x, b4.x);
-                  v[i + 1] = fmaf(__uint_as_float(raw[i + 1]), s4.y, b4.y);
-                  v[i + 2] = fmaf(__uint_as_float(raw[i + 2]), s4.z, b4.z);
-                  v[i + 3] = fmaf(__uint_as_float(raw[i + 3]), s4.w, b4.w);
+                  fma_f32x2(v[i], v[i + 1], __uint_as_float(raw[i]), __uint_as_float(raw[i + 1]), s4.x, s4.y, b4.x,
+                            b4.y);
+                  fma_f32x2(v[i + 2], v[i + 3], __uint_as_float(raw[i + 2]), __uint_as_float(raw[i + 3]), s4.z, s4.w,
+                            b4.z, b4.w);
                 }
               } else {
                 float b[32];
@@ -986,10 +986,10 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int i = 0; i < 32; i += 4) {
                   const float4 b4 = *reinterpret_cast<const float4 *>(bias + col0 + i);
                   const float4 s4 = *reinterpret_cast<const float4 *>(scales + bias_offset(g) + col0 + i);
-                  v[i] = fmaf(__uint_as_float(raw[i]), s4.x, b4.x);
-                  v[i + 1] = fmaf(__uint_as_float(raw[i + 1]), s4.y, b4.y);
-                  v[i + 2] = fmaf(__uint_as_float(raw[i + 2]), s4.z, b4.z);
-                  v[i + 3] = fmaf(__uint_as_float(raw[i + 3]), s4.w, b4.w);
+                  fma_f32x2(v[i], v[i + 1], __uint_as_float(raw[i]), __uint_as_float(raw[i + 1]), s4.x, s4.y, b4.x,
+                            b4.y);
+                  fma_f32x2(v[i + 2], v[i + 3], __uint_as_float(raw[i + 2]), __uint_as_float(raw[i + 3]), s4.z, s4.w,
+                            b4.z, b4.w);
                 }
               } else {
                 float b[32];
@@ -997,7 +997,8 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int i = 0; i < 32; i += 4) *reinterpret_cast<float4 *>(b + i) = *reinterpret_cast<const float4 *>(bias + col0 + i);
                 tmem_wait32(raw);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) v[i] = __uint_as_float(raw[i]) + b[i];
+                for (int i = 0; i < 32; i += 2)
+                  add_f32x2(v[i], v[i + 1], __uint_as_float(raw[i]), __uint_as_float(raw[i + 1]), b[i], b[i + 1]);
               }
               if (g == 7) {
 #pragma unroll

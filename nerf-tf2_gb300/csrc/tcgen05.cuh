@@ -184,6 +184,16 @@ __device__ __forceinline__ void add_f32x2(float &d0, float &d1, float x0, float 
       : "f"(x0), "f"(x1), "f"(y0), "f"(y1));
 }
 
+// (x0 * y0 + z0, x1 * y1 + z1) in one paired FP32 FMA (each rounded once,
+// as fmaf).
+__device__ __forceinline__ void fma_f32x2(float &d0, float &d1, float x0, float x1, float y0, float y1, float z0,
+                                          float z1) {
+  asm("{\n.reg .b64 a, b, c, d;\nmov.b64 a, {%2, %3};\nmov.b64 b, {%4, %5};\nmov.b64 c, {%6, %7};\n"
+      "fma.rn.f32x2 d, a, b, c;\nmov.b64 {%0, %1}, d;\n}"
+      : "=f"(d0), "=f"(d1)
+      : "f"(x0), "f"(x1), "f"(y0), "f"(y1), "f"(z0), "f"(z1));
+}
+
 // Shared-memory matrix descriptor: K-major, no swizzle (layout type 0),
 // descriptor version 1 at bit 46. lbo = byte stride between core matrices
 // adjacent in K, sbo = byte stride between 8-row groups.
