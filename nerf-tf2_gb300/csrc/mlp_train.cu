@@ -32,110 +32,144 @@ __device__ __forceinline__ float4 tape4(const uint16_t *p) {
                      __uint_as_float(u.y & 0xffff0000u));
 }
 
+// Eight tape values as FP32 (16-byte BF16 load, or two of FP32).
+__device__ __forceinline__ void tape8(const float *p, float (&v)[8]) {
+  const float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void tape8(const uint16_t *p, float (&v)[8]) {
+  const uint4 u = *reinterpret_cast<const uint4 *>(p);
+  const uint32_t w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    v[2 * i] = __uint_as_float(w[i] << 16);
+    v[2 * i + 1] = __uint_as_float(w[i] & 0xffff0000u);
+  }
+}
+
+// One warp per row at a time, kHeadRows rows loaded before any is used:
+// lane l owns h9 columns 4l..4l+3 and h7 columns 8l..8l+7 (coalesced tape
+// loads), the head dot products are lane partials summed by a shuffle
+// butterfly (every lane ends with the sums), dZ9 is written 16 bytes per
+// lane, and the head weights' gradients accumulate in the lanes' registers
+// over all of the warp's rows; they reach the blob once per block (shared
+// atomics, then one global atomic per parameter).
+constexpr int kHeadWarps = 8;
+constexpr int kHeadRows = 2;
+
 template <typename T>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(32 * kHeadWarps, 2)
     head_bwd_kernel(const float *__restrict__ table, const T *__restrict__ acts, long long n,
                     const float *__restrict__ d_rgb, const float *__restrict__ d_sigma, float *__restrict__ dz9,
                     float *__restrict__ dsp_out, float *__restrict__ grads) {
-  extern __shared__ __align__(16) float hsm[];
-  float(*sH9)[128 + 4] = reinterpret_cast<float(*)[128 + 4]>(hsm);
-  float(*sH7)[256 + 4] = reinterpret_cast<float(*)[256 + 4]>(hsm + kTM * (128 + 4));
-  float(*sDRP)[3] = reinterpret_cast<float(*)[3]>(hsm + kTM * (128 + 4) + kTM * (256 + 4));
-  float *sDSP = hsm + kTM * (128 + 4) + kTM * (256 + 4) + kTM * 3;
-  float *sAcc = sDSP + kTM;  // dWr [128][3], dbr [3], dws [256], dbs [1]
-  const int tid = threadIdx.x;
-  for (int e = tid; e < 644; e += 256) sAcc[e] = 0.0f;
-  const float *Wr = table + kRgbWOff, *br = table + kRgbBOff, *ws = table + kSigmaWOff;
-  const long long ntiles = (n + kTM - 1) / kTM;
-  for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const long long row0 = tile * kTM;
-    __syncthreads();
-    for (int e = tid; e < kTM * 32; e += 256) {
-      const int r = e >> 5, q = e & 31;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (row0 + r < n) v = tape4(acts + (row0 + r) * kActsLd + acts_offset(9) + 4 * q);
-      *reinterpret_cast<float4 *>(&sH9[r][4 * q]) = v;
-    }
-    for (int e = tid; e < kTM * 64; e += 256) {
-      const int r = e >> 6, q = e & 63;
-      float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (row0 + r < n) v = tape4(acts + (row0 + r) * kActsLd + acts_offset(7) + 4 * q);
-      *reinterpret_cast<float4 *>(&sH7[r][4 * q]) = v;
-    }
-    __syncthreads();
-    {
-      // head pre-activations: four threads per row, each a quarter of the
-      // dot products (j = part + 4i: conflict-free with the padded rows),
-      // combined by shuffles in the four-lane group
-      const int r = tid >> 2, part = tid & 3;
-      const bool valid = row0 + r < n;
-      float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, sp = 0.0f;
-#pragma unroll 8
-      for (int i = 0; i < 32; ++i) {
-        const int j = part + 4 * i;
-        const float h = sH9[r][j];
-        p0 = fmaf(h, Wr[3 * j], p0);
-        p1 = fmaf(h, Wr[3 * j + 1], p1);
-        p2 = fmaf(h, Wr[3 * j + 2], p2);
+  __shared__ float sAcc[644];  // dWr [128][3], dbr [3], dws [256], dbs [1]
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int e = threadIdx.x; e < 644; e += blockDim.x) sAcc[e] = 0.0f;
+  float wr[4][3], wsg[8];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) wr[j][c] = table[kRgbWOff + (4 * lane + j) * 3 + c];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) wsg[j] = table[kSigmaWOff + 8 * lane + j];
+  const float br[3] = {table[kRgbBOff], table[kRgbBOff + 1], table[kRgbBOff + 2]};
+  const float bs = table[kSigmaBOff];
+  float gwr[4][3], gws[8], gbr[3] = {0.f, 0.f, 0.f}, gbs = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) gwr[j][0] = gwr[j][1] = gwr[j][2] = 0.0f;
+#pragma unroll
+  for (int j = 0; j < 8; ++j) gws[j] = 0.0f;
+  __syncthreads();
+  const long long wstep = (long long)gridDim.x * kHeadWarps * kHeadRows;
+  for (long long r0 = ((long long)blockIdx.x * kHeadWarps + warp) * kHeadRows; r0 < n; r0 += wstep) {
+    float h9[kHeadRows][4], h7[kHeadRows][8], drgb[kHeadRows][3], dsg[kHeadRows];
+#pragma unroll
+    for (int q = 0; q < kHeadRows; ++q) {
+      const long long r = r0 + q;
+      if (r < n) {
+        const float4 a = tape4(acts + r * kActsLd + acts_offset(9) + 4 * lane);
+        h9[q][0] = a.x; h9[q][1] = a.y; h9[q][2] = a.z; h9[q][3] = a.w;
+        tape8(acts + r * kActsLd + acts_offset(7) + 8 * lane, h7[q]);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) drgb[q][c] = d_rgb[r * 3 + c];
+        dsg[q] = d_sigma ? d_sigma[r] : 0.0f;
+      } else {
+#pragma unroll
+        for (int j = 0; j < 4; ++j) h9[q][j] = 0.0f;
+#pragma unroll
+        for (int j = 0; j < 8; ++j) h7[q][j] = 0.0f;
+        drgb[q][0] = drgb[q][1] = drgb[q][2] = dsg[q] = 0.0f;
       }
-#pragma unroll 8
-      for (int i = 0; i < 64; ++i) {
-        const int j = part + 4 * i;
-        sp = fmaf(sH7[r][j], ws[j], sp);
+    }
+#pragma unroll
+    for (int q = 0; q < kHeadRows; ++q) {
+      const long long r = r0 + q;
+      const bool valid = r < n;
+      float p0 = 0.0f, p1 = 0.0f, p2 = 0.0f, sp = 0.0f;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        p0 = fmaf(h9[q][j], wr[j][0], p0);
+        p1 = fmaf(h9[q][j], wr[j][1], p1);
+        p2 = fmaf(h9[q][j], wr[j][2], p2);
       }
 #pragma unroll
-      for (int o = 1; o <= 2; o <<= 1) {
+      for (int j = 0; j < 8; ++j) sp = fmaf(h7[q][j], wsg[j], sp);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
         p0 += __shfl_xor_sync(0xffffffffu, p0, o);
         p1 += __shfl_xor_sync(0xffffffffu, p1, o);
         p2 += __shfl_xor_sync(0xffffffffu, p2, o);
         sp += __shfl_xor_sync(0xffffffffu, sp, o);
       }
-      if (part == 0) {
-        const float pre[3] = {br[0] + p0, br[1] + p1, br[2] + p2};
-        for (int c = 0; c < 3; ++c) {
-          const float y = 1.0f / (1.0f + expf(-pre[c]));
-          sDRP[r][c] = valid ? d_rgb[(row0 + r) * 3 + c] * y * (1.0f - y) : 0.0f;
+      // rgb = sigmoid(h9 Wr + br), sigma = ReLU(h7 ws + bs) (model.py:374-386)
+      const float pre[3] = {br[0] + p0, br[1] + p1, br[2] + p2};
+      float drp[3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const float y = 1.0f / (1.0f + expf(-pre[c]));
+        drp[c] = valid ? drgb[q][c] * y * (1.0f - y) : 0.0f;
+      }
+      const float dsp = (valid && sp + bs > 0.0f) ? dsg[q] : 0.0f;
+      if (valid) {
+        if (lane == 0) dsp_out[r] = dsp;
+        float o[4];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float g = drp[0] * wr[j][0] + drp[1] * wr[j][1] + drp[2] * wr[j][2];
+          o[j] = h9[q][j] > 0.0f ? g : 0.0f;
         }
-        sp += table[kSigmaBOff];
-        const float dsp = (valid && d_sigma && sp > 0.0f) ? d_sigma[row0 + r] : 0.0f;
-        sDSP[r] = dsp;
-        if (valid) dsp_out[row0 + r] = dsp;
+        *reinterpret_cast<float4 *>(dz9 + r * kDzLd + 4 * lane) = make_float4(o[0], o[1], o[2], o[3]);
       }
-    }
-    __syncthreads();
-    for (int e = tid; e < kTM * 128; e += 256) {
-      const int r = e >> 7, j = e & 127;
-      if (row0 + r < n) {
-        const float g = sDRP[r][0] * Wr[3 * j] + sDRP[r][1] * Wr[3 * j + 1] + sDRP[r][2] * Wr[3 * j + 2];
-        dz9[(row0 + r) * kDzLd + j] = sH9[r][j] > 0.0f ? g : 0.0f;
-      }
-    }
-    for (int e = tid; e < 644; e += 256) {
-      float a = 0.0f;
-      if (e < 384) {
-        const int j = e / 3, c = e - 3 * j;
-        for (int r = 0; r < kTM; ++r) a = fmaf(sH9[r][j], sDRP[r][c], a);
-      } else if (e < 387) {
-        for (int r = 0; r < kTM; ++r) a += sDRP[r][e - 384];
-      } else if (e < 643) {
-        const int j = e - 387;
-        for (int r = 0; r < kTM; ++r) a = fmaf(sH7[r][j], sDSP[r], a);
-      } else {
-        for (int r = 0; r < kTM; ++r) a += sDSP[r];
-      }
-      sAcc[e] += a;
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) gwr[j][c] = fmaf(h9[q][j], drp[c], gwr[j][c]);
+#pragma unroll
+      for (int j = 0; j < 8; ++j) gws[j] = fmaf(h7[q][j], dsp, gws[j]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) gbr[c] += drp[c];
+      gbs += dsp;
     }
   }
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) atomicAdd(&sAcc[(4 * lane + j) * 3 + c], gwr[j][c]);
+#pragma unroll
+  for (int j = 0; j < 8; ++j) atomicAdd(&sAcc[387 + 8 * lane + j], gws[j]);
+  if (lane == 0) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) atomicAdd(&sAcc[384 + c], gbr[c]);
+    atomicAdd(&sAcc[643], gbs);
+  }
   __syncthreads();
-  float *gWr = grads + flat_offset(11), *gbr = gWr + 128 * 3;
-  float *gws = grads + flat_offset(8), *gbs = gws + 256;
-  for (int e = tid; e < 644; e += 256) {
-    float *dst = e < 384 ? gWr + e : e < 387 ? gbr + (e - 384) : e < 643 ? gws + (e - 387) : gbs;
+  float *gWr = grads + flat_offset(11), *gbr_out = gWr + 128 * 3;
+  float *gws_out = grads + flat_offset(8), *gbs_out = gws_out + 256;
+  for (int e = threadIdx.x; e < 644; e += blockDim.x) {
+    float *dst = e < 384 ? gWr + e : e < 387 ? gbr_out + (e - 384) : e < 643 ? gws_out + (e - 387) : gbs_out;
     atomicAdd(dst, sAcc[e]);
   }
 }
-
-constexpr size_t kHeadSmem = (size_t)(kTM * (128 + 4) + kTM * (256 + 4) + kTM * 3 + kTM + 644) * sizeof(float);
 
 // ---------------------------------------------------------------------------
 // dX: dz_out[m][k] = (sum_n dz_in[m][n] W[k][n] + dsp[m] ws[k]) * mask, k < 256
@@ -304,10 +338,13 @@ template <typename T>
 static int launch_head_bwd_t(const float *table, const T *tape, long long n, const float *d_rgb,
                              const float *d_sigma, float *dz9, float *dsp, float *grads, cudaStream_t st) {
   using namespace train;
-  if (cudaFuncSetAttribute(head_bwd_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kHeadSmem) !=
-      cudaSuccess)
-    return NERFGB_E_CUDA;
-  head_bwd_kernel<T><<<persistent_grid(n), 256, kHeadSmem, st>>>(table, tape, n, d_rgb, d_sigma, dz9, dsp, grads);
+  if (n == 0) return NERFGB_OK;
+  const long long rows_per_block = (long long)kHeadWarps * kHeadRows;
+  const long long blocks = (n + rows_per_block - 1) / rows_per_block;
+  const int sms = num_sms();
+  const long long cap = (long long)(sms > 0 ? sms : 148) * 2;  // two blocks per SM (launch bounds)
+  head_bwd_kernel<T><<<(unsigned)(blocks < cap ? blocks : cap), 32 * kHeadWarps, 0, st>>>(table, tape, n, d_rgb,
+                                                                                        d_sigma, dz9, dsp, grads);
   return launch_status();
 }
 
