@@ -333,15 +333,25 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
 }
 
 // grads[r][c] += sum_s part[s][r][c] for r < rows, c < cols (part row stride
-// ld, split stride split_rows * ld); grads row stride gld.
-__global__ void reduce_splits_kernel(const float *__restrict__ part, int splits, long long split_rows, int ld,
-                                     int rows, int cols, float *__restrict__ grads, int gld) {
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= (long long)rows * cols) return;
-  const int r = (int)(e / cols), c = (int)(e % cols);
+// ld, split stride split_rows * ld); grads row stride gld. A block takes 64
+// elements; its four warp pairs sum the splits s = g, g + 4, ... (g = the
+// pair) in order, and the four sums are added in order: the same result
+// whatever the launch.
+constexpr int kRedElems = 64, kRedGroups = 4;
+__global__ void __launch_bounds__(kRedElems *kRedGroups)
+    reduce_splits_kernel(const float *__restrict__ part, int splits, long long split_rows, int ld, int rows, int cols,
+                         float *__restrict__ grads, int gld) {
+  __shared__ float sums[kRedGroups][kRedElems];
+  const int t = threadIdx.x % kRedElems, grp = threadIdx.x / kRedElems;
+  const long long e = (long long)blockIdx.x * kRedElems + t;
+  const bool ok = e < (long long)rows * cols;
+  const int r = ok ? (int)(e / cols) : 0, c = ok ? (int)(e % cols) : 0;
   float s = 0.0f;
-  for (int k = 0; k < splits; ++k) s += part[(k * split_rows + r) * ld + c];
-  grads[(long long)r * gld + c] += s;
+  if (ok)
+    for (int k = grp; k < splits; k += kRedGroups) s += part[(k * split_rows + r) * ld + c];
+  sums[grp][t] = s;
+  __syncthreads();
+  if (grp == 0 && ok) grads[(long long)r * gld + c] += ((sums[0][t] + sums[1][t]) + sums[2][t]) + sums[3][t];
 }
 
 template <bool A_MN, bool B_MN, int MT, int EPI, bool B_RES = false>
@@ -414,8 +424,9 @@ int launch_gemm_dw(const __nv_bfloat16 *in, long long ld_in, int k_in, const __n
                              : gemm::launch<true, true, 2, gemm::kEpiF32>(a, st);
   if (rc != NERFGB_OK) return rc;
   const long long n = (long long)k_in * n_out;
-  gemm::reduce_splits_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(part, a.k_splits, a.M, 256, k_in, n_out,
-                                                                           grads, n_out);
+  gemm::reduce_splits_kernel<<<(unsigned)((n + gemm::kRedElems - 1) / gemm::kRedElems),
+                               gemm::kRedElems * gemm::kRedGroups, 0, st>>>(part, a.k_splits, a.M, 256, k_in, n_out,
+                                                                            grads, n_out);
   return launch_status();
 }
 

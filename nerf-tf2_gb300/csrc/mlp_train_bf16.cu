@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(256)
     w[i] = SIG ? ws[c0 + i] : 0.0f;
     sum[i] = 0.0f;
   }
-#pragma unroll 2
+#pragma unroll 4
   for (long long m = m0 + rsub; m < m1; m += rpp) {
     float z[8];
     load8(raw + m * kDzLd + c0, z);
