@@ -60,6 +60,7 @@ def parse():
                     help="mlp: the MLP kernel alone at the fine-pass launch shape; train: training steps; "
                          "chain: the gated render of --chunks 4096-ray chunks (for ncu captures)")
     ap.add_argument("--chunks", type=int, default=4)
+    ap.add_argument("--batch", type=int, default=4096, help="rays per training step of --kernel train")
     ap.add_argument("--rows", type=int, default=CHUNK * (SC + SF))
     ap.add_argument("--proposal", type=int, default=1, help="1: BF16 + learned proposal (headline)")
     ap.add_argument("--proposal-mode", default="gate", choices=["gate", "replace"])
@@ -111,7 +112,8 @@ def train_only(args):
     params = ng.make_params(N_coarse=SC, N_fine=SF)
     blob = ng.synthetic.sparse_scene_blob(SCENE_SEED, max_freq_log2=SCENE_MAX_FREQ_LOG2)
     teacher = ng.NeRF(params, precision="fp32", coarse_params=blob, fine_params=blob)
-    batch = [torch.from_numpy(x[:4096]).to(dev) for x in ng.synthetic.training_rays(500, 4, 1024)]
+    batch = [torch.from_numpy(x[:args.batch]).to(dev)
+             for x in ng.synthetic.training_rays(500, 4, (args.batch + 3) // 4)]
     target = teacher.render(*batch, seed=3)["rgb"]
     student = ng.NeRF(params, precision=args.path, seed=60)
     tile = args.train_tile or None
@@ -126,7 +128,7 @@ def train_only(args):
         torch.cuda.synchronize()
         ts.append(e0.elapsed_time(e1))
     student.coarse_model.check_device_errors()
-    print(json.dumps({"kernel": f"train_{args.path}", "batch_rays": 4096, "tile_rays": tile,
+    print(json.dumps({"kernel": f"train_{args.path}", "batch_rays": args.batch, "tile_rays": tile,
                       "step_ms": statistics.median(ts)}), flush=True)
 
 

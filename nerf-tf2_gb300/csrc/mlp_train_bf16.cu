@@ -21,7 +21,7 @@ namespace train16 {
 
 constexpr int kDzLd = 256;                    // row stride of the dZ buffers
 constexpr int kMaxSplits = 160;               // row splits of a dW GEMM (partial sums in the workspace)
-constexpr int kPrepRows = 1024;               // rows per prep block
+constexpr int kPrepBlocksPerSm = 4;          // persistent prep grid (resident at 54 registers)
 
 __global__ void to_bf16_kernel(const float *__restrict__ src, __nv_bfloat16 *__restrict__ dst, long long n) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
@@ -30,9 +30,10 @@ __global__ void to_bf16_kernel(const float *__restrict__ src, __nv_bfloat16 *__r
 
 // z = raw (+ dsp * ws) (* [tape act > 0]) over N columns (N = 128 or 256);
 // dz = bf16(z); db[n] += sum_m z. Eight columns per thread (16-byte loads
-// and stores), N / 8 threads per row, 256 threads per block over kPrepRows
-// rows; the column sums are reduced in shared memory, one atomic per column
-// per block.
+// and stores), N / 8 threads per row; the blocks stride over the rows (a
+// persistent grid of several blocks per SM, for the loads in flight), each
+// thread keeping its columns' sums in registers over all of its rows; the
+// sums are reduced in shared memory, one atomic per column per block.
 __device__ __forceinline__ void load8(const float *p, float (&v)[8]) {
   const float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 4);
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
@@ -56,8 +57,7 @@ __global__ void __launch_bounds__(256)
   const int tpr = N / 8;                    // threads per row
   const int rpp = 256 / tpr;                // rows per pass
   const int t = threadIdx.x, c0 = (t % tpr) * 8, rsub = t / tpr;
-  const long long m0 = (long long)blockIdx.x * kPrepRows;
-  const long long m1 = m0 + kPrepRows < M ? m0 + kPrepRows : M;
+  const long long mstep = (long long)gridDim.x * rpp;
   float w[8], sum[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(256)
     sum[i] = 0.0f;
   }
 #pragma unroll 4
-  for (long long m = m0 + rsub; m < m1; m += rpp) {
+  for (long long m = (long long)blockIdx.x * rpp + rsub; m < M; m += mstep) {
     float z[8];
     load8(raw + m * kDzLd + c0, z);
     if (SIG) {
@@ -134,8 +134,12 @@ static Ws carve(void *base, long long n) {
 template <bool MASK, bool SIG, typename Tin>
 static int prep(const Tin *raw, long long M, int N, const uint16_t *tape, int act_off, const float *dsp,
                 const float *ws, __nv_bfloat16 *dz, float *db, cudaStream_t st) {
-  const long long blocks = (M + kPrepRows - 1) / kPrepRows;
-  prep_kernel<Tin, MASK, SIG><<<(unsigned)blocks, 256, 0, st>>>(raw, M, N, tape, act_off, dsp, ws, dz, db);
+  const long long rpp = 256 / (N / 8);  // rows per block pass
+  const long long passes = (M + rpp - 1) / rpp;
+  const int sms = num_sms();
+  const long long cap = (long long)(sms > 0 ? sms : 148) * kPrepBlocksPerSm;
+  prep_kernel<Tin, MASK, SIG><<<(unsigned)(passes < cap ? passes : cap), 256, 0, st>>>(raw, M, N, tape, act_off, dsp,
+                                                                                     ws, dz, db);
   return launch_status();
 }
 
