@@ -4,10 +4,13 @@
 //
 //   C[M][N] = sum_k A[m][k] B[n][k]        (tcgen05.mma.cta_group::1.kind::f16)
 //
-// Operands are read from row-major global memory with 16-byte cp.async
-// copies into the no-swizzle core-matrix layout (8 rows x 16 bytes). The same
-// bytes serve both operand orientations: a row-major [rows][cols] tile copied
-// as "element (r, c) at (c/8)*S + r*16 + (c%8)*2" is
+// Operands stream from row-major global memory by tensor copies (TMA) into
+// the no-swizzle core-matrix layout (8 rows x 16 bytes): a 3-D tensor map
+// (8 elements, rows, 8-element column groups; strides 2, the row stride, 16
+// bytes) makes one box land as "element (r, c) at (c/8)*S + r*16 + (c%8)*2"
+// with S = 16 * box rows, rows and groups past the bounds zero-filled. The
+// same bytes serve both operand orientations: that image of a row-major
+// [rows][cols] tile is
 //   K-major  when the reduction runs along cols (descriptor LBO = S, the
 //            stride between 8-column groups; SBO = 128, between 8-row groups),
 //   MN-major when the reduction runs along rows (LBO = 128, between 8-row
@@ -22,8 +25,9 @@
 //                 reduction kernel adds the splits into the gradient blob.
 //
 // Warp roles (9 warps): 0-3 epilogue (TMEM lane quadrant = warp), 4-7
-// loaders (cp.async into an NST-stage ring, full/empty mbarriers), 8 TMEM
-// allocation and the MMA issuer (one thread). Work items (an M tile, a split
+// loaders (warp 4's first lane issues the tensor copies of an NST-stage
+// ring, full/empty mbarriers; all four warps copy a resident B once with
+// cp.async), 8 TMEM allocation and the MMA issuer (one thread). Work items (an M tile, a split
 // of K) are taken persistently: item = blockIdx.x + i * gridDim.x. With one
 // 128-row M tile per item the accumulator is double-buffered in TMEM, so an
 // item's epilogue overlaps the next item's MMAs.
@@ -49,10 +53,14 @@ constexpr int kLoadWarps = 4;
 constexpr int kLoadThreads = kLoadWarps * 32;
 constexpr int kIssuerWarp = kEpiWarps + kLoadWarps;
 constexpr int kThreads = (kIssuerWarp + 1) * 32;  // 288
-constexpr int kLag = 2;                    // loader stages in flight before it signals the oldest
 constexpr uint32_t kPad = 16;              // bytes added to a group stride (bank spread of the copies)
 
 enum Epi { kEpiBf16 = 0, kEpiF32 = 1 };
+
+// Tensor maps of the streamed operands (A, and B unless resident).
+struct Maps {
+  CUtensorMap a, b;
+};
 
 struct Args {
   const __nv_bfloat16 *A;  // K-major: [M][K] row stride lda; MN-major: [K][M] row stride lda
@@ -73,8 +81,10 @@ struct Args {
 template <bool A_MN, bool B_MN, int MT, bool B_RES = false>
 struct Geo {
   // group strides (bytes) of the copied images
-  static constexpr uint32_t kSA = A_MN ? kKc * 16 + kPad : MT * 128 * 16 + kPad;  // A: per 8 M-cols / 8 K-cols
-  static constexpr uint32_t kSB = B_MN ? kKc * 16 + kPad : 256 * 16 + kPad;
+  // group strides of the tensor-copied images (A; B streamed MN-major), and
+  // of the resident B copied by cp.async (padded for the copies' banks)
+  static constexpr uint32_t kSA = A_MN ? kKc * 16 : MT * 128 * 16;  // A: per 8 M-cols / 8 K-cols
+  static constexpr uint32_t kSB = B_MN ? kKc * 16 : 256 * 16 + kPad;
   static constexpr uint32_t kABytes = A_MN ? (MT * 128 / 8) * kSA : (kKc / 8) * kSA;
   static constexpr uint32_t kBBytes = B_RES ? 0 : B_MN ? (256 / 8) * kSB : (kKc / 8) * kSB;
   static constexpr uint32_t kStage = (kABytes + kBBytes + 127) / 128 * 128;
@@ -105,35 +115,18 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
-// Copies the [rows x 64] (K-major) or [64 x cols] (MN-major) piece of one
-// operand into a stage image. K-major: piece (r, kg) = X[r][k0 + 8kg ..]
-// -> kg*S + r*16. MN-major: piece (kr, g) = X[k0 + kr][c0 + 8g ..] -> g*S +
-// kr*16. Rows/columns past the bounds are zero-filled.
-template <bool MN, int ROWS>
-__device__ __forceinline__ void load_operand(uint32_t dst, const __nv_bfloat16 *X, long long ld, long long r0,
-                                             long long r_end, long long k0, long long k_end, uint32_t S, int t) {
-  constexpr int kPieces = ROWS * 8;  // 16-byte pieces per stage image
-#pragma unroll 4
-  for (int p = t; p < kPieces; p += kLoadThreads) {
-    if (!MN) {
-      const int r = p >> 3, kg = p & 7;
-      const long long gr = r0 + r, gk = k0 + 8 * kg;
-      const bool ok = gr < r_end && gk < k_end;
-      const __nv_bfloat16 *src = ok ? X + gr * ld + gk : X;
-      cp_async16(dst + (uint32_t)kg * S + (uint32_t)r * 16u, src, ok ? 16u : 0u);
-    } else {
-      constexpr int G = ROWS / 8;  // 8-element groups across the M (or N) extent
-      const int g = p % G, kr = p / G;
-      const long long gk = k0 + kr, gc = r0 + 8 * g;
-      const bool ok = gk < k_end && gc < r_end;
-      const __nv_bfloat16 *src = ok ? X + gk * ld + gc : X;
-      cp_async16(dst + (uint32_t)g * S + (uint32_t)kr * 16u, src, ok ? 16u : 0u);
-    }
-  }
+// One box of a 3-D tensor map into shared memory at dst, completing on the
+// mbarrier bar (coordinates innermost first).
+__device__ __forceinline__ void tma_3d(uint32_t dst, const CUtensorMap *map, int c0, int c1, int c2, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];" ::
+          "r"(dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(bar)
+      : "memory");
 }
 
 template <bool A_MN, bool B_MN, int MT, int EPI, bool B_RES = false>
-__global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
+__global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_constant__ Maps maps) {
   using G = Geo<A_MN, B_MN, MT, B_RES>;
   extern __shared__ __align__(1024) uint8_t smem[];
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
@@ -153,7 +146,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < G::kNst; ++s) {
-      mbar_init(sbase + G::kBarFull + 8 * s, kLoadThreads);
+      mbar_init(sbase + G::kBarFull + 8 * s, 1);  // the copying thread's arrive, then the bytes
       mbar_init(sbase + G::kBarEmpty + 8 * s, 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -193,36 +186,44 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a) {
       fence_proxy_async();
       mbar_arrive(sbase + G::kBarB);
     }
-    long long q = 0, q_sig = 0;  // chunks issued, chunks signalled full
-    bool ok = true;
-    for (long long it = blockIdx.x; it < items && ok; it += gridDim.x) {
-      long long mt, kb, ke;
-      item_range(it, mt, kb, ke);
-      const long long m0 = mt * MT * 128;
-      for (long long k0 = kb; k0 < ke; k0 += kKc, ++q) {
-        const int st = (int)(q % G::kNst);
-        const uint32_t ph = (uint32_t)((q / G::kNst) & 1);
-        if (!wait_bar(sbase + G::kBarEmpty + 8 * st, ph ^ 1u, abort_flag, a.err)) {
-          ok = false;
-          break;
-        }
-        const uint32_t sa = sbase + st * G::kStage, sb = sa + G::kABytes;
-        load_operand<A_MN, MT * 128>(sa, a.A, a.lda, m0, a.M, k0, ke, G::kSA, t);
-        if (!B_RES) load_operand<B_MN, 256>(sb, a.B, a.ldb, 0, a.N, k0, ke, G::kSB, t);
-        cp_async_commit();
-        if (q - q_sig >= kLag) {
-          // the oldest pending stage has landed (this thread's copies): publish it
-          cp_async_wait<kLag>();
-          fence_proxy_async();
-          mbar_arrive(sbase + G::kBarFull + 8 * (int)(q_sig % G::kNst));
-          ++q_sig;
+    if (t == 0) {
+      // One thread issues each stage's tensor copies: A (MT*128 rows or
+      // kKc rows of MN-major groups) and a streamed B; the stage completes
+      // on their bytes.
+      constexpr uint32_t kBytes = G::kABytes + G::kBBytes;
+      long long q = 0;
+      bool ok = true;
+      for (long long it = blockIdx.x; it < items && ok; it += gridDim.x) {
+        long long mt, kb, ke;
+        item_range(it, mt, kb, ke);
+        const int m0 = (int)(mt * MT * 128);
+        for (long long k0 = kb; k0 < ke; k0 += kKc, ++q) {
+          const int st = (int)(q % G::kNst);
+          const uint32_t ph = (uint32_t)((q / G::kNst) & 1);
+          if (!wait_bar(sbase + G::kBarEmpty + 8 * st, ph ^ 1u, abort_flag, a.err)) {
+            ok = false;
+            break;
+          }
+          const uint32_t full = sbase + G::kBarFull + 8 * st, sa = sbase + st * G::kStage;
+          mbar_expect_tx(full, kBytes);
+          // MN-major: rows = the reduction (k0 ..), groups = M columns (m0 / 8 ..);
+          // K-major: rows = M (m0 ..), groups = the reduction columns (k0 / 8 ..)
+          if (A_MN)
+            tma_3d(sa, &maps.a, 0, (int)k0, m0 / 8, full);
+          else
+            tma_3d(sa, &maps.a, 0, m0, (int)(k0 / 8), full);
+          if (!B_RES) tma_3d(sa + G::kABytes, &maps.b, 0, (int)k0, 0, full);
         }
       }
+      if (!ok) {
+        // Drain: wait (bounded) for the copies of the stages still in flight.
+        const uint64_t t0 = globaltimer();
+        for (long long d = q > G::kNst ? q - G::kNst : 0; d < q; ++d)
+          while (!mbar_try(sbase + G::kBarFull + 8 * (int)(d % G::kNst), (uint32_t)((d / G::kNst) & 1)) &&
+                 globaltimer() - t0 < 10000000ull) {
+          }
+      }
     }
-    cp_async_wait<0>();
-    fence_proxy_async();
-    if (ok)
-      for (; q_sig < q; ++q_sig) mbar_arrive(sbase + G::kBarFull + 8 * (int)(q_sig % G::kNst));
   } else if (warp == kIssuerWarp) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
@@ -354,6 +355,19 @@ __global__ void __launch_bounds__(kRedElems *kRedGroups)
   if (grp == 0 && ok) grads[(long long)r * gld + c] += ((sums[0][t] + sums[1][t]) + sums[2][t]) + sums[3][t];
 }
 
+// A row-major BF16 matrix [rows][groups * 8] (row stride ld elements) as the
+// 3-D tensor (8 elements, rows, 8-element groups) whose box {8, box_rows,
+// box_groups} lands as the core-matrix image "(r, c) at (c/8)*(16*box_rows)
+// + r*16 + (c%8)*2"; groups past `groups` read as zeros.
+static int operand_map(CUtensorMap *m, const __nv_bfloat16 *X, long long ld, long long rows, long long groups,
+                       unsigned box_rows, unsigned box_groups) {
+  if (reinterpret_cast<uintptr_t>(X) % 16 != 0 || (ld * 2) % 16 != 0) return NERFGB_E_INVALID_ARG;
+  const unsigned long long dims[3] = {8, (unsigned long long)rows, (unsigned long long)groups};
+  const unsigned long long strides[2] = {(unsigned long long)(ld * 2), 16};
+  const unsigned box[3] = {8, box_rows, box_groups};
+  return encode_tensor_map_u16(m, X, 3, dims, strides, box);
+}
+
 template <bool A_MN, bool B_MN, int MT, int EPI, bool B_RES = false>
 static int launch(const Args &a, cudaStream_t st) {
   using G = Geo<A_MN, B_MN, MT, B_RES>;
@@ -365,7 +379,21 @@ static int launch(const Args &a, cudaStream_t st) {
   const long long items = (long long)a.m_tiles * a.k_splits;
   if (items == 0) return NERFGB_OK;
   const int grid = (int)(items < sms ? items : sms);
-  kern<<<grid, kThreads, G::kSmem, st>>>(a);
+  Maps maps{};
+  int rc;
+  // A: MN-major [K rows][M cols] in kKc-row boxes of all MT*128 columns;
+  // K-major [M rows][K cols] in 128-row boxes of kKc columns
+  if (A_MN)
+    rc = operand_map(&maps.a, a.A, a.lda, a.K, a.M / 8, kKc, MT * 128 / 8);
+  else
+    rc = operand_map(&maps.a, a.A, a.lda, a.M, a.K / 8, MT * 128, kKc / 8);
+  if (rc != NERFGB_OK) return rc;
+  if (!B_RES) {
+    static_assert(B_RES || B_MN, "a streamed B is MN-major");
+    // [K rows][N cols] in kKc-row boxes of 256 columns (past N: zeros)
+    if ((rc = operand_map(&maps.b, a.B, a.ldb, a.K, a.N / 8, kKc, 256 / 8)) != NERFGB_OK) return rc;
+  }
+  kern<<<grid, kThreads, G::kSmem, st>>>(a, maps);
   return launch_status();
 }
 

@@ -1,5 +1,6 @@
 // Launchers shared between the MLP translation units.
 #pragma once
+#include <cuda.h>  // CUtensorMap (the encoder is reached through the runtime's entry-point query)
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -17,6 +18,12 @@ struct RowMap {
   const int *map = nullptr;
   const int *n_dev = nullptr;
 };
+
+// A tensor map of 16-bit elements over `base` (mlp_tc.cu): rank dims
+// (innermost first), the byte strides of dims 1.. (multiples of 16), box
+// sizes; no interleave or swizzle, zero fill outside the dims.
+int encode_tensor_map_u16(CUtensorMap *map, const void *base, int rank, const unsigned long long *dims,
+                          const unsigned long long *strides, const unsigned *box);
 
 // FP32 SIMT forward (mlp.cu).
 int launch_mlp_fp32(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,

@@ -1166,25 +1166,39 @@ static EncodeTiledFn encode_tiled() {
   return fn;
 }
 
+int encode_tensor_map_u16(CUtensorMap *map, const void *base, int rank, const unsigned long long *dims,
+                          const unsigned long long *strides, const unsigned *box) {
+  const EncodeTiledFn enc = encode_tiled();
+  if (!enc || rank < 1 || rank > 5) return NERFGB_E_CUDA;
+  cuuint64_t d[5], st[4];
+  cuuint32_t b[5], e[5];
+  for (int i = 0; i < rank; ++i) {
+    d[i] = dims[i];
+    b[i] = box[i];
+    e[i] = 1;
+    if (i > 0) st[i - 1] = strides[i - 1];
+  }
+  return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, (cuuint32_t)rank, const_cast<void *>(base), d, st, b, e,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
+             ? NERFGB_OK
+             : NERFGB_E_CUDA;
+}
+
 // The pair pack's weights (kBf16WBytes from kBf16PairOff) as a 2-D tensor of
 // 256-byte rows (128 16-bit elements), boxes of 64, 32 and 16 rows: every
 // weight half of the pair layout starts on a row (its byte offset is a
 // multiple of 256) and is one such box.
 static int pair_maps(const uint8_t *packed, tc::PairMaps &m) {
-  const EncodeTiledFn enc = encode_tiled();
-  if (!enc) return NERFGB_E_CUDA;
   static_assert(kBf16PairOff % 1024 == 0 && kBf16WBytes % 256 == 0, "pair pack rows");
   if (reinterpret_cast<uintptr_t>(packed) % 256 != 0) return NERFGB_E_INVALID_ARG;
-  const cuuint64_t dims[2] = {128, (cuuint64_t)(kBf16WBytes / 256)};
-  const cuuint64_t strides[1] = {256};
-  const cuuint32_t estr[2] = {1, 1};
-  const cuuint32_t rows[3] = {64, 32, 16};
+  const unsigned long long dims[2] = {128, (unsigned long long)(kBf16WBytes / 256)};
+  const unsigned long long strides[1] = {256};
+  const unsigned rows[3] = {64, 32, 16};
   for (int i = 0; i < 3; ++i) {
-    const cuuint32_t box[2] = {128, rows[i]};
-    if (enc(&m.map[i], CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<uint8_t *>(packed + kBf16PairOff), dims,
-            strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
-      return NERFGB_E_CUDA;
+    const unsigned box[2] = {128, rows[i]};
+    const int rc = encode_tensor_map_u16(&m.map[i], packed + kBf16PairOff, 2, dims, strides, box);
+    if (rc != NERFGB_OK) return rc;
   }
   return NERFGB_OK;
 }
