@@ -159,10 +159,30 @@ __device__ __forceinline__ void stage_weights_bf16(const float *__restrict__ par
   if (threadIdx.x == 0) sp.B3 = params[kB3];
 }
 
+// Octaves l0 .. l1-1 of coordinate c of the encoding (sin, cos of
+// x * 2^l pi) from one sincosf at octave l0: the angle doubles exactly from
+// one octave to the next, and sin 2a = (2 sin a) cos a, cos 2a = cos a cos a
+// - sin a sin a, each operation rounded in FP32 (no FMA). Five doublings put
+// an absolute error of a few 1e-6 on a value that is then rounded to BF16.
+__device__ __forceinline__ void encode_octaves_bf16(__nv_bfloat16 *er, float xc, int c, int l0, int l1) {
+  float sn, cs;
+  sincosf(fmul(xc, enc_multiplier(l0)), &sn, &cs);
+  for (int l = l0; l < l1; ++l) {
+    if (l > l0) {
+      const float s2 = fmul(fmul(2.0f, sn), cs);
+      cs = fsub(fmul(cs, cs), fmul(sn, sn));
+      sn = s2;
+    }
+    er[3 + c * 12 + 2 * l] = __float2bfloat16_rn(sn);
+    er[3 + c * 12 + 2 * l + 1] = __float2bfloat16_rn(cs);
+  }
+}
+
 // One 16-row tile's encodings (BF16) into the warp's buffer: two lanes per
-// row (row = lane / 2), each computing nine of the row's eighteen sin/cos
-// pairs (angles a = h, h + 2, ..., a = 6c + l) plus the three coordinates
-// (h = 0) or the zero padding (h = 1). x: the lane's row's point.
+// row (row = lane / 2). Lane h = 0 writes the three coordinates, coordinate
+// 0's six octaves and coordinate 2's octaves 0-2; lane h = 1 the zero
+// padding, coordinate 1's octaves and coordinate 2's octaves 3-5 (two
+// sincosf per lane, encode_octaves_bf16). x: the lane's row's point.
 __device__ __forceinline__ void encode_row_bf16(__nv_bfloat16 *enc, int lane, const float (&x)[3]) {
   const int row = lane >> 1, h = lane & 1;
   __nv_bfloat16 *er = enc + row * kEncLdB;
@@ -170,17 +190,13 @@ __device__ __forceinline__ void encode_row_bf16(__nv_bfloat16 *enc, int lane, co
     er[0] = __float2bfloat16_rn(x[0]);
     er[1] = __float2bfloat16_rn(x[1]);
     er[2] = __float2bfloat16_rn(x[2]);
+    encode_octaves_bf16(er, x[0], 0, 0, 6);
+    encode_octaves_bf16(er, x[2], 2, 0, 3);
   } else {
 #pragma unroll
     for (int k = kIn; k < kK1; ++k) er[k] = __float2bfloat16_rn(0.0f);
-  }
-#pragma unroll
-  for (int a = h; a < 18; a += 2) {
-    const int c = a / 6, l = a % 6;
-    float sn, cs;
-    sincosf(fmul(x[c], enc_multiplier(l)), &sn, &cs);
-    er[3 + c * 12 + 2 * l] = __float2bfloat16_rn(sn);
-    er[3 + c * 12 + 2 * l + 1] = __float2bfloat16_rn(cs);
+    encode_octaves_bf16(er, x[1], 1, 0, 6);
+    encode_octaves_bf16(er, x[2], 2, 3, 6);
   }
 }
 

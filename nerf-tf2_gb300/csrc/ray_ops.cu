@@ -133,6 +133,73 @@ __device__ __forceinline__ bool sort_before(float a, int ia, float b, int ib) {
   return a < b || (a == b && ia < ib);
 }
 
+// Bitonic sort of P = 32 E (key, index) pairs held E per lane (element i =
+// lane E + e), ascending by key, ties by index (keys not NaN): the
+// compare-exchange of elements i and i ^ j runs in registers for j < E and
+// through shuffles (lane ^ j / E) otherwise. Both sides of a pair compute
+// the same min and max, each keeping its own.
+__device__ __forceinline__ bool key_before(float a, int ia, float b, int ib) { return a < b || (a == b && ia < ib); }
+template <int E>
+__device__ __forceinline__ void warp_bitonic_sort(float (&key)[E], int (&idx)[E], int lane) {
+  constexpr int P = 32 * E;
+#pragma unroll
+  for (int k = 2; k <= P; k <<= 1) {
+#pragma unroll
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      if (j >= E) {
+        const int m = j / E;
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          const int i = lane * E + e;
+          const float pk = __shfl_xor_sync(0xffffffffu, key[e], m);
+          const int pi = __shfl_xor_sync(0xffffffffu, idx[e], m);
+          const bool take_min = ((i & j) == 0) == ((i & k) == 0);
+          const bool other_first = key_before(pk, pi, key[e], idx[e]);
+          if (other_first == take_min) {
+            key[e] = pk;
+            idx[e] = pi;
+          }
+        }
+      } else {
+#pragma unroll
+        for (int e = 0; e < E; ++e) {
+          if (e & j) continue;  // e is the pair's lower element, e + j the upper
+          const int i = lane * E + e;
+          const bool asc = (i & k) == 0;
+          if (key_before(key[e + j], idx[e + j], key[e], idx[e]) == asc) {
+            const float tk = key[e];
+            const int ti = idx[e];
+            key[e] = key[e + j];
+            idx[e] = idx[e + j];
+            key[e + j] = tk;
+            idx[e + j] = ti;
+          }
+        }
+      }
+    }
+  }
+}
+
+// The fine draws (s_t[Sc .. Sc + Sf)) padded to P = 32 E with (+inf, index
+// >= Sf), sorted by warp_bitonic_sort into s_fk (keys) and s_fi (indices).
+template <int E>
+__device__ __forceinline__ void sort_fine_draws(const float *s_t, int Sc, int Sf, float *s_fk, int *s_fi, int lane) {
+  float key[E];
+  int idx[E];
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    const int i = lane * E + e;
+    key[e] = i < Sf ? s_t[Sc + i] : INFINITY;
+    idx[e] = i;
+  }
+  warp_bitonic_sort<E>(key, idx, lane);
+#pragma unroll
+  for (int e = 0; e < E; ++e) {
+    s_fk[lane * E + e] = key[e];
+    s_fi[lane * E + e] = idx[e];
+  }
+}
+
 // Shared-memory words per warp of fine_sample_kernel: w, pdf, left edges,
 // widths (4 Sc), the CDF (Sc + 1), concat and sorted t (2 S), the bitonic
 // keys and indices (2 P), the permutation (S), rgb_c (3 Sc), the draws'
@@ -142,7 +209,7 @@ __host__ __device__ __forceinline__ int fine_smem_floats(int Sc, int Sf, int P) 
   return 4 * Sc + (Sc + 1) + 2 * S + 2 * P + S + 3 * Sc + Sf;
 }
 
-__global__ void __launch_bounds__(32 * kFineWarps)
+__global__ void __launch_bounds__(32 * kFineWarps, 8)
     fine_sample_kernel(const float *__restrict__ rays_o, const float *__restrict__ rays_d,
                        const float *__restrict__ bin_weights, const float *__restrict__ left_edges,
                        int ld_left, const float *__restrict__ bin_widths,
@@ -258,29 +325,41 @@ __global__ void __launch_bounds__(32 * kFineWarps)
       fast = __all_sync(0xffffffffu, ok);
     }
     if (fast) {
-      // Bitonic sort of (t_f[k], k), padded to P with (+inf, k >= Sf).
-      for (int k = lane; k < P; k += 32) {
-        s_fk[k] = k < Sf ? s_t[Sc + k] : INFINITY;
-        s_fi[k] = k;
-      }
-      __syncwarp();
-      for (int size = 2; size <= P; size <<= 1) {
-        for (int stride = size >> 1; stride > 0; stride >>= 1) {
-          for (int q = lane; q < P / 2; q += 32) {
-            const int lo = 2 * stride * (q / stride) + (q % stride), hi = lo + stride;
-            const float a = s_fk[lo], b = s_fk[hi];
-            const int ia = s_fi[lo], ib = s_fi[hi];
-            const bool b_first = b < a || (b == a && ib < ia);
-            if (b_first == ((lo & size) == 0)) {  // ascending block: b first -> swap; descending: a first -> swap
-              s_fk[lo] = b;
-              s_fk[hi] = a;
-              s_fi[lo] = ib;
-              s_fi[hi] = ia;
+      // Bitonic sort of (t_f[k], k), padded to P with (+inf, k >= Sf): in
+      // registers and shuffles up to P = 128, through shared memory above
+      // (the same network; more keys per lane would cost the kernel's
+      // occupancy in registers).
+      if (P == 32) {
+        sort_fine_draws<1>(s_t, Sc, Sf, s_fk, s_fi, lane);
+      } else if (P == 64) {
+        sort_fine_draws<2>(s_t, Sc, Sf, s_fk, s_fi, lane);
+      } else if (P == 128) {
+        sort_fine_draws<4>(s_t, Sc, Sf, s_fk, s_fi, lane);
+      } else {
+        for (int k = lane; k < P; k += 32) {
+          s_fk[k] = k < Sf ? s_t[Sc + k] : INFINITY;
+          s_fi[k] = k;
+        }
+        __syncwarp();
+        for (int size = 2; size <= P; size <<= 1) {
+          for (int stride = size >> 1; stride > 0; stride >>= 1) {
+            for (int q = lane; q < P / 2; q += 32) {
+              const int lo = 2 * stride * (q / stride) + (q % stride), hi = lo + stride;
+              const float a = s_fk[lo], b = s_fk[hi];
+              const int ia = s_fi[lo], ib = s_fi[hi];
+              // ascending block: b first -> swap; descending: a first -> swap
+              if (key_before(b, ib, a, ia) == ((lo & size) == 0)) {
+                s_fk[lo] = b;
+                s_fk[hi] = a;
+                s_fi[lo] = ib;
+                s_fi[hi] = ia;
+              }
             }
+            __syncwarp();
           }
-          __syncwarp();
         }
       }
+      __syncwarp();
       // t_c[i] lands after the fine draws strictly below it; the j-th
       // sorted draw after the coarse samples at or below it.
       for (int i = lane; i < Sc; i += 32) {

@@ -769,11 +769,34 @@ def mlp_forward_lowp(p, xyz, dirs, fmt):
     return rgb.astype(F32), sigma.astype(F32)
 
 
+def proposal_encoding_kernel(xyz):
+    """The L=6 encoding as the proposal's tensor-core kernels compute it
+    (nerf-tf2_gb300/csrc/proposal.cu, encode_octaves_bf16): per coordinate
+    chain, sin/cos at the first octave of the chain, then each next octave
+    by sin 2a = (2 sin a) cos a, cos 2a = cos a cos a - sin a sin a in float32
+    (rounded per operation); chains: coordinates 0 and 1 over octaves 0-5,
+    coordinate 2 over 0-2 and over 3-5."""
+    x = np.asarray(xyz, F32)
+    out = np.zeros((x.shape[0], 39), F32)
+    out[:, :3] = x
+    mult = encoder_multipliers(6, F32)
+    for c, l0, l1 in ((0, 0, 6), (1, 0, 6), (2, 0, 3), (2, 3, 6)):
+        th = (x[:, c] * mult[l0]).astype(F32)
+        s, co = np.sin(th).astype(F32), np.cos(th).astype(F32)
+        for l in range(l0, l1):
+            if l > l0:
+                s, co = (F32(2) * s) * co, co * co - s * s
+            out[:, 3 + c * 12 + 2 * l] = s
+            out[:, 4 + c * 12 + 2 * l] = co
+    return out
+
+
 def prop_forward_bf16(blob, xyz):
     """The proposal network (prop_forward) as its tensor-core kernel computes
-    it: BF16 encoding, W1, h1 and W2, FP32 biases, the last layer in FP32."""
+    it: the kernels' encoding (proposal_encoding_kernel) in BF16, W1, h1 and
+    W2 in BF16, FP32 biases, the last layer in FP32."""
     p = prop_unpack(blob, F32)
-    enc = positional_encoding(xyz, 6, F32)
+    enc = proposal_encoding_kernel(xyz)
     h1 = np.maximum(round_bf16(enc).astype(F64) @ round_bf16(p["W1"]).astype(F64) + p["b1"], 0)
     z2 = round_bf16(h1.astype(F32)).astype(F64) @ round_bf16(p["W2"]).astype(F64) + p["b2"]
     z3 = np.maximum(z2, 0) @ p["W3"].astype(F64) + p["b3"][0]

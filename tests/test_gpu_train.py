@@ -131,7 +131,7 @@ def test_proposal_forward_bf16_vs_oracle(ng, oracle, cuda, n):
     prop = ng.ProposalNetwork(blob)
     sig = host(prop(dev(x), precision="bf16"))[:, 0]
     p = oracle.prop_unpack(blob, F32)
-    enc = oracle.positional_encoding(x, 6, F32)
+    enc = oracle.proposal_encoding_kernel(x)
     h1 = np.maximum(_bf16(enc).astype(F64) @ _bf16(p["W1"]).astype(F64) + p["b1"], 0)
     z2 = _bf16(h1.astype(F32)).astype(F64) @ _bf16(p["W2"]).astype(F64) + p["b2"]
     z3 = np.maximum(z2, 0) @ p["W3"].astype(F64) + p["b3"][0]

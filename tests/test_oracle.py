@@ -361,3 +361,15 @@ def test_low_precision_roundings(oracle):
     vals = np.array([s * m * 2.0 ** e for s in (1, -1) for e in range(-6, 9) for m in np.arange(8, 16) / 8
                      if m * 2.0 ** e <= 448], np.float32)
     assert np.array_equal(oracle.round_e4m3(vals), vals)
+
+
+def test_proposal_encoding_kernel_close_to_exact(oracle):
+    """The proposal kernels' octave-doubling encoding stays within a few 1e-6
+    of sin/cos evaluated at every octave in float32 (the reference encoding's
+    arithmetic), far below the BF16 rounding it then gets; both are ~2.5e-5
+    from float64 at the top octave (the float32 rounding of the angle)."""
+    x = np.random.default_rng(3).uniform(-4, 4, (5000, 3)).astype(np.float32)
+    got = oracle.proposal_encoding_kernel(x)
+    want = oracle.positional_encoding(x, 6, np.float32)
+    assert got.shape == want.shape and np.array_equal(got[:, :3], x)
+    assert np.abs(got - want).max() < 4e-6
