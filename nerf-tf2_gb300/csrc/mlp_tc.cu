@@ -107,6 +107,43 @@ struct Layout {
 // ---------------------------------------------------------------------------
 // Positional encodings written as BF16 A-operand rows.
 // ---------------------------------------------------------------------------
+// The tensor-core kernels' positional encoding (model.py:319-331): octave
+// l of a coordinate from one sincosf at octave 4*floor(l/4) and l % 4 angle
+// doublings (the FP32 angle doubles exactly from one octave to the next;
+// sin 2a = (2 sin a) cos a, cos 2a = cos a cos a - sin a sin a, each
+// operation rounded in FP32): at most three doublings, ~5e-7 from sincosf at
+// every octave, below the BF16 (or E4M3) rounding the value then gets. The
+// value of an octave does not depend on which warp computes it.
+template <int NP, int L, int W, int Q>
+__device__ __forceinline__ void encode_pairs_q(const float (&x)[3], float (&v)[W]) {
+  float sn = 0.0f, cs = 1.0f;
+  int cur_c = -1, cur_l = -1;
+#pragma unroll
+  for (int p = 0; p < NP; ++p) {
+    const int ks = 3 + 2 * p;  // sin at ks, cos at ks + 1
+    if (ks + 1 < W * Q || ks >= W * Q + W) continue;
+    const int c = p / L, l = p % L;
+    if (c != cur_c || (l & 3) == 0 || cur_l != l - 1) {
+      // a chain starts at octave 4*floor(l/4)
+      const int l0 = l & ~3;
+      sincosf(fmul(x[c], enc_multiplier(l0)), &sn, &cs);
+      for (int d = l0; d < l; ++d) {
+        const float s2 = fmul(fmul(2.0f, sn), cs);
+        cs = fsub(fmul(cs, cs), fmul(sn, sn));
+        sn = s2;
+      }
+    } else {
+      const float s2 = fmul(fmul(2.0f, sn), cs);
+      cs = fsub(fmul(cs, cs), fmul(sn, sn));
+      sn = s2;
+    }
+    cur_c = c;
+    cur_l = l;
+    if (ks >= W * Q && ks < W * Q + W) v[ks - W * Q] = sn;
+    if (ks + 1 >= W * Q && ks + 1 < W * Q + W) v[ks + 1 - W * Q] = cs;
+  }
+}
+
 // enc_xyz columns [32*HF, 32*HF + 32) of row r (63 values, column 63 = 0).
 // tape_dst (BF16 path only, may be NULL): the same 32 values to the tape.
 template <int HF, bool F8>
@@ -119,16 +156,7 @@ __device__ __forceinline__ void write_enc_xyz(uint32_t enc, int r, const float (
     v[1] = x[1];
     v[2] = x[2];
   }
-#pragma unroll
-  for (int p = 0; p < 30; ++p) {
-    const int ks = 3 + 2 * p;  // sin at ks, cos at ks + 1
-    if (ks + 1 < 32 * HF || ks >= 32 * HF + 32) continue;
-    const int c = p / 10, l = p % 10;
-    float s, co;
-    sincosf(fmul(x[c], enc_multiplier(l)), &s, &co);
-    if (ks >= 32 * HF && ks < 32 * HF + 32) v[ks - 32 * HF] = s;
-    if (ks + 1 >= 32 * HF && ks + 1 < 32 * HF + 32) v[ks + 1 - 32 * HF] = co;
-  }
+  encode_pairs_q<30, 10, 32, HF>(x, v);
   if (!F8 && tape_dst) {
     uint32_t u[16];
     pack32_bf16(v, u);
@@ -146,14 +174,7 @@ __device__ __forceinline__ void write_enc_dir(uint32_t enc, int r, const float (
   v[0] = d[0];
   v[1] = d[1];
   v[2] = d[2];
-#pragma unroll
-  for (int p = 0; p < 12; ++p) {
-    const int c = p / 4, l = p % 4;
-    float s, co;
-    sincosf(fmul(d[c], enc_multiplier(l)), &s, &co);
-    v[3 + 2 * p] = s;
-    v[4 + 2 * p] = co;
-  }
+  encode_pairs_q<12, 4, 32, 0>(d, v);
   if (!F8 && tape_dst) {
     uint32_t u[16];
     pack32_bf16(v, u);
@@ -203,16 +224,7 @@ __device__ __forceinline__ void write_enc_xyz_q(uint32_t enc, int r, const float
     v[1] = x[1];
     v[2] = x[2];
   }
-#pragma unroll
-  for (int p = 0; p < 30; ++p) {
-    const int ks = 3 + 2 * p;  // sin at ks, cos at ks + 1
-    if (ks + 1 < 16 * Q || ks >= 16 * Q + 16) continue;
-    const int c = p / 10, l = p % 10;
-    float s, co;
-    sincosf(fmul(x[c], enc_multiplier(l)), &s, &co);
-    if (ks >= 16 * Q && ks < 16 * Q + 16) v[ks - 16 * Q] = s;
-    if (ks + 1 >= 16 * Q && ks + 1 < 16 * Q + 16) v[ks + 1 - 16 * Q] = co;
-  }
+  encode_pairs_q<30, 10, 16, Q>(x, v);
   if (!F8 && tape_dst) {
     uint4 *t = reinterpret_cast<uint4 *>(tape_dst);
     t[0] = make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));
@@ -229,16 +241,7 @@ __device__ __forceinline__ void write_enc_dir_q(uint32_t enc, int r, const float
   float v[8];
 #pragma unroll
   for (int i = 0; i < 8; ++i) v[i] = (8 * Q + i < 3) ? d[8 * Q + i] : 0.0f;
-#pragma unroll
-  for (int p = 0; p < 12; ++p) {
-    const int ks = 3 + 2 * p;  // sin at ks, cos at ks + 1
-    if (ks + 1 < 8 * Q || ks >= 8 * Q + 8) continue;
-    const int c = p / 4, l = p % 4;
-    float s, co;
-    sincosf(fmul(d[c], enc_multiplier(l)), &s, &co);
-    if (ks >= 8 * Q && ks < 8 * Q + 8) v[ks - 8 * Q] = s;
-    if (ks + 1 >= 8 * Q && ks + 1 < 8 * Q + 8) v[ks + 1 - 8 * Q] = co;
-  }
+  encode_pairs_q<12, 4, 8, Q>(d, v);
   if (!F8 && tape_dst)
     *reinterpret_cast<uint4 *>(tape_dst) =
         make_uint4(pack_bf16(v[0], v[1]), pack_bf16(v[2], v[3]), pack_bf16(v[4], v[5]), pack_bf16(v[6], v[7]));

@@ -745,13 +745,35 @@ def _gemm_lowp(a_q, W, b, fmt):
     return (acc.astype(F64) * s + b).astype(F32)   # fmaf(acc, s, b): one rounding
 
 
+def positional_encoding_kernel(x, L):
+    """positional_encoding (float32) as the tensor-core MLP kernels compute
+    it (nerf-tf2_gb300/csrc/mlp_tc.cu, encode_pairs_q): octave l from sin/cos
+    at octave 4*floor(l/4) and l % 4 angle doublings, sin 2a = (2 sin a)
+    cos a, cos 2a = cos a cos a - sin a sin a, each operation rounded in
+    float32."""
+    x = np.asarray(x, F32)
+    mult = encoder_multipliers(L, F32)
+    out = np.empty((x.shape[0], 3 + 6 * L), F32)
+    out[:, :3] = x
+    for c in range(3):
+        for l0 in range(0, L, 4):
+            th = (x[:, c] * mult[l0]).astype(F32)
+            s, co = np.sin(th).astype(F32), np.cos(th).astype(F32)
+            for l in range(l0, min(l0 + 4, L)):
+                if l > l0:
+                    s, co = (F32(2) * s) * co, co * co - s * s
+                out[:, 3 + c * 2 * L + 2 * l] = s
+                out[:, 4 + c * 2 * L + 2 * l] = co
+    return out
+
+
 def mlp_forward_lowp(p, xyz, dirs, fmt):
     """get_coarse_or_fine_model's network (model.py:334-394) as the BF16
     (fmt="bf16") or FP8-e4m3 (fmt="fp8") tensor-core kernels compute it.
     p: unpack_params(blob, F32). Returns (rgb [M,3], sigma [M,1]) float32."""
     q = round_bf16 if fmt == "bf16" else round_e4m3
-    enc_xyz = q(positional_encoding(xyz, 10, F32))
-    enc_dir = q(positional_encoding(dirs, 4, F32))
+    enc_xyz = q(positional_encoding_kernel(xyz, 10))
+    enc_dir = q(positional_encoding_kernel(dirs, 4))
     h = enc_xyz
     for i in range(8):
         v = _gemm_lowp(h, *p[f"dense_{i}"], fmt)

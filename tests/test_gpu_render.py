@@ -159,8 +159,12 @@ def test_fused_render_lowp_vs_oracle(ng, oracle, cuda, case1024, precision):
     # Against the emulation the MLPs differ only in FP32 summation order and
     # the BF16/E4M3 roundings it flips (rgb 5e-4 max per sample, see
     # test_mlp_lowp_vs_emulation); the fine sampler then moves draws by the
-    # coarse weights' difference, which the rough density amplifies.
-    tight = {"bf16": 1e-3, "fp8": 5e-3}[precision]
+    # coarse weights' difference, which the rough density amplifies. The
+    # encoding's octaves come from a sincos every fourth octave and up to
+    # three doublings (oracle.positional_encoding_kernel); CUDA's sincosf and
+    # numpy's sin differ by a few ulps there, which the doublings multiply by
+    # up to 8, so a few more BF16 roundings of the encoding flip.
+    tight = {"bf16": 1.5e-3, "fp8": 5e-3}[precision]
     for key, scale in (("rgb", 1.0), ("acc", 1.0), ("depth", 10.0)):
         e = stats[key]
         assert np.quantile(e, 0.96) < tight * scale, (key, np.quantile(e, 0.96))

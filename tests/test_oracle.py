@@ -373,3 +373,15 @@ def test_proposal_encoding_kernel_close_to_exact(oracle):
     want = oracle.positional_encoding(x, 6, np.float32)
     assert got.shape == want.shape and np.array_equal(got[:, :3], x)
     assert np.abs(got - want).max() < 4e-6
+
+
+def test_mlp_encoding_kernel_close_to_float32(oracle):
+    """The tensor-core MLP's encoding (octaves by at most three doublings from
+    every fourth) stays within 1e-6 of the float32 encoding at every octave."""
+    rng = np.random.default_rng(4)
+    for L in (10, 4):
+        x = rng.uniform(-4, 4, (5000, 3)).astype(np.float32)
+        got = oracle.positional_encoding_kernel(x, L)
+        want = oracle.positional_encoding(x, L, np.float32)
+        assert got.shape == want.shape
+        assert np.abs(got - want).max() < 1e-6, (L, float(np.abs(got - want).max()))
