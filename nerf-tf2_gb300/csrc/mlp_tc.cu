@@ -878,6 +878,10 @@ __global__ void __launch_bounds__(kThreads, 1)
               float *part = reinterpret_cast<float *>(smem + kEncOff + s * L::kEncBytes + L::kSigPartOff);
               part[cq * 128 + r] = sig;
               head_arrive(s);
+              // h7 is written: dense_8 may start while the quarter sums meet
+              // (they sit in the enc region's upper half, which nothing
+              // rewrites before the next tile's encoding)
+              operands_ready(s);
               if (cq == 0) {
                 // the head barrier completes twice per tile (sigma, rgb): parity 0, then 1
                 if (!__all_sync(0xffffffffu, wait_bar(bar_head, 0, abort_flag, err))) {
@@ -929,7 +933,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               // the enc region is free (dense_9 done); the rgb partials are
               // read before this warp's arrival lets dense_0 overwrite them
               if (has_next) start_rows(tile + t_step, s);
-            } else {
+            } else if (g != 7) {
               operands_ready(s);
             }
           }
