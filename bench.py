@@ -65,6 +65,8 @@ def parse():
     ap.add_argument("--proposal", type=int, default=1, help="1: BF16 + learned proposal (headline)")
     ap.add_argument("--proposal-mode", default="gate", choices=["gate", "replace"])
     ap.add_argument("--gate-tau", type=float, default=1e-4)
+    ap.add_argument("--streams", type=int, default=2,
+                    help="streams the render's chunks alternate over (NeRF.render(streams=))")
     ap.add_argument("--gate-fine-draws", type=int, default=1,
                     help="1: the gate also skips fine draws in coarse bins the proposal calls empty")
     ap.add_argument("--proposal-steps", type=int, default=2000)
@@ -150,7 +152,8 @@ def chain_only(args):
     for i in range(args.warmup + args.steps):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        nerf.render(*rays, chunk=CHUNK, seed=i, proposal=prop, proposal_mode="gate", gate_tau=args.gate_tau,
+        nerf.render(*rays, chunk=CHUNK, streams=args.streams,
+                    seed=i, proposal=prop, proposal_mode="gate", gate_tau=args.gate_tau,
                     gate_fine_draws=bool(args.gate_fine_draws))
         e1.record()
         torch.cuda.synchronize()
@@ -434,7 +437,7 @@ def main():
 
     # headline: device-resident frame through the fast path
     def step(i):
-        fast.render(*rays, chunk=CHUNK, seed=1000 * i, **prop_kw)
+        fast.render(*rays, chunk=CHUNK, streams=args.streams, seed=1000 * i, **prop_kw)
     bus = getattr(torch.cuda.get_device_properties(dev), "pci_bus_id", None)
     with ClockSampler(str(bus) if bus is not None else None) as clk:
         ms = timed_steps(step, args.steps, args.warmup)
@@ -445,7 +448,7 @@ def main():
 
     def e2e_step(i):
         dr = [h.to(dev, non_blocking=True) for h in host]
-        out = fast.render(*dr, chunk=CHUNK, seed=1000 * i, **prop_kw)
+        out = fast.render(*dr, chunk=CHUNK, streams=args.streams, seed=1000 * i, **prop_kw)
         for k in out_host:
             out_host[k].copy_(out[k], non_blocking=True)
     e2e_ms = timed_steps(e2e_step, max(2, args.steps // 2), 1)
@@ -453,11 +456,14 @@ def main():
     d2h = sum(v.numel() * v.element_size() for v in out_host.values())
 
     # the plain paths: FP32 coarse+fine (the denominator) and BF16 coarse+fine
-    plain_ms = timed_steps(lambda i: plain.render(*rays, chunk=CHUNK, seed=1000 * i), args.plain_steps, 1)
-    bf16_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, seed=1000 * i), args.plain_steps, 1) \
+    plain_ms = timed_steps(lambda i: plain.render(*rays, chunk=CHUNK, streams=args.streams,
+                                                  seed=1000 * i), args.plain_steps, 1)
+    bf16_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, streams=args.streams,
+                                                seed=1000 * i), args.plain_steps, 1) \
         if proposal is not None else ms
     other_mode = "replace" if args.proposal_mode == "gate" else "gate"
-    other_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, seed=1000 * i, proposal=proposal,
+    other_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, streams=args.streams,
+                                                 seed=1000 * i, proposal=proposal,
                                                  proposal_mode=other_mode, gate_tau=args.gate_tau),
                            args.plain_steps, 1) if proposal is not None else None
 
@@ -466,13 +472,13 @@ def main():
     rows = torch.arange(0, H, 4, device=dev)
     sub = (rows[:, None] * W + torch.arange(W, device=dev)[None, :]).reshape(-1)
     sr = [x[sub] for x in rays]
-    img_plain = plain.render(*sr, chunk=CHUNK, seed=7)
-    img_fast = fast.render(*sr, chunk=CHUNK, seed=7, **prop_kw)
-    img_other = fast.render(*sr, chunk=CHUNK, seed=7, proposal=proposal, proposal_mode=other_mode,
+    img_plain = plain.render(*sr, chunk=CHUNK, streams=args.streams, seed=7)
+    img_fast = fast.render(*sr, chunk=CHUNK, streams=args.streams, seed=7, **prop_kw)
+    img_other = fast.render(*sr, chunk=CHUNK, streams=args.streams, seed=7, proposal=proposal, proposal_mode=other_mode,
                             gate_tau=args.gate_tau) if proposal is not None else None
-    img_bf16 = fast.render(*sr, chunk=CHUNK, seed=7)
+    img_bf16 = fast.render(*sr, chunk=CHUNK, streams=args.streams, seed=7)
     gt = ng.NeRF(ng.make_params(N_coarse=SC, N_fine=512), precision="fp32", coarse_params=blob,
-                 fine_params=blob).render(*sr, chunk=CHUNK, seed=9)["rgb"]
+                 fine_params=blob).render(*sr, chunk=CHUNK, streams=args.streams, seed=9)["rgb"]
     psnr_plain, psnr_fast = ng.psnr(gt, img_plain["rgb"]), ng.psnr(gt, img_fast["rgb"])
     quality = {"rays": int(sub.numel()), "ground_truth": "plain FP32 hierarchical, 64 coarse + 512 fine",
                "psnr_plain_fp32_db": psnr_plain, "psnr_fast_db": psnr_fast,
@@ -486,8 +492,9 @@ def main():
     if proposal is not None and args.path == "bf16":
         # the same gated path with FP8-e4m3 MLP GEMMs (per-channel scales), for reference
         fp8 = ng.NeRF(params, precision="fp8", coarse_params=blob, fine_params=blob)
-        fp8_ms = timed_steps(lambda i: fp8.render(*rays, chunk=CHUNK, seed=1000 * i, **prop_kw), args.plain_steps, 1)
-        img_fp8 = fp8.render(*sr, chunk=CHUNK, seed=7, **prop_kw)
+        fp8_ms = timed_steps(lambda i: fp8.render(*rays, chunk=CHUNK, streams=args.streams,
+                                                  seed=1000 * i, **prop_kw), args.plain_steps, 1)
+        img_fp8 = fp8.render(*sr, chunk=CHUNK, streams=args.streams, seed=7, **prop_kw)
         fp8.coarse_model.check_device_errors()
         quality["fp8_" + args.proposal_mode] = {
             "rays_per_s": whole_job_rate(world, R, fp8_ms), "psnr_db": ng.psnr(gt, img_fp8["rgb"]),
@@ -497,8 +504,9 @@ def main():
         # the gate as it was before the fine draws were gated: coarse samples
         # only, threshold 1e-5
         co_kw = {"proposal": proposal, "proposal_mode": "gate", "gate_tau": 1e-5, "gate_fine_draws": False}
-        co_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, seed=1000 * i, **co_kw), args.plain_steps, 1)
-        co_psnr = ng.psnr(gt, fast.render(*sr, chunk=CHUNK, seed=7, **co_kw)["rgb"])
+        co_ms = timed_steps(lambda i: fast.render(*rays, chunk=CHUNK, streams=args.streams,
+                                                  seed=1000 * i, **co_kw), args.plain_steps, 1)
+        co_psnr = ng.psnr(gt, fast.render(*sr, chunk=CHUNK, streams=args.streams, seed=7, **co_kw)["rgb"])
         quality["gate_coarse_only_tau_1e-5"] = {"rays_per_s": whole_job_rate(world, R, co_ms), "psnr_db": co_psnr,
                                                 "psnr_gap_db": psnr_plain - co_psnr,
                                                 "gate_met": bool(psnr_plain - co_psnr <= 0.1)}
@@ -518,12 +526,13 @@ def main():
                                                                   steps=args.proposal_steps)
         g_kw = {"proposal": g_prop, "proposal_mode": "gate", "gate_tau": args.gate_tau,
                 "gate_fine_draws": bool(args.gate_fine_draws)}
-        g_ms = timed_steps(lambda i: g_fast.render(*rays, chunk=CHUNK, seed=1000 * i, **g_kw), args.plain_steps, 1)
+        g_ms = timed_steps(lambda i: g_fast.render(*rays, chunk=CHUNK, streams=args.streams,
+                                                   seed=1000 * i, **g_kw), args.plain_steps, 1)
         g_gt = ng.NeRF(ng.make_params(N_coarse=SC, N_fine=512), precision="fp32", coarse_params=bc,
-                       fine_params=bfn).render(*sr, chunk=CHUNK, seed=9)["rgb"]
-        g_img_plain = g_plain.render(*sr, chunk=CHUNK, seed=7)
-        g_img = g_fast.render(*sr, chunk=CHUNK, seed=7, **g_kw)
-        g_bf16 = ng.psnr(g_gt, g_fast.render(*sr, chunk=CHUNK, seed=7)["rgb"])
+                       fine_params=bfn).render(*sr, chunk=CHUNK, streams=args.streams, seed=9)["rgb"]
+        g_img_plain = g_plain.render(*sr, chunk=CHUNK, streams=args.streams, seed=7)
+        g_img = g_fast.render(*sr, chunk=CHUNK, streams=args.streams, seed=7, **g_kw)
+        g_bf16 = ng.psnr(g_gt, g_fast.render(*sr, chunk=CHUNK, streams=args.streams, seed=7)["rgb"])
         g_fast.coarse_model.check_device_errors()
         gp, gf = ng.psnr(g_gt, g_img_plain["rgb"]), ng.psnr(g_gt, g_img["rgb"])
         glorot = {"scene": "coarse = Glorot-uniform blob seed 31, fine = seed 32, zero biases",
@@ -677,7 +686,7 @@ def main():
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": args.path, "data": "synthetic",
             "config": {"workload": WORKLOAD + "; proposal 2x64 (L=6) trained on 200k rays from 100 cameras",
-                       "rays_per_step_per_gpu": R, "path": path,
+                       "rays_per_step_per_gpu": R, "path": path, "streams": args.streams,
                        "l2": "512 MB buffer written between timed steps"},
             "plain_fp32": {"value": world * R / (plain_ms / 1000.0), "unit": "rays/s",
                            "speedup": plain_ms / ms},

@@ -280,9 +280,18 @@ class NeRF:
         rgb_s, sig_s = self.coarse_model((xyz, rays_d), precision=precision, rows_per_dir=S)
         return ray_utils.post_process_model_output(rgb_s, sig_s, t, self.white_bg, trans_mode=self.trans_mode)
 
+    def _side_streams(self, n):
+        """n CUDA streams of the current device, made once and kept."""
+        dev = torch.cuda.current_device()
+        cache = self.__dict__.setdefault("_render_streams", {})
+        have = cache.setdefault(dev, [])
+        while len(have) < n:
+            have.append(torch.cuda.Stream(device=dev))
+        return have[:n]
+
     def render(self, rays_o, rays_d, near, far, *, chunk=4096, u_coarse=None, u_fine=None, seed=0,
                precision=None, return_coarse=False, proposal=None, proposal_mode="replace",
-               gate_tau=1e-4, gate_fine_draws=True):
+               gate_tau=1e-4, gate_fine_draws=True, streams=2):
         """Fine (and optionally coarse) rgb/depth/acc maps for every ray, in
         chunks of `chunk` rays (the reference renders 4096-ray batches,
         base_dataset.py:853-857). Uniforms come from Philox keyed by `seed`
@@ -293,7 +302,15 @@ class NeRF:
         run as in the plain chain but skip the coarse samples whose proposal
         weight is at most `gate_tau` (sigma = 0 there); with
         `gate_fine_draws` they also skip the fine draws that fall in such a
-        coarse bin."""
+        coarse bin.
+
+        Chunk k runs on stream k % `streams` (the caller's current stream and
+        `streams` - 1 side streams, each with its own workspace), so that one
+        chunk's ray kernels fill the SMs another chunk's MLP leaves idle.
+        Chunks are independent: the maps do not depend on `streams`. The
+        side streams start after the caller's stream has reached this call
+        and the caller's stream waits for them before returning, so the maps
+        are ordered on the caller's stream like a single-stream render."""
         if proposal is not None and proposal_mode not in ("replace", "gate"):
             raise ValueError(f"proposal_mode must be 'replace' or 'gate', not {proposal_mode!r}")
         gated = proposal is not None and proposal_mode == "gate"
@@ -311,54 +328,87 @@ class NeRF:
         out = {k: empty(R, 3) if k.startswith("rgb") else empty(R)
                for k in (["rgb", "depth", "acc"] + (["rgb_coarse", "depth_coarse", "acc_coarse"]
                                                      if return_coarse else []))}
+        if proposal is not None and return_coarse:
+            raise ValueError("the proposal paths have no coarse maps")
+        if int(streams) < 1:
+            raise ValueError(f"streams must be at least 1, not {streams}")
         lib = _lib.lib()
         ws_bytes = (lib.nerfgb_render_gated_workspace_bytes if gated else lib.nerfgb_render_workspace_bytes)(
             min(chunk, R), Sc, Sf)
-        ws = torch.empty(ws_bytes, dtype=torch.uint8, device=rays_o.device)
         pc, pf = self.coarse_model.packed(precision), self.fine_model.packed(precision)
-        for s in range(0, R, chunk):
+        n_st = min(int(streams), max(1, (R + chunk - 1) // chunk))
+        main = torch.cuda.current_stream()
+        sts = [main] + self._side_streams(n_st - 1)
+        wss = [torch.empty(ws_bytes, dtype=torch.uint8, device=rays_o.device) for _ in range(n_st)]
+        if n_st > 1:
+            # side streams: start after everything the caller's stream has
+            # queued (inputs, outputs, packed weights); the caching allocator
+            # learns which streams use each buffer
+            fork = torch.cuda.Event()
+            fork.record(main)
+            used = [rays_o, rays_d, near, far, u_coarse, u_fine, pc, pf, *out.values()]
+            if proposal is not None:
+                used.append(proposal.params)
+            for k, st in enumerate(sts[1:], 1):
+                st.wait_event(fork)
+                wss[k].record_stream(st)
+                for t in used:
+                    if t is not None:
+                        t.record_stream(st)
+        for k, s in enumerate(range(0, R, chunk)):
             e = min(R, s + chunk)
             sl = slice(s, e)
-            if proposal is not None and return_coarse:
-                raise ValueError("the proposal paths have no coarse maps")
-            if gated:
-                _lib.call("nerfgb_render_rays_gated", ptr(proposal.params), ptr(pc), ptr(pf), prec,
-                          ptr(rays_o[sl]), ptr(rays_d[sl]), ptr(near[sl]), ptr(far[sl]),
-                          ptr(u_coarse[sl]) if u_coarse is not None else None,
-                          ptr(u_fine[sl]) if u_fine is not None else None,
-                          ctypes.c_ulonglong(int(seed) + s), e - s, Sc, Sf,
-                          int(bool(self.params.sampling.perturb)),
-                          int(bool(self.params.sampling.lin_inv_depth)), int(self.white_bg),
-                          int(self.trans_mode), ctypes.c_float(gate_tau),
-                          _lib.GATE_FINE_DRAWS if gate_fine_draws else 0, ptr(out["rgb"][sl]),
-                          ptr(out["depth"][sl]), ptr(out["acc"][sl]), ptr(ws),
-                          ptr(self.coarse_model.err_word), stream())
-                continue
-            if proposal is not None:
-                _lib.call("nerfgb_render_rays_proposal", ptr(proposal.params), ptr(pf), prec,
-                          ptr(rays_o[sl]), ptr(rays_d[sl]), ptr(near[sl]), ptr(far[sl]),
-                          ptr(u_coarse[sl]) if u_coarse is not None else None,
-                          ptr(u_fine[sl]) if u_fine is not None else None,
-                          ctypes.c_ulonglong(int(seed) + s), e - s, Sc, Sf,
-                          int(bool(self.params.sampling.perturb)),
-                          int(bool(self.params.sampling.lin_inv_depth)), int(self.white_bg),
-                          int(self.trans_mode), ptr(out["rgb"][sl]), ptr(out["depth"][sl]),
-                          ptr(out["acc"][sl]), ptr(ws), ptr(self.fine_model.err_word), stream())
-                continue
-            _lib.call("nerfgb_render_rays", ptr(pc), ptr(pf), prec, ptr(rays_o[sl]), ptr(rays_d[sl]),
-                      ptr(near[sl]), ptr(far[sl]),
+            ws = wss[k % n_st]
+            with torch.cuda.stream(sts[k % n_st]):
+                self._render_chunk(lib, gated, proposal, pc, pf, prec, rays_o, rays_d, near, far, u_coarse,
+                                   u_fine, seed, s, sl, e, Sc, Sf, gate_tau, gate_fine_draws, return_coarse, out,
+                                   ws)
+        for st in sts[1:]:
+            join = torch.cuda.Event()
+            join.record(st)
+            main.wait_event(join)
+        return out
+
+    def _render_chunk(self, lib, gated, proposal, pc, pf, prec, rays_o, rays_d, near, far, u_coarse, u_fine,
+                      seed, s, sl, e, Sc, Sf, gate_tau, gate_fine_draws, return_coarse, out, ws):
+        """One chunk's library call, on the current stream."""
+        if gated:
+            _lib.call("nerfgb_render_rays_gated", ptr(proposal.params), ptr(pc), ptr(pf), prec,
+                      ptr(rays_o[sl]), ptr(rays_d[sl]), ptr(near[sl]), ptr(far[sl]),
                       ptr(u_coarse[sl]) if u_coarse is not None else None,
                       ptr(u_fine[sl]) if u_fine is not None else None,
                       ctypes.c_ulonglong(int(seed) + s), e - s, Sc, Sf,
                       int(bool(self.params.sampling.perturb)),
                       int(bool(self.params.sampling.lin_inv_depth)), int(self.white_bg),
-                      int(self.trans_mode),
-                      ptr(out["rgb_coarse"][sl]) if return_coarse else None,
-                      ptr(out["depth_coarse"][sl]) if return_coarse else None,
-                      ptr(out["acc_coarse"][sl]) if return_coarse else None,
-                      ptr(out["rgb"][sl]), ptr(out["depth"][sl]), ptr(out["acc"][sl]), ptr(ws),
+                      int(self.trans_mode), ctypes.c_float(gate_tau),
+                      _lib.GATE_FINE_DRAWS if gate_fine_draws else 0, ptr(out["rgb"][sl]),
+                      ptr(out["depth"][sl]), ptr(out["acc"][sl]), ptr(ws),
                       ptr(self.coarse_model.err_word), stream())
-        return out
+            return
+        if proposal is not None:
+            _lib.call("nerfgb_render_rays_proposal", ptr(proposal.params), ptr(pf), prec,
+                      ptr(rays_o[sl]), ptr(rays_d[sl]), ptr(near[sl]), ptr(far[sl]),
+                      ptr(u_coarse[sl]) if u_coarse is not None else None,
+                      ptr(u_fine[sl]) if u_fine is not None else None,
+                      ctypes.c_ulonglong(int(seed) + s), e - s, Sc, Sf,
+                      int(bool(self.params.sampling.perturb)),
+                      int(bool(self.params.sampling.lin_inv_depth)), int(self.white_bg),
+                      int(self.trans_mode), ptr(out["rgb"][sl]), ptr(out["depth"][sl]),
+                      ptr(out["acc"][sl]), ptr(ws), ptr(self.fine_model.err_word), stream())
+            return
+        _lib.call("nerfgb_render_rays", ptr(pc), ptr(pf), prec, ptr(rays_o[sl]), ptr(rays_d[sl]),
+                  ptr(near[sl]), ptr(far[sl]),
+                  ptr(u_coarse[sl]) if u_coarse is not None else None,
+                  ptr(u_fine[sl]) if u_fine is not None else None,
+                  ctypes.c_ulonglong(int(seed) + s), e - s, Sc, Sf,
+                  int(bool(self.params.sampling.perturb)),
+                  int(bool(self.params.sampling.lin_inv_depth)), int(self.white_bg),
+                  int(self.trans_mode),
+                  ptr(out["rgb_coarse"][sl]) if return_coarse else None,
+                  ptr(out["depth_coarse"][sl]) if return_coarse else None,
+                  ptr(out["acc_coarse"][sl]) if return_coarse else None,
+                  ptr(out["rgb"][sl]), ptr(out["depth"][sl]), ptr(out["acc"][sl]), ptr(ws),
+                  ptr(self.coarse_model.err_word), stream())
 
     def load_model(self, load_dir, load_tag, skip_optimizer=False):
         """NeRF.set_everything (nerf/core/model.py:238-287): unless

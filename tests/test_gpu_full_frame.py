@@ -70,6 +70,37 @@ def test_full_frame_gated_render_commutes_with_ray_permutation(ng, cuda, frame):
     assert 0.0 < float(a["acc"].mean()) < 1.0
 
 
+@pytest.mark.parametrize("mode", ["plain", "gate", "replace"])
+def test_full_frame_streams_do_not_change_maps(ng, cuda, frame, mode):
+    """Chunks alternate over the caller's stream and side streams with their
+    own workspaces: one, two and three streams give the same maps bit for
+    bit, and the maps are complete when the caller's stream reaches them
+    (read here on that stream without another synchronisation)."""
+    rays, uc, uf, blob = frame
+    nerf = ng.NeRF(ng.make_params(), precision="bf16", coarse_params=blob, fine_params=blob)
+    kw = dict(chunk=4096, u_coarse=uc, u_fine=uf)
+    if mode != "plain":
+        kw.update(proposal=ng.ProposalNetwork(seed=7), proposal_mode=mode, gate_tau=1e-4)
+    maps = {n: nerf.render(*rays, streams=n, **kw) for n in (1, 2, 3)}
+    sums = {n: torch.stack([m[k].double().sum() for k in ("rgb", "depth", "acc")]).cpu() for n, m in maps.items()}
+    nerf.coarse_model.check_device_errors()
+    for n in (2, 3):
+        for k in ("rgb", "depth", "acc"):
+            assert torch.equal(maps[n][k], maps[1][k]), (n, k)
+        assert torch.equal(sums[n], sums[1]), n
+
+
+def test_render_streams_argument(ng, cuda):
+    nerf = ng.NeRF(ng.make_params(), precision="bf16")
+    rays = [torch.from_numpy(x).cuda() for x in ng.synthetic.frame_rays(3, 8, 8, 10.0)]
+    with pytest.raises(ValueError):
+        nerf.render(*rays, streams=0)
+    one = nerf.render(*rays, chunk=16, seed=3, streams=1)
+    many = nerf.render(*rays, chunk=16, seed=3, streams=8)  # more streams than chunks
+    for k in ("rgb", "depth", "acc"):
+        assert torch.equal(one[k], many[k]), k
+
+
 @pytest.mark.parametrize("precision", ["bf16", "fp8"])
 def test_fine_pass_mlp_row_permutation(ng, cuda, precision):
     """The tensor-core MLP at its fine-pass launch shape: every row is computed
