@@ -65,8 +65,9 @@ def parse():
     ap.add_argument("--proposal", type=int, default=1, help="1: BF16 + learned proposal (headline)")
     ap.add_argument("--proposal-mode", default="gate", choices=["gate", "replace"])
     ap.add_argument("--gate-tau", type=float, default=1e-4)
-    ap.add_argument("--streams", type=int, default=2,
-                    help="streams the render's chunks alternate over (NeRF.render(streams=))")
+    ap.add_argument("--streams", type=int, default=3,
+                    help="streams the render's chunks alternate over (NeRF.render(streams=)) and "
+                         "the training backward runs on (NeRF.backward_streams)")
     ap.add_argument("--gate-fine-draws", type=int, default=1,
                     help="1: the gate also skips fine draws in coarse bins the proposal calls empty")
     ap.add_argument("--proposal-steps", type=int, default=2000)
@@ -118,6 +119,7 @@ def train_only(args):
              for x in ng.synthetic.training_rays(500, 4, (args.batch + 3) // 4)]
     target = teacher.render(*batch, seed=3)["rgb"]
     student = ng.NeRF(params, precision=args.path, seed=60)
+    student.backward_streams = args.streams
     tile = args.train_tile or None
     for _ in range(args.warmup):
         student.train_step((tuple(batch), (target,)), tile_rays=tile)
@@ -659,6 +661,7 @@ def main():
                              "in backward", "train_tile": args.train_tile}
         for tp, tile in (("bf16", 4096), ("bf16", args.train_tile or None), ("fp32", 4096)):
             student = ng.NeRF(params, precision=tp, seed=60)
+            student.backward_streams = args.streams
             tms = timed_steps(lambda i: student.train_step((tuple(batch), (target,)), tile_rays=tile),
                               args.train_steps, 1)
             student.coarse_model.check_device_errors()

@@ -57,16 +57,43 @@ def _keep_tape(nerf, passes):
                                    for k, (t, s, r, a, pp) in zip(("coarse", "fine"), passes)}
 
 
+def _backward_pass(nerf, model, t, sig, rgb_s, acts, g_map, g):
+    """Compositing backward then MLP backward of one network, on the current
+    stream, its gradient accumulated into g."""
+    n, S = t.shape
+    d_sig, d_rgb = empty(n * S), empty(n * S, 3)
+    _lib.call("nerfgb_composite_backward", ptr(sig), ptr(t), ptr(rgb_s), ptr(g_map), None, n, S,
+              int(nerf.white_bg), ptr(d_sig), ptr(d_rgb), stream())
+    model.backward(acts, d_rgb, d_sig, g)
+
+
 def _backward_passes(nerf, passes, grad_maps, grads):
-    """Compositing backward then MLP backward of both networks, gradients
-    accumulated into grads = (coarse blob grad, fine blob grad)."""
-    for model, (t, sig, rgb_s, acts, _), g_map, g in zip((nerf.coarse_model, nerf.fine_model), passes, grad_maps,
-                                                          grads):
-        n, S = t.shape
-        d_sig, d_rgb = empty(n * S), empty(n * S, 3)
-        _lib.call("nerfgb_composite_backward", ptr(sig), ptr(t), ptr(rgb_s), ptr(g_map.contiguous()), None, n, S,
-                  int(nerf.white_bg), ptr(d_sig), ptr(d_rgb), stream())
-        model.backward(acts, d_rgb, d_sig, g)
+    """Both networks' backward, gradients accumulated into grads = (coarse
+    blob grad, fine blob grad). The two are independent (the fine samples
+    carry no gradient into the coarse network), so with
+    nerf.backward_streams > 1 the coarse network's runs on a side stream
+    beside the fine network's on the current stream, which waits for it
+    before returning."""
+    jobs = [(model, t, sig, rgb_s, acts, g_map.contiguous(), g)
+            for model, (t, sig, rgb_s, acts, _), g_map, g in zip((nerf.coarse_model, nerf.fine_model), passes,
+                                                                  grad_maps, grads)]
+    if getattr(nerf, "backward_streams", 1) <= 1:
+        for job in jobs:
+            _backward_pass(nerf, *job)
+        return
+    main = torch.cuda.current_stream()
+    side = nerf._side_streams(1)[0]
+    fork = torch.cuda.Event()
+    fork.record(main)
+    side.wait_event(fork)
+    for x in jobs[0][1:]:
+        x.record_stream(side)
+    with torch.cuda.stream(side):
+        _backward_pass(nerf, *jobs[0])
+    _backward_pass(nerf, *jobs[1])
+    join = torch.cuda.Event()
+    join.record(side)
+    main.wait_event(join)
 
 
 class RenderFunction(torch.autograd.Function):

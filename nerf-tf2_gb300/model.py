@@ -183,6 +183,9 @@ class NeRF:
                                                      precision=precision)
         self.fine_model = get_coarse_or_fine_model("fine", params=fine_params, seed=seed + 1,
                                                    precision=precision)
+        # 2: the training backward runs the coarse network's gradient on a
+        # side stream beside the fine network's (1: one stream)
+        self.backward_streams = 2
 
     def forward(self, rays_o, rays_d, near, far, *, u_coarse=None, u_fine=None):
         """model.py:57-125 with optional explicit jitter uniforms."""
@@ -291,7 +294,7 @@ class NeRF:
 
     def render(self, rays_o, rays_d, near, far, *, chunk=4096, u_coarse=None, u_fine=None, seed=0,
                precision=None, return_coarse=False, proposal=None, proposal_mode="replace",
-               gate_tau=1e-4, gate_fine_draws=True, streams=2):
+               gate_tau=1e-4, gate_fine_draws=True, streams=3):
         """Fine (and optionally coarse) rgb/depth/acc maps for every ray, in
         chunks of `chunk` rays (the reference renders 4096-ray batches,
         base_dataset.py:853-857). Uniforms come from Philox keyed by `seed`

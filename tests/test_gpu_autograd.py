@@ -117,3 +117,38 @@ def test_single_tile_keeps_forward_tape(ng, cuda):
         assert np.array_equal(r[2], res[0][2]) and np.array_equal(r[3], res[0][3])
         for ga, gb in ((res[0][0], r[0]), (res[0][1], r[1])):
             np.testing.assert_allclose(gb, ga, rtol=1e-4, atol=1e-6 * np.abs(ga).max())
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_backward_streams_give_the_same_gradients(ng, cuda, precision):
+    """The coarse network's backward on a side stream beside the fine
+    network's (NeRF.backward_streams = 2) gives the one-stream gradients, up
+    to the FP32 order of the backward's atomic row reductions, and a full
+    train_step after it the same loss; the gradients are complete when the
+    caller's stream reads them."""
+    (o, d, n, f), uc, uf, target = _case(ng, R=64, seed=17)
+    p = ng.make_params()
+    bc, bf = biased_blob(ng, 31), biased_blob(ng, 32)
+    res = {}
+    for streams in (1, 2):
+        nerf = ng.NeRF(p, precision=precision, coarse_params=bc, fine_params=bf)
+        nerf.backward_streams = streams
+        for tile in (None, 16):
+            for m in (nerf.coarse_model, nerf.fine_model):
+                m.params.grad = None
+            rgb_c, rgb_f = ng.autograd.render_with_grad(nerf, dev(o), dev(d), dev(n), dev(f), u_coarse=dev(uc),
+                                                        u_fine=dev(uf), tile_rays=tile)
+            (ng.autograd.mse(rgb_c, dev(target)) + ng.autograd.mse(rgb_f, dev(target))).backward()
+            res[streams, tile] = (nerf.coarse_model.params.grad.double().sum().cpu(),
+                                  host(nerf.coarse_model.params.grad), host(nerf.fine_model.params.grad))
+        data = ((dev(o), dev(d), dev(n), dev(f)), (dev(target),))
+        res[streams, "step"] = nerf.train_step(data, u_coarse=dev(uc), u_fine=dev(uf))["loss"]
+        nerf.coarse_model.check_device_errors()
+    for tile in (None, 16):
+        a, b = res[1, tile], res[2, tile]
+        assert float(a[0]) != 0.0
+        np.testing.assert_allclose(float(b[0]), float(a[0]), rtol=1e-4)
+        for ga, gb in ((a[1], b[1]), (a[2], b[2])):
+            assert np.abs(ga).max() > 0
+            np.testing.assert_allclose(gb, ga, rtol=1e-4, atol=1e-6 * np.abs(ga).max())
+    assert res[1, "step"] == res[2, "step"]
