@@ -61,11 +61,21 @@ namespace tc {
 
 constexpr int kRows = 256;          // rows per CTA tile
 constexpr int kThreads = 18 * 32;
+// The pair kernel that writes the activation tape has a 19th warp whose
+// first lane stores each written operand region to the tape.
+constexpr int kTapeWarp = 18;
+__host__ __device__ constexpr int threads_of(bool tape_warp) { return tape_warp ? (kTapeWarp + 1) * 32 : kThreads; }
 
 // Tensor maps of the pair pack's weights (2-D, 256-byte rows of 128 BF16),
-// one per weight-half size: 64 rows (16 KB), 32 (8 KB), 16 (4 KB).
+// one per weight-half size: 64 rows (16 KB), 32 (8 KB), 16 (4 KB). With the
+// tape: the tape (kActsLd BF16 per row) as 3-D (8 elements, rows, 8-element
+// column groups; strides 2 B, the row stride, 16 B), whose 128-row boxes
+// have the operand regions' image (element (r, k) at (k/8)*2048 + r*16 +
+// (k%8)*2), so a region is stored to its tape columns as one box: tape[0]
+// 32 groups (a 256-wide activation), tape[1] 8 (enc_xyz), tape[2] 4 (enc_dir).
 struct PairMaps {
   CUtensorMap map[3];
+  CUtensorMap tape[3];
 };
 __host__ __device__ constexpr int pair_map_of(uint32_t bytes) { return bytes == 16384u ? 0 : bytes == 8192u ? 1 : 2; }
 
@@ -93,6 +103,8 @@ struct Layout {
   static constexpr uint32_t kTmemSlot = kMiscOff + 296;
   static constexpr uint32_t kAbort = kMiscOff + 304;    // int, then the wait limit (u64) at +8
   static constexpr uint32_t kBarHead = kMiscOff + 320;  // [2]
+  static constexpr uint32_t kBarTapeRdy = kMiscOff + 336;   // [2] (the pair kernel with the tape)
+  static constexpr uint32_t kBarTapeDone = kMiscOff + 352;  // [2]
   static constexpr uint32_t kSigPart = kMiscOff + 384;  // float [2][128] (single-CTA epilogue)
   static constexpr uint32_t kSmemBytes = kSigPart + 2 * 128 * 4;
   // Pair epilogue: head partial sums (float), in regions idle at the time: sigma's [4][128]
@@ -481,12 +493,13 @@ __device__ __forceinline__ void for_each_load(long long t_first, long long t_ste
 // CTA's full barrier; the odd CTA's epilogue warps arrive on the even CTA's
 // operand barriers; commits reach both CTAs.
 template <int KCH, int NST, bool PINGPONG, bool TSMEM, bool F8, bool STORE, bool PAIR = false>
-__global__ void __launch_bounds__(kThreads, 1)
+__global__ void __launch_bounds__(threads_of(STORE && PAIR), 1)
     mlp_tc_kernel(const uint8_t *__restrict__ packed, const float *__restrict__ xyz,
                     const float *__restrict__ dirs, long long n_max, int rpd, float *__restrict__ rgb_out,
                     float *__restrict__ sigma_out, int *__restrict__ err, RowMap rm, uint16_t *__restrict__ tape,
                     unsigned long long wait_ns, long long withhold, const __grid_constant__ PairMaps maps) {
   static_assert(!(STORE && F8), "the activation tape is BF16");
+  static_assert(kActsLd % 8 == 0 && kActsEncXyz % 8 == 0 && kActsEncDir % 8 == 0, "tape columns in 8-element groups");
   static_assert(!PAIR || (!F8 && PINGPONG && KCH == kPairKch), "pair path: BF16 ping-pong, the pair pack's chunks");
   using L = Layout<TSMEM, F8>;
   constexpr uint32_t kE = L::kE;           // bytes per operand element
@@ -549,6 +562,13 @@ __global__ void __launch_bounds__(kThreads, 1)
       mbar_init(sbase + L::kBarHead + 8 * s, PAIR ? 16 : 4);
     }
     mbar_init(sbase + kBarDrain, 1);
+    if (STORE && PAIR) {
+      for (int s = 0; s < 2; ++s) {
+        // one arrival per epilogue warp of this CTA; the tape writer's
+        mbar_init(sbase + L::kBarTapeRdy + 8 * s, 16);
+        mbar_init(sbase + L::kBarTapeDone + 8 * s, 1);
+      }
+    }
     *abort_flag = 0;
     set_wait_limit(abort_flag, wait_ns);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -695,6 +715,44 @@ __global__ void __launch_bounds__(kThreads, 1)
         }
       }
     }
+  } else if (STORE && PAIR && warp == kTapeWarp) {
+    // ---------------- tape writer (pair kernel with the tape) ----------------
+    // Per tile and sub-tile the epilogue signals ten regions on tape_rdy, in
+    // order: enc_xyz (written for the tile's dense_0), then h0 .. h8 (each
+    // layer's output, the next layer's operand; with h8 the enc_dir of
+    // dense_9). Each goes to its tape columns of the sub-tile's 128 rows as
+    // one tensor store (rows past n are not written); once the store has read
+    // shared memory, tape_done tells the epilogue that the region may be
+    // rewritten. h9 (never an operand) is stored by the epilogue itself.
+    if (lane == 0) {
+      uint32_t rdy_phase[2] = {0u, 0u};
+      bool ok = true;
+      for (long long tile = t_first; tile < ntiles && ok; tile += t_step) {
+        for (int e = 0; e < 10 && ok; ++e) {
+          for (int s = 0; s < 2; ++s) {
+            if (!wait_bar(sbase + L::kBarTapeRdy + 8 * s, rdy_phase[s], abort_flag, err)) {
+              ok = false;
+              break;
+            }
+            rdy_phase[s] ^= 1u;
+            const long long row = tile * kTileRows + (long long)crank * kRows + s * 128;
+            const uint32_t enc = sbase + kEncOff + s * L::kEncBytes, act = sbase + kActOff + s * L::kActBytes;
+            if (row < n) {  // (a box from row n on would write nothing)
+              if (e == 0) {
+                tma_store_3d(&maps.tape[1], enc, 0, (int)row, kActsEncXyz / 8);
+              } else {
+                tma_store_3d(&maps.tape[0], act, 0, (int)row, acts_offset(e - 1) / 8);
+                if (e == 9) tma_store_3d(&maps.tape[2], enc, 0, (int)row, kActsEncDir / 8);
+              }
+              bulk_commit();
+              bulk_wait_read();
+            }
+            mbar_arrive(sbase + L::kBarTapeDone + 8 * s);
+          }
+        }
+      }
+      bulk_wait_all();  // no store still reads this CTA's shared memory or writes the tape
+    }
   } else {
     if constexpr (PAIR) {
       // ---------------- epilogue warps (pair) ----------------
@@ -708,9 +766,22 @@ __global__ void __launch_bounds__(kThreads, 1)
       const int qd = warp & 3, cq = ew >> 2;
       const int r = 32 * qd + lane;  // row within a sub-tile (= TMEM lane)
       const uint32_t tlane = tmem + ((uint32_t)(32 * qd) << 16);
+      // With the tape: a region signalled to the tape writer is not rewritten
+      // before its store has read it (tape_done; at most one pending per
+      // sub-tile, so a parity wait cannot miss a phase).
+      bool tape_pending[2] = {false, false};
+      uint32_t tape_phase[2] = {0u, 0u};
+      auto tape_settle = [&](int s) -> bool {
+        if (!STORE || !tape_pending[s]) return true;
+        tape_pending[s] = false;
+        const bool done = __all_sync(0xffffffffu, wait_bar(sbase + L::kBarTapeDone + 8 * s, tape_phase[s], abort_flag,
+                                                           err));
+        tape_phase[s] ^= 1u;
+        return done;
+      };
       // The operands of sub-tile s's next MMAs are written (and its
       // accumulators read): one arrival per warp, on the even CTA's barrier
-      // for a pair.
+      // for a pair (with the tape, also on this CTA's tape_rdy).
       auto operands_ready = [&](int s) {
         fence_proxy_async();
         tc_fence_before();
@@ -720,7 +791,9 @@ __global__ void __launch_bounds__(kThreads, 1)
             mbar_arrive_remote(peer_addr(sbase + kBarActr + 8 * s, 0));
           else
             mbar_arrive(sbase + kBarActr + 8 * s);
+          if (STORE) mbar_arrive(sbase + L::kBarTapeRdy + 8 * s);
         }
+        if (STORE) tape_pending[s] = true;
       };
       auto head_arrive = [&](int s) {
         __syncwarp();
@@ -741,7 +814,9 @@ __global__ void __launch_bounds__(kThreads, 1)
         float x[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) x[c] = valid[s] ? xyz[prow[s] * 3 + c] : 0.0f;
-        uint16_t *tt = trow_tape[s] ? trow_tape[s] + kActsEncXyz + 16 * cq : nullptr;
+        // (with the tape, the encoding reaches it by the tape writer's store)
+        uint16_t *const tt = nullptr;
+        tape_settle(s);  // nothing pending here: the sub-tile's dense_9 epilogue settled it
         if (cq == 0)
           write_enc_xyz_q<0, F8>(enc, r, x, tt);
         else if (cq == 1)
@@ -772,6 +847,12 @@ __global__ void __launch_bounds__(kThreads, 1)
               break;
             }
             tc_fence_after();
+            // the sub-tile's regions are rewritten below (the next operand,
+            // head partials, encodings) once the tape has them
+            if (!tape_settle(s)) {
+              ok = false;
+              break;
+            }
             const uint32_t enc = sbase + kEncOff + s * L::kEncBytes;
             const uint32_t act = sbase + kActOff + s * L::kActBytes;
             float sig = 0.0f;
@@ -843,7 +924,7 @@ __global__ void __launch_bounds__(kThreads, 1)
                 else
                   store_row32<true, true>(act, r, col0, v);
               } else if (STORE) {
-                // BF16 operands of the next layer, to shared memory and the tape
+                // BF16 operands of the next layer (the tape writer stores them)
                 uint32_t u[16];
                 if (g == 8) {  // dense_8 is linear (model.py:377-378)
 #pragma unroll
@@ -856,7 +937,6 @@ __global__ void __launch_bounds__(kThreads, 1)
                 for (int kg = 0; kg < 4; ++kg)
                   st_shared_v4(act + (uint32_t)(col0 / 8 + kg) * 2048u + r * 16, u[4 * kg], u[4 * kg + 1],
                                u[4 * kg + 2], u[4 * kg + 3]);
-                if (trow_tape[s]) tape_store32(trow_tape[s] + acts_offset(g) + col0, u);
               } else if (g == 8) {  // dense_8 is linear (model.py:377-378)
 #pragma unroll
                 for (int kg = 0; kg < 4; ++kg)
@@ -899,7 +979,7 @@ __global__ void __launch_bounds__(kThreads, 1)
               float d[3];
 #pragma unroll
               for (int c = 0; c < 3; ++c) d[c] = dirs[dr * 3 + c];
-              uint16_t *tt = trow_tape[s] ? trow_tape[s] + kActsEncDir + 8 * cq : nullptr;
+              uint16_t *const tt = nullptr;  // (the tape writer stores it with h8)
               if (cq == 0)
                 write_enc_dir_q<0, F8>(enc, r, d, tt);
               else if (cq == 1)
@@ -1233,7 +1313,7 @@ static int launch_variant(const void *packed, const float *xyz, const float *dir
     attr[0].val.clusterDim.x = 2;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    cfg.blockDim = dim3(tc::kThreads);
+    cfg.blockDim = dim3((unsigned)tc::threads_of(STORE));
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
     cfg.attrs = attr;
@@ -1259,9 +1339,21 @@ static int launch_variant(const void *packed, const float *xyz, const float *dir
     if (max_pairs < 1) return NERFGB_E_UNSUPPORTED;
     const long long pairs = ntiles < max_pairs ? (ntiles > 0 ? ntiles : 1) : max_pairs;
     cfg.gridDim = dim3((unsigned)(2 * pairs));
-    tc::PairMaps maps;
+    tc::PairMaps maps{};
     int rc = pair_maps(pk, maps);
     if (rc != NERFGB_OK) return rc;
+    if constexpr (STORE) {
+      // the tape [n][kActsLd] BF16 as 3-D (8 elements, rows, 8-element
+      // groups), boxes of 128 rows by 32, 8 and 4 groups (tc::PairMaps)
+      if (reinterpret_cast<uintptr_t>(tape) % 16 != 0) return NERFGB_E_INVALID_ARG;
+      const unsigned long long dims[3] = {8, (unsigned long long)(n > 0 ? n : 1), kActsLd / 8};
+      const unsigned long long strides[2] = {(unsigned long long)kActsLd * 2, 16};
+      const unsigned groups[3] = {32, 8, 4};
+      for (int i = 0; i < 3; ++i) {
+        const unsigned box[3] = {8, 128, groups[i]};
+        if ((rc = encode_tensor_map_u16(&maps.tape[i], tape, 3, dims, strides, box)) != NERFGB_OK) return rc;
+      }
+    }
     if (cudaLaunchKernelEx(&cfg, kern, pk, xyz, dirs, n, rpd, rgb, sigma, err_word, rm, tape, wait_ns, withhold,
                            maps) != cudaSuccess)
       return NERFGB_E_CUDA;

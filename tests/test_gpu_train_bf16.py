@@ -119,3 +119,33 @@ def test_train_step_resumes_loaded_adam_state(ng, oracle, cuda):
         fresh, _, _ = oracle.apply_adam(before[k], 0.0, 0.0, grads[k], 1, 1e-3)
         assert np.abs(fresh - want).max() > 1e-4  # the loaded state matters
     assert nerf._train_state()["step"] == 42
+
+
+def test_bf16_tape_rows_permute_and_stop_at_n(ng, cuda):
+    """The tape at a ragged size (several 512-row pair tiles, a partial last
+    one): each row's tape is its own row's operands, bit for bit under a row
+    permutation, including the encodings (columns 0-63 and enc_dir) and h9;
+    rows past n of a larger buffer are not written."""
+    lib = ng._lib
+    n = 100_003
+    g = torch.Generator(device="cuda")
+    g.manual_seed(23)
+    xyz = torch.rand(n, 3, device="cuda", generator=g) * 4 - 2
+    dirs = torch.nn.functional.normalize(torch.randn(n, 3, device="cuda", generator=g), dim=1)
+    mlp = ng.get_coarse_or_fine_model("fine", params=biased_blob(ng, 5), precision="bf16")
+    _, _, acts = mlp.forward_train(xyz, dirs, precision="bf16")
+    perm = torch.randperm(n, device="cuda", generator=g)
+    _, _, acts_p = mlp.forward_train(xyz[perm], dirs[perm], precision="bf16")
+    mlp.check_device_errors()
+    assert torch.equal(acts_p, acts[perm])
+    ld = acts.shape[1]
+    assert bool((acts[:, :63] != 0).any(dim=1).all())  # every row's encoding written
+    # rows past n: a buffer of n + 700 rows holding a sentinel
+    big = torch.full((n + 700, ld), 0x7BCD, dtype=torch.int16, device="cuda")
+    rgb, sig = torch.empty(n, 3, device="cuda"), torch.empty(n, 1, device="cuda")
+    lib.call("nerfgb_mlp_forward_train_bf16", mlp.packed("bf16").data_ptr(), xyz.data_ptr(), dirs.data_ptr(), n,
+             1, rgb.data_ptr(), sig.data_ptr(), big.data_ptr(), mlp.err_word.data_ptr(),
+             torch.cuda.current_stream().cuda_stream)
+    mlp.check_device_errors()
+    assert torch.equal(big[:n], acts)
+    assert bool((big[n:] == 0x7BCD).all())
