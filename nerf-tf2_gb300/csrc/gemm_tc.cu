@@ -17,7 +17,10 @@
 //            groups of K; SBO = S, between 8-column groups of M or N; the
 //            instruction descriptor's transpose bit set).
 // The backward uses both:
-//   dX = dZ W^T   A = dZ [rows][n_out] (K-major), B = W [k_in][n_out]
+//   dX = dZ W^T   A = dZ [rows][n_out] (K-major; streamed instead as 2-D
+//                 boxes of 64 columns (128 bytes) by 128 rows in the
+//                 128-byte swizzled layout, one request per 128-byte row
+//                 rather than per 16 bytes), B = W [k_in][n_out]
 //                 (K-major), C = dX [rows][k_in] stored as BF16;
 //   dW = In^T dZ  A = In [rows][k_in] (MN-major: M = k_in), B = dZ
 //                 [rows][n_out] (MN-major: N = n_out), reduced over rows in
@@ -83,7 +86,7 @@ struct Geo {
   // group strides (bytes) of the copied images
   // group strides of the tensor-copied images (A; B streamed MN-major), and
   // of the resident B copied by cp.async (padded for the copies' banks)
-  static constexpr uint32_t kSA = A_MN ? kKc * 16 : MT * 128 * 16;  // A: per 8 M-cols / 8 K-cols
+  static constexpr uint32_t kSA = A_MN ? kKc * 16 : MT * 128 * 16;  // A: per 8 M-cols (K-major: 16 KB swizzled)
   static constexpr uint32_t kSB = B_MN ? kKc * 16 : 256 * 16 + kPad;
   static constexpr uint32_t kABytes = A_MN ? (MT * 128 / 8) * kSA : (kKc / 8) * kSA;
   static constexpr uint32_t kBBytes = B_RES ? 0 : B_MN ? (256 / 8) * kSB : (kKc / 8) * kSB;
@@ -125,9 +128,31 @@ __device__ __forceinline__ void tma_3d(uint32_t dst, const CUtensorMap *map, int
       : "memory");
 }
 
+// One box of a 2-D tensor map (coordinates innermost first).
+__device__ __forceinline__ void tma_2d(uint32_t dst, const CUtensorMap *map, int c0, int c1, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(bar)
+      : "memory");
+}
+
+// Descriptor of a K-major operand in the 128-byte swizzled layout: rows of
+// 64 BF16 (128 bytes) at a 128-byte pitch, each 1024-byte block of 8 rows
+// with its 16-byte chunks permuted by the row (as the 128-byte-swizzle
+// tensor copy writes them; the block must start 1024-byte aligned). SBO =
+// 1024 (between 8-row blocks), LBO unused, swizzle mode 2 (bits 61-63); a
+// K step of 16 elements advances the start address by 32 bytes.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | (1ull << 16) | ((uint64_t)(1024u >> 4) << 32) | (1ull << 46) |
+         (2ull << 61);
+}
+
 template <bool A_MN, bool B_MN, int MT, int EPI, bool B_RES = false>
 __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_constant__ Maps maps) {
   using G = Geo<A_MN, B_MN, MT, B_RES>;
+  static_assert(A_MN || (MT == 1 && G::kABytes == 128u * 128u && G::kStage % 1024u == 0),
+                "a K-major A is one 128-row tile of 128-byte swizzled rows per stage");
   extern __shared__ __align__(1024) uint8_t smem[];
   const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -157,6 +182,11 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_
     mbar_init(sbase + G::kBarB, kLoadThreads);
     *abort_flag = 0;
     set_wait_limit(abort_flag, kWaitNs);
+    if (!A_MN && (sbase & 1023u) != 0) {
+      // the swizzled stages need 1024-byte alignment: nothing is copied
+      atomicExch(a.err, NERFGB_E_UNSUPPORTED);
+      *abort_flag = 1;
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == kIssuerWarp) {
@@ -204,6 +234,10 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_
             ok = false;
             break;
           }
+          if (*abort_flag) {
+            ok = false;
+            break;
+          }
           const uint32_t full = sbase + G::kBarFull + 8 * st, sa = sbase + st * G::kStage;
           mbar_expect_tx(full, kBytes);
           // MN-major: rows = the reduction (k0 ..), groups = M columns (m0 / 8 ..);
@@ -211,7 +245,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_
           if (A_MN)
             tma_3d(sa, &maps.a, 0, (int)k0, m0 / 8, full);
           else
-            tma_3d(sa, &maps.a, 0, m0, (int)(k0 / 8), full);
+            tma_2d(sa, &maps.a, (int)k0, m0, full);  // 64 columns x 128 rows, 128-byte swizzle
           if (!B_RES) tma_3d(sa + G::kABytes, &maps.b, 0, (int)k0, 0, full);
         }
       }
@@ -260,7 +294,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_
 #pragma unroll
             for (int h = 0; h < MT; ++h) {
               const uint64_t adesc = A_MN ? smem_desc(sa + (uint32_t)h * 16u * G::kSA + 256u * s, 128u, G::kSA)
-                                          : smem_desc(sa + (uint32_t)h * 2048u + 2u * s * G::kSA, G::kSA, 128u);
+                                          : smem_desc_sw128(sa + 32u * s);
               tc_mma(d0 + (uint32_t)h * 256u, adesc, bdesc, idesc, (first && s == 0) ? 0u : 1u);
             }
           }
@@ -383,10 +417,17 @@ static int launch(const Args &a, cudaStream_t st) {
   int rc;
   // A: MN-major [K rows][M cols] in kKc-row boxes of all MT*128 columns;
   // K-major [M rows][K cols] in 128-row boxes of kKc columns
-  if (A_MN)
+  if (A_MN) {
     rc = operand_map(&maps.a, a.A, a.lda, a.K, a.M / 8, kKc, MT * 128 / 8);
-  else
-    rc = operand_map(&maps.a, a.A, a.lda, a.M, a.K / 8, MT * 128, kKc / 8);
+  } else {
+    // K-major [M rows][K cols]: boxes of kKc columns (128 bytes) by 128 rows,
+    // 128-byte swizzle (one TMA row request per 128 bytes)
+    if (reinterpret_cast<uintptr_t>(a.A) % 16 != 0 || (a.lda * 2) % 16 != 0) return NERFGB_E_INVALID_ARG;
+    const unsigned long long dims[2] = {(unsigned long long)a.K, (unsigned long long)a.M};
+    const unsigned long long strides[1] = {(unsigned long long)(a.lda * 2)};
+    const unsigned box[2] = {kKc, 128};
+    rc = encode_tensor_map_u16(&maps.a, a.A, 2, dims, strides, box, true);
+  }
   if (rc != NERFGB_OK) return rc;
   if (!B_RES) {
     static_assert(B_RES || B_MN, "a streamed B is MN-major");

@@ -21,9 +21,11 @@ struct RowMap {
 
 // A tensor map of 16-bit elements over `base` (mlp_tc.cu): rank dims
 // (innermost first), the byte strides of dims 1.. (multiples of 16), box
-// sizes; no interleave or swizzle, zero fill outside the dims.
+// sizes; no interleave, zero fill outside the dims; no swizzle, or with
+// swizzle128 the 128-byte swizzle (box rows of 128 bytes land with their
+// 16-byte chunks permuted by the row within each 8-row, 1024-byte block).
 int encode_tensor_map_u16(CUtensorMap *map, const void *base, int rank, const unsigned long long *dims,
-                          const unsigned long long *strides, const unsigned *box);
+                          const unsigned long long *strides, const unsigned *box, bool swizzle128 = false);
 
 // FP32 SIMT forward (mlp.cu).
 int launch_mlp_fp32(const void *packed, const float *xyz, const float *dirs, long long n, int rows_per_dir,

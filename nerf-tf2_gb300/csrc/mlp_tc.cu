@@ -1254,7 +1254,7 @@ static EncodeTiledFn encode_tiled() {
 }
 
 int encode_tensor_map_u16(CUtensorMap *map, const void *base, int rank, const unsigned long long *dims,
-                          const unsigned long long *strides, const unsigned *box) {
+                          const unsigned long long *strides, const unsigned *box, bool swizzle128) {
   const EncodeTiledFn enc = encode_tiled();
   if (!enc || rank < 1 || rank > 5) return NERFGB_E_CUDA;
   cuuint64_t d[5], st[4];
@@ -1266,7 +1266,8 @@ int encode_tensor_map_u16(CUtensorMap *map, const void *base, int rank, const un
     if (i > 0) st[i - 1] = strides[i - 1];
   }
   return enc(map, CU_TENSOR_MAP_DATA_TYPE_UINT16, (cuuint32_t)rank, const_cast<void *>(base), d, st, b, e,
-             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+             CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
+             CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS
              ? NERFGB_OK
              : NERFGB_E_CUDA;
