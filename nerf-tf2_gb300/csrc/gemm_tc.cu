@@ -4,24 +4,24 @@
 //
 //   C[M][N] = sum_k A[m][k] B[n][k]        (tcgen05.mma.cta_group::1.kind::f16)
 //
-// Operands stream from row-major global memory by tensor copies (TMA) into
-// the no-swizzle core-matrix layout (8 rows x 16 bytes): a 3-D tensor map
-// (8 elements, rows, 8-element column groups; strides 2, the row stride, 16
-// bytes) makes one box land as "element (r, c) at (c/8)*S + r*16 + (c%8)*2"
-// with S = 16 * box rows, rows and groups past the bounds zero-filled. The
-// same bytes serve both operand orientations: that image of a row-major
-// [rows][cols] tile is
-//   K-major  when the reduction runs along cols (descriptor LBO = S, the
-//            stride between 8-column groups; SBO = 128, between 8-row groups),
-//   MN-major when the reduction runs along rows (LBO = 128, between 8-row
-//            groups of K; SBO = S, between 8-column groups of M or N; the
-//            instruction descriptor's transpose bit set).
-// The backward uses both:
-//   dX = dZ W^T   A = dZ [rows][n_out] (K-major; streamed instead as 2-D
-//                 boxes of 64 columns (128 bytes) by 128 rows in the
-//                 128-byte swizzled layout, one request per 128-byte row
-//                 rather than per 16 bytes), B = W [k_in][n_out]
-//                 (K-major), C = dX [rows][k_in] stored as BF16;
+// The streamed operands come from row-major global memory by tensor copies
+// (TMA) in the 128-byte swizzled layout, so that the copy engine fetches
+// whole 128-byte rows (boxes whose innermost extent is 16 bytes cost one
+// request per 16 bytes and held these kernels near 4 TB/s):
+//   K-major A (the reduction along the row, dX's dZ): 2-D boxes of 64
+//            columns by 128 rows, row r at r*128 bytes (smem_desc_sw128);
+//   MN-major A and B (the reduction along the rows, dW's In and dZ): 3-D
+//            boxes of 64-element atoms by kKc rows by the atoms of the tile,
+//            atom a at a*8 KB, row k at k*128 bytes (smem_desc_mn_sw128,
+//            the instruction descriptor's transpose bit set);
+// rows and atoms past the bounds are zero-filled, and within every 1024-byte
+// block the 16-byte chunks of row k sit permuted by k % 8, as the swizzled
+// descriptors read them. dX's resident B (W) is copied once by cp.async in
+// the no-swizzle core-matrix layout (8 rows x 16 bytes; K-major, LBO = the
+// stride between 8-column groups, SBO = 128).
+// The backward uses:
+//   dX = dZ W^T   A = dZ [rows][n_out] (K-major), B = W [k_in][n_out]
+//                 (K-major, resident), C = dX [rows][k_in] stored as BF16;
 //   dW = In^T dZ  A = In [rows][k_in] (MN-major: M = k_in), B = dZ
 //                 [rows][n_out] (MN-major: N = n_out), reduced over rows in
 //                 splits; each split's FP32 partial goes to a workspace and a
@@ -83,10 +83,10 @@ struct Args {
 // the stages hold A alone.
 template <bool A_MN, bool B_MN, int MT, bool B_RES = false>
 struct Geo {
-  // group strides (bytes) of the copied images
-  // group strides of the tensor-copied images (A; B streamed MN-major), and
-  // of the resident B copied by cp.async (padded for the copies' banks)
-  static constexpr uint32_t kSA = A_MN ? kKc * 16 : MT * 128 * 16;  // A: per 8 M-cols (K-major: 16 KB swizzled)
+  // bytes per 8 columns of a streamed stage (A; B streamed MN-major), which
+  // size the stages; the resident B's group stride (padded for the
+  // cp.async copies' banks)
+  static constexpr uint32_t kSA = A_MN ? kKc * 16 : MT * 128 * 16;
   static constexpr uint32_t kSB = B_MN ? kKc * 16 : 256 * 16 + kPad;
   static constexpr uint32_t kABytes = A_MN ? (MT * 128 / 8) * kSA : (kKc / 8) * kSA;
   static constexpr uint32_t kBBytes = B_RES ? 0 : B_MN ? (256 / 8) * kSB : (kKc / 8) * kSB;
@@ -148,6 +148,18 @@ __device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t addr) {
          (2ull << 61);
 }
 
+// Descriptor of an MN-major operand in the 128-byte swizzled layout: atoms
+// of 64 MN-elements (128-byte rows, one per K row), 64 K rows each (8 KB),
+// each 1024-byte block of 8 K rows with its 16-byte chunks permuted by the
+// row (as the 128-byte-swizzle tensor copy of a box of 64 elements x 64
+// rows x atoms writes them; blocks 1024-byte aligned). LBO = 8192 (between
+// MN atoms), SBO = 1024 (between 8-row K blocks), swizzle mode 2; a K step
+// of 16 rows advances the start address by 2048 bytes.
+__device__ __forceinline__ uint64_t smem_desc_mn_sw128(uint32_t addr) {
+  return (uint64_t)((addr & 0x3FFFFu) >> 4) | ((uint64_t)(8192u >> 4) << 16) | ((uint64_t)(1024u >> 4) << 32) |
+         (1ull << 46) | (2ull << 61);
+}
+
 template <bool A_MN, bool B_MN, int MT, int EPI, bool B_RES = false>
 __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_constant__ Maps maps) {
   using G = Geo<A_MN, B_MN, MT, B_RES>;
@@ -182,7 +194,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_
     mbar_init(sbase + G::kBarB, kLoadThreads);
     *abort_flag = 0;
     set_wait_limit(abort_flag, kWaitNs);
-    if (!A_MN && (sbase & 1023u) != 0) {
+    if ((sbase & 1023u) != 0) {
       // the swizzled stages need 1024-byte alignment: nothing is copied
       atomicExch(a.err, NERFGB_E_UNSUPPORTED);
       *abort_flag = 1;
@@ -243,7 +255,7 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_
           // MN-major: rows = the reduction (k0 ..), groups = M columns (m0 / 8 ..);
           // K-major: rows = M (m0 ..), groups = the reduction columns (k0 / 8 ..)
           if (A_MN)
-            tma_3d(sa, &maps.a, 0, (int)k0, m0 / 8, full);
+            tma_3d(sa, &maps.a, 0, (int)k0, m0 / 64, full);  // 64-element atoms x kKc rows, swizzled
           else
             tma_2d(sa, &maps.a, (int)k0, m0, full);  // 64 columns x 128 rows, 128-byte swizzle
           if (!B_RES) tma_3d(sa + G::kABytes, &maps.b, 0, (int)k0, 0, full);
@@ -290,10 +302,11 @@ __global__ void __launch_bounds__(kThreads, 1) gemm_kernel(Args a, const __grid_
 #pragma unroll
           for (int s = 0; s < kKc / 16; ++s) {
             // B: K-major k-step s = 2 column groups (2s * SB); MN-major = 2 row groups (2s * 128)
-            const uint64_t bdesc = B_MN ? smem_desc(sb + 256u * s, 128u, G::kSB) : smem_desc(sb + 2u * s * G::kSB, G::kSB, 128u);
+            const uint64_t bdesc =
+                B_MN ? smem_desc_mn_sw128(sb + 2048u * s) : smem_desc(sb + 2u * s * G::kSB, G::kSB, 128u);
 #pragma unroll
             for (int h = 0; h < MT; ++h) {
-              const uint64_t adesc = A_MN ? smem_desc(sa + (uint32_t)h * 16u * G::kSA + 256u * s, 128u, G::kSA)
+              const uint64_t adesc = A_MN ? smem_desc_mn_sw128(sa + (uint32_t)h * 16384u + 2048u * s)
                                           : smem_desc_sw128(sa + 32u * s);
               tc_mma(d0 + (uint32_t)h * 256u, adesc, bdesc, idesc, (first && s == 0) ? 0u : 1u);
             }
@@ -389,17 +402,17 @@ __global__ void __launch_bounds__(kRedElems *kRedGroups)
   if (grp == 0 && ok) grads[(long long)r * gld + c] += ((sums[0][t] + sums[1][t]) + sums[2][t]) + sums[3][t];
 }
 
-// A row-major BF16 matrix [rows][groups * 8] (row stride ld elements) as the
-// 3-D tensor (8 elements, rows, 8-element groups) whose box {8, box_rows,
-// box_groups} lands as the core-matrix image "(r, c) at (c/8)*(16*box_rows)
-// + r*16 + (c%8)*2"; groups past `groups` read as zeros.
-static int operand_map(CUtensorMap *m, const __nv_bfloat16 *X, long long ld, long long rows, long long groups,
-                       unsigned box_rows, unsigned box_groups) {
-  if (reinterpret_cast<uintptr_t>(X) % 16 != 0 || (ld * 2) % 16 != 0) return NERFGB_E_INVALID_ARG;
-  const unsigned long long dims[3] = {8, (unsigned long long)rows, (unsigned long long)groups};
-  const unsigned long long strides[2] = {(unsigned long long)(ld * 2), 16};
-  const unsigned box[3] = {8, box_rows, box_groups};
-  return encode_tensor_map_u16(m, X, 3, dims, strides, box);
+// An MN-major operand [rows][cols] (cols contiguous, row stride ld) as 3-D
+// (64 elements, rows, 64-element atoms; strides 2 B, ld * 2, 128 B) with the
+// 128-byte swizzle: boxes of kKc rows by box_atoms atoms (atoms past the
+// bounds zero-filled) land as smem_desc_mn_sw128 reads them.
+static int operand_map_mn_sw128(CUtensorMap *m, const __nv_bfloat16 *X, long long ld, long long rows, long long atoms,
+                                unsigned box_atoms) {
+  if (reinterpret_cast<uintptr_t>(X) % 16 != 0 || (ld * 2) % 16 != 0 || atoms < 1) return NERFGB_E_INVALID_ARG;
+  const unsigned long long dims[3] = {64, (unsigned long long)rows, (unsigned long long)atoms};
+  const unsigned long long strides[2] = {(unsigned long long)(ld * 2), 128};
+  const unsigned box[3] = {64, kKc, box_atoms};
+  return encode_tensor_map_u16(m, X, 3, dims, strides, box, true);
 }
 
 template <bool A_MN, bool B_MN, int MT, int EPI, bool B_RES = false>
@@ -418,7 +431,7 @@ static int launch(const Args &a, cudaStream_t st) {
   // A: MN-major [K rows][M cols] in kKc-row boxes of all MT*128 columns;
   // K-major [M rows][K cols] in 128-row boxes of kKc columns
   if (A_MN) {
-    rc = operand_map(&maps.a, a.A, a.lda, a.K, a.M / 8, kKc, MT * 128 / 8);
+    rc = operand_map_mn_sw128(&maps.a, a.A, a.lda, a.K, a.M / 64, MT * 128 / 64);
   } else {
     // K-major [M rows][K cols]: boxes of kKc columns (128 bytes) by 128 rows,
     // 128-byte swizzle (one TMA row request per 128 bytes)
@@ -432,7 +445,7 @@ static int launch(const Args &a, cudaStream_t st) {
   if (!B_RES) {
     static_assert(B_RES || B_MN, "a streamed B is MN-major");
     // [K rows][N cols] in kKc-row boxes of 256 columns (past N: zeros)
-    if ((rc = operand_map(&maps.b, a.B, a.ldb, a.K, a.N / 8, kKc, 256 / 8)) != NERFGB_OK) return rc;
+    if ((rc = operand_map_mn_sw128(&maps.b, a.B, a.ldb, a.K, a.N / 64, 256 / 64)) != NERFGB_OK) return rc;
   }
   kern<<<grid, kThreads, G::kSmem, st>>>(a, maps);
   return launch_status();
