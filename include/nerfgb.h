@@ -409,7 +409,7 @@ int nerfgb_mlp_backward(const void *packed, const float *acts, long long n_rows,
 /* nerfgb_mlp_forward with the BF16 pack that also writes the BF16 activation
  * tape: [n_rows][nerfgb_mlp_acts_floats_per_row()] BF16 values (uint16
  * bits) at the FP32 tape's columns, each the operand the next layer's GEMM
- * read. err_word: caller-zeroed device int32. */
+ * read; tape 16-byte aligned. err_word: caller-zeroed device int32. */
 int nerfgb_mlp_forward_train_bf16(const void *packed_bf16, const float *xyz,
                                   const float *dirs, long long n_rows,
                                   int rows_per_dir, float *rgb, float *sigma,

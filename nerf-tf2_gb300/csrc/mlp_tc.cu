@@ -18,7 +18,7 @@
 //   single CTA (FP8): tcgen05.mma.cta_group::1, M = 128 per sub-tile, every
 //     weight chunk streamed once per sub-tile, 8 epilogue warps per sub-tile.
 //
-// Warp roles (18 warps):
+// Warp roles (18 warps; 19 with the tape):
 //   warp 0      weight producer: bulk copies of KCH-row weight chunks into
 //               an NST-stage ring (full/empty mbarriers); pair: one thread in
 //               ring order issuing 2-SM tensor copies that complete on the
@@ -30,6 +30,9 @@
 //               read the accumulator (tcgen05.ld), add bias, apply ReLU,
 //               round to BF16 (or E4M3) and write the next layer's A operand;
 //               the sigma and rgb heads run in FP32.
+//   warp 18     (the pair kernel that writes the training tape only) one
+//               thread storing each written operand region to the tape by a
+//               3-D tensor store, then releasing the region to the epilogue.
 //
 // Shared memory (bytes, BF16): ring [0,64K) | encA [64K,80K) | encB
 // [80K,96K) | actA [96K,160K) | actB [160K,224K) | barriers, sigma partials.
